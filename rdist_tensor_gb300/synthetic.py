@@ -1,0 +1,143 @@
+"""Seeded synthetic sparse tensors with the shapes and value distributions of
+the sampled-ALS workloads (the reference ships no tensors; its FROSTT inputs
+are loaded from HDF5 files that are not part of the repository).
+
+All generators are deterministic functions of their seed.
+
+* ``planted_uniform``: coordinates uniform without replacement over the full
+  index space; values from a planted nonnegative CP model (|N(0,1)| factor
+  entries) plus Gaussian noise.  Workload "3-mode 2000^3, 2e6 nonzeros, planted
+  rank 10, noise variance 0.01".
+* ``zipf_tensor``: per-mode Zipf(alpha) coordinates truncated to the mode
+  range, deduplicated; values log-normal(0, 1) or N(0, 1) in float32.
+  Workloads "4-mode 5e6 x 5e6 x 2e4 x 1e3, 1e8 nonzeros, alpha 1.2" and
+  "5-mode 1e6 x 1e6 x 1e5 x 1e3 x 100, 2e8 nonzeros, alpha 1.1".
+* ``poisson_counts``: counts ~ Poisson(planted nonnegative CP with Gamma(0.5, 1)
+  factors) on a Zipf support (generalized-CP workload).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def planted_uniform(dims=(2000, 2000, 2000), nnz=2_000_000, rank=10, noise_var=0.01, seed=0):
+    rng = np.random.default_rng(seed)
+    dims = tuple(int(d) for d in dims)
+    total = int(np.prod(np.array(dims, dtype=np.float64)))
+    # Uniform without replacement: oversample, deduplicate, keep the first nnz
+    # in draw order.
+    lin = np.empty(0, dtype=np.int64)
+    while len(lin) < nnz:
+        extra = rng.integers(0, total, size=int((nnz - len(lin)) * 1.05) + 16, dtype=np.int64)
+        cand = np.concatenate([lin, extra])
+        _, first = np.unique(cand, return_index=True)
+        lin = cand[np.sort(first)]
+    lin = lin[:nnz]
+    idx = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.uint32)
+    A = [np.abs(rng.standard_normal((d, rank))) for d in dims]
+    model = np.ones((nnz, rank))
+    for k, Ak in enumerate(A):
+        model *= Ak[idx[:, k]]
+    vals = model.sum(axis=1) + rng.normal(0.0, np.sqrt(noise_var), size=nnz)
+    return np.array(dims, dtype=np.int64), np.ascontiguousarray(idx), np.ascontiguousarray(vals)
+
+
+def random_sparse(dims, nnz, seed=0):
+    """Uniform coordinates without replacement and U(0,1) values (small cases)."""
+    rng = np.random.default_rng(seed)
+    dims = tuple(int(d) for d in dims)
+    total = int(np.prod(dims))
+    lin = rng.choice(total, size=min(nnz, total), replace=False)
+    idx = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.uint32)
+    vals = rng.random(len(lin))
+    return np.array(dims, dtype=np.int64), np.ascontiguousarray(idx), np.ascontiguousarray(vals)
+
+
+def zipf_coords(rng, dim: int, alpha: float, n: int) -> np.ndarray:
+    """Zipf(alpha) over {0..dim-1} (rank k+1 has mass proportional to (k+1)^-alpha),
+    by inverse-CDF search on the exact truncated distribution."""
+    k = np.arange(1, dim + 1, dtype=np.float64)
+    cdf = np.cumsum(k ** (-alpha))
+    cdf /= cdf[-1]
+    u = rng.random(n)
+    return np.minimum(np.searchsorted(cdf, u, side="right"), dim - 1).astype(np.uint32)
+
+
+def zipf_tensor(dims, nnz, alpha=1.2, values="lognormal", seed=0, max_rounds=8):
+    """Per-mode Zipf coordinates, deduplicated; oversamples until ``nnz`` unique
+    coordinates are found or ``max_rounds`` rounds ran (the achieved count is
+    then smaller, and is what the returned arrays hold)."""
+    rng = np.random.default_rng(seed)
+    dims = [int(d) for d in dims]
+    N = len(dims)
+    bits = [max(1, int(np.ceil(np.log2(d)))) for d in dims]
+    have = np.zeros((0, N), dtype=np.uint32)
+    want = nnz
+    for _ in range(max_rounds):
+        m = int(want * 1.3) + 1024
+        cand = np.stack([zipf_coords(rng, d, alpha, m) for d in dims], axis=1)
+        allc = np.concatenate([have, cand])
+        keys = _pack(allc, bits)
+        _, first = np.unique(keys, axis=0, return_index=True)
+        have = allc[np.sort(first)]
+        if len(have) >= nnz:
+            break
+        want = nnz - len(have)
+    have = have[:nnz]
+    if values == "lognormal":
+        vals = rng.lognormal(0.0, 1.0, size=len(have)).astype(np.float32)
+    else:
+        vals = rng.standard_normal(len(have)).astype(np.float32)
+    return np.array(dims, dtype=np.int64), np.ascontiguousarray(have), vals
+
+
+def _pack(idx, bits):
+    """Packs coordinates into two uint64 words per row (most significant mode first)."""
+    hi = np.zeros(len(idx), dtype=np.uint64)
+    lo = np.zeros(len(idx), dtype=np.uint64)
+    for k, b in enumerate(bits):
+        b = np.uint64(b)
+        hi = (hi << b) | (lo >> (np.uint64(64) - b))
+        lo = (lo << b) | idx[:, k].astype(np.uint64)
+    return np.stack([hi, lo], axis=1)
+
+
+def poisson_counts(dims, nnz, rank=16, seed=0):
+    """Count tensor: Zipf(1.1) support, entries ~ Poisson(planted rank-`rank`
+    CP with Gamma(0.5, 1) factors) (zeros redrawn as 1 so every stored entry is
+    a nonzero)."""
+    rng = np.random.default_rng(seed)
+    d, idx, _ = zipf_tensor(dims, nnz, alpha=1.1, seed=seed + 1)
+    A = [rng.gamma(0.5, 1.0, size=(int(n), rank)) for n in d]
+    rate = np.ones((len(idx), rank))
+    for k, Ak in enumerate(A):
+        rate *= Ak[idx[:, k]]
+    lam = rate.sum(axis=1)
+    vals = rng.poisson(lam).astype(np.float32)
+    vals[vals == 0] = 1.0
+    return d, idx, vals, A
+
+
+def gaussian_factors(dims, R, seed=0):
+    """initialize_factors_gaussian_random (low_rank_tensor.hpp:35-41,
+    distmat.hpp:153-168, 85-138): N(0,1) entries, columns normalised."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for d in dims:
+        U = rng.standard_normal((int(d), R))
+        U /= np.sqrt((U * U).sum(axis=0))[None, :]
+        out.append(np.ascontiguousarray(U))
+    return out
+
+
+def deterministic_factors(dims, R):
+    """initialize_factors_deterministic (distmat.hpp:140-151) at one rank:
+    U[i, j] = cos(i * R + j), columns normalised."""
+    out = []
+    for d in dims:
+        i = np.arange(int(d), dtype=np.float64)[:, None]
+        j = np.arange(R, dtype=np.float64)[None, :]
+        U = np.cos(i * R + j)
+        U /= np.sqrt((U * U).sum(axis=0))[None, :]
+        out.append(np.ascontiguousarray(U))
+    return out
