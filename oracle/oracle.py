@@ -447,3 +447,29 @@ def sts_uniform_stream(seed: int, N: int, J: int, steps: int) -> list:
                 pos += J
         out.append(u)
     return out
+
+
+def exact_als_sweep(ora: "OracleALS", sweeps: int = 1):
+    """ExactALS (exact_als.hpp:90-143) at one rank, `sweeps` rounds, applied to
+    the oracle's factors in place (decompose.py:82-96 runs one as the
+    "-p exact" preprocessing).  Keeps its own Gram matrices, as the reference
+    does, and ends by refreshing the sampler."""
+    N, R = ora.N, ora.R
+    grams = [gram(U) for U in ora.factors]
+    for _ in range(sweeps):
+        for n in range(N):
+            chain = np.ones((R, R))
+            for k in range(N):
+                if k != n:
+                    chain = chain * grams[k]
+            Phi = pinv_square(chain)
+            Us = [np.ascontiguousarray(U) for U in ora.factors]
+            arr = (ctypes.c_void_p * N)(*[U.ctypes.data for U in Us])
+            M = np.zeros((ora.dims[n], R))
+            lib().or_exact_mttkrp(N, n, R, ora.idx.shape[0], _p(ora.idx), _p(ora.val), arr, ora.dims[n], _p(M))
+            U, norms = renormalize(M @ Phi)
+            ora.factors[n] = U
+            ora.sigma = norms
+            grams[n] = gram(U)
+    for n in range(N):
+        ora.update_sampler(n)

@@ -1,0 +1,16 @@
+// Small dense FP64 R x R kernels (eigendecomposition, pseudo-inverse).
+#pragma once
+#include "common.cuh"
+
+namespace exafac {
+
+size_t syev_smem_bytes(int R);
+size_t syev_scratch_doubles(int R, int batch);
+
+// Batched symmetric eigendecomposition / pseudo-inverse, one CTA per matrix
+// (matrix b at A + b * a_stride, upper triangle read).  V, lam, pinv may be
+// null.  vt_scratch: syev_scratch_doubles(R, batch) doubles.
+int launch_syev(int R, const double* A, int64_t a_stride, int batch, double* V, double* lam, int64_t v_stride,
+                double* pinv, double tol, double* vt_scratch, cudaStream_t stream);
+
+}  // namespace exafac

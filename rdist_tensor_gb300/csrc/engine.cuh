@@ -1,0 +1,148 @@
+// Sampled-ALS session state and the kernels of one step.
+//
+// Data layout in HBM (all inside the caller's workspace):
+//   idx      nnz x N uint32    coordinates as given (fit, exact MTTKRP)
+//   vals     nnz float64       preprocessed values
+//   per mode n (SortIdxLookup, sort_lookup.hpp:37-102):
+//     rows_n  nnz uint32       mode-n coordinate, nonzeros ordered by the
+//                              packed key of the other coordinates
+//     vals_n  nnz float64      values in the same order
+//     slots_n hash table       fiber key -> [start, start + len) in rows_n
+//   sampler state per mode (scores + CDF for CP-ARLS-LEV; packed Gram tree +
+//   Gram for STS-CP), step scratch sized for J_max samples and nnz hits.
+#pragma once
+#include "common.cuh"
+#include "tree.cuh"
+
+namespace exafac {
+
+constexpr uint32_t kEmpty = 0xffffffffu;
+constexpr int64_t kExactCdfMax = 16384;  // CDFs up to this length are summed strictly in order
+
+struct Slot1 {
+    unsigned long long key;
+    unsigned int start, len;
+};
+struct Slot2 {
+    unsigned long long lo, hi;
+    unsigned int start, len;
+    unsigned long long pad;
+};
+
+struct Lookup {
+    uint32_t* rows = nullptr;
+    double* vals = nullptr;
+    void* slots = nullptr;  // Slot1[nslots] or Slot2[nslots]
+    int64_t nslots = 0;     // power of two
+    int kw = 1;             // key words
+    KeySpec spec;
+};
+
+struct Session {
+    exafac_als_config cfg;
+    int N = 0, R = 0, P = 0;
+    int64_t dims[kMaxModes] = {0};
+    int64_t nnz = 0, Jmax = 0, Imax = 0;
+    Arena arena;
+    bool initialized = false;
+    double tensor_norm = 0.0;
+    exafac_factors F;
+
+    uint32_t* idx = nullptr;
+    double* vals = nullptr;
+    Lookup look[kMaxModes];
+
+    // CP-ARLS-LEV state
+    double* scores[kMaxModes] = {nullptr};
+    double* cdf[kMaxModes] = {nullptr};
+    double* cdf_total = nullptr;  // [N] sum of the scores (log-weight numerator)
+    // STS-CP state
+    TreeShape rtree[kMaxModes];
+    double* treeG[kMaxModes] = {nullptr};
+    TreeShape etree;
+    double* eigG = nullptr;    // [N] eigen trees, etree.node_count * P each
+    double* gram = nullptr;    // [N] R x R factor Grams (full)
+    double* chain = nullptr;   // [N] R x R suffix Hadamard products
+    double* Emat = nullptr;    // [N+1] R x R scaled eigenvector rows
+    double* eigV = nullptr;    // [N+1] R x R eigenvectors
+    double* eigL = nullptr;    // [N+1] R eigenvalues
+    double* Phi = nullptr;     // R x R (full)
+    double* PhiP = nullptr;    // packed
+    double* vt = nullptr;      // Jacobi scratch, N+1 matrices
+
+    // nonzero-row tracking per factor (rows outside the list are zero)
+    bool dense[kMaxModes] = {false};
+    uint32_t* nzrows[kMaxModes] = {nullptr};
+    int64_t* nzcount = nullptr;  // [N]
+
+    // step scratch
+    double* uni = nullptr;  // N x 2 x Jmax
+    uint32_t* samples = nullptr;
+    double* weights = nullptr;
+    int64_t dtab = 0;  // dedup table size (power of two)
+    int32_t* d_owner = nullptr;
+    int32_t* d_minj = nullptr;
+    int32_t* d_count = nullptr;
+    int32_t* slot_of = nullptr;
+    uint32_t* flags = nullptr;
+    int64_t* pos = nullptr;
+    uint32_t* sd = nullptr;
+    double* wd = nullptr;
+    int64_t* counters = nullptr;  // [0] J_u, [1] H, [2] touched, [3..] scratch
+    double* D = nullptr;          // Jmax x R design rows (scaled twice)
+    double* part = nullptr;       // Gram partials
+    int64_t part_rows = 0;
+    double* dgram = nullptr;      // R x R design Gram
+    double* dpinv = nullptr;      // R x R its pseudo-inverse
+    uint32_t* f_start = nullptr;
+    uint32_t* f_len = nullptr;
+    int64_t* f_off = nullptr;
+    uint32_t* rowcnt = nullptr;   // Imax
+    uint32_t* rowfill = nullptr;  // Imax
+    int64_t* rowoff = nullptr;    // Imax
+    uint32_t* hit_j = nullptr;    // nnz
+    double* hit_val = nullptr;    // nnz
+    uint32_t* touched = nullptr;  // Imax
+    double* ugram = nullptr;      // R x R
+    double* ngram = nullptr;      // R x R normalised factor Gram
+    double* upinv = nullptr;      // R x R
+    double* fitpart = nullptr;
+    DeviceStatus* status = nullptr;
+    void* scan_sc = nullptr;
+    int64_t* dims_dev = nullptr;  // [kMaxModes]
+    double* Mexact = nullptr;     // Imax x R (exact MTTKRP)
+    double* scal = nullptr;       // [8] device scalars (norms, fit terms)
+
+    uint64_t seed = 0x5eed;
+    uint64_t counter = 0;
+};
+
+// ---- sampler kernels (sampler_kernels.cu)
+int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st);
+int arls_build_cdf(Session& s, int k, cudaStream_t st);
+int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStream_t st);
+int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* perms, cudaStream_t st);
+int sts_compute_M(Session& s, int n, cudaStream_t st);
+int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
+
+// ---- step kernels (step_kernels.cu)
+int dedup(Session& s, int n, int64_t J, cudaStream_t st);
+int design_gram(Session& s, int n, int64_t J, cudaStream_t st);
+int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist, const int64_t* count_dev,
+              double* out_full, cudaStream_t st);
+int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st);
+int spmm_solve(Session& s, int n, cudaStream_t st);
+int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStream_t st);
+int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st);
+int zero_factor_rows(Session& s, int n, cudaStream_t st);
+int fit_residual(Session& s, double* out_dev, cudaStream_t st);
+int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st);
+int matmul_rows_sym(Session& s, const double* M, const double* Phi, double* U, int64_t rows, cudaStream_t st);
+int chain_gram(Session& s, int skip, double* out, cudaStream_t st);
+
+// ---- setup kernels (setup_kernels.cu)
+size_t setup_bytes(const Session& s);
+int build_lookup(Session& s, int n, void* setup, size_t setup_bytes, cudaStream_t st);
+int preprocess_values(Session& s, const double* vals_in, cudaStream_t st);
+
+}  // namespace exafac

@@ -1,0 +1,441 @@
+// Samplers on the GPU: the session's Philox stream, CP-ARLS-LEV (leverage
+// scores, discrete CDF, inverse-CDF draws) and STS-CP (computeM, eigen trees,
+// fused warp-per-sample descent through the eigen and row trees).
+#include "dense.cuh"
+#include "engine.cuh"
+#include "prims.cuh"
+
+namespace exafac {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter-based uniforms.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        unsigned lo0 = c.x * 0xD2511F53u, hi0 = __umulhi(c.x, 0xD2511F53u);
+        unsigned lo1 = c.z * 0xCD9E8D57u, hi1 = __umulhi(c.z, 0xCD9E8D57u);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+__device__ __forceinline__ double u53(unsigned a, unsigned b) {
+    unsigned long long x = ((unsigned long long)a << 32) | b;
+    return (double)(x >> 11) * 0x1.0p-53;
+}
+
+__global__ void philox_uniform_kernel(double* out, int64_t count, uint64_t seed, uint64_t ctr) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i = 2 * t;
+    if (i >= count) return;
+    uint4 c = make_uint4((unsigned)t, (unsigned)(t >> 32), (unsigned)ctr, (unsigned)(ctr >> 32));
+    uint4 r = philox4x32_10(c, make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    out[i] = u53(r.x, r.y);
+    if (i + 1 < count) out[i + 1] = u53(r.z, r.w);
+}
+
+int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st) {
+    if (count <= 0) return EXAFAC_OK;
+    int64_t threads = (count + 1) / 2;
+    philox_uniform_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(out, count, s.seed, s.counter++);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CP-ARLS-LEV
+// ---------------------------------------------------------------------------
+
+// libstdc++ discrete_distribution::param_type::_M_initialize
+// (bits/random.tcc:2657-2678) for short weight vectors, strictly in order:
+// sequential sum, p_i = w_i / sum, sequential partial sums, last = 1.0.
+__global__ void cdf_sequential_kernel(const double* __restrict__ w, int64_t n, double* __restrict__ cdf,
+                                      double* __restrict__ total) {
+    __shared__ double sum_sh;
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int64_t i = 0; i < n; i++) sum += w[i];
+        sum_sh = sum;
+        *total = sum;
+    }
+    __syncthreads();
+    const double sum = sum_sh;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) cdf[i] = w[i] / sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double run = 0.0;
+        for (int64_t i = 0; i < n; i++) {
+            run += cdf[i];
+            cdf[i] = run;
+        }
+        cdf[n - 1] = 1.0;
+    }
+}
+
+// Long weight vectors: blockwise inclusive scan S, cdf_i = S_i / S_n, last = 1.
+__global__ void cdf_normalize_kernel(double* __restrict__ cdf, int64_t n, const double* __restrict__ total) {
+    const double t = *total;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        cdf[i] = (i == n - 1) ? 1.0 : cdf[i] / t;
+}
+
+int arls_build_cdf(Session& s, int k, cudaStream_t st) {
+    const int64_t n = s.dims[k];
+    if (n < 2) {
+        // A one-row distribution always yields row 0 and consumes no draw.
+        cdf_sequential_kernel<<<1, 32, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k);
+        EXAFAC_CHECK_LAUNCH();
+        return EXAFAC_OK;
+    }
+    if (n <= kExactCdfMax) {
+        cdf_sequential_kernel<<<1, 256, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k);
+        EXAFAC_CHECK_LAUNCH();
+        return EXAFAC_OK;
+    }
+    EXAFAC_TRY(scan_inclusive_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st));
+    int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
+    cdf_normalize_kernel<<<blocks, 256, 0, st>>>(s.cdf[k], n, s.cdf_total + k);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// compute_DAGAT (common.h:727-746) row by row: l_r = u_r^T P u_r with
+// y = P u (dsymm) then the dot product.  Warp per row.
+__global__ void leverage_kernel(int R, const double* __restrict__ U, const double* __restrict__ Pm, int64_t rows,
+                                const uint32_t* __restrict__ list, const int64_t* __restrict__ count_dev,
+                                double* __restrict__ scores) {
+    extern __shared__ double sm[];
+    double* Psm = sm;
+    const int warps = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* usm = Psm + R * R + w * R;
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) Psm[e] = Pm[e];
+    __syncthreads();
+    const int64_t cnt = list ? *count_dev : rows;
+    for (int64_t i = (int64_t)blockIdx.x * warps + w; i < cnt; i += (int64_t)gridDim.x * warps) {
+        const int64_t r = list ? (int64_t)list[i] : i;
+        for (int a = lane; a < R; a += 32) usm[a] = U[r * R + a];
+        __syncwarp();
+        double acc = 0.0;
+        for (int a = lane; a < R; a += 32) {
+            double y = 0.0;
+            for (int b = 0; b < R; b++) y = fma(Psm[a * R + b], usm[b], y);
+            acc = fma(usm[a], y, acc);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) scores[r] = acc;
+        __syncwarp();
+    }
+}
+
+int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStream_t st) {
+    const int R = s.R;
+    const int warps = 8;
+    size_t smem = sizeof(double) * ((size_t)R * R + warps * R);
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(leverage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t rows = all_rows ? s.dims[k] : s.dims[k];
+    int blocks = (int)std::min<int64_t>(ceil_div(rows, warps), 152 * 16);
+    leverage_kernel<<<blocks, warps * 32, smem, st>>>(R, s.F.U[k], pinv, s.dims[k], all_rows ? nullptr : s.touched,
+                                                      s.counters + 2, s.scores[k]);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+struct ArlsModes {
+    const double* cdf[kMaxModes];
+    const double* scores[kMaxModes];
+    int64_t dims[kMaxModes];
+};
+
+// CP_ARLS_LEV::KRPDrawSamples + draw_leverage_score_samples
+// (cp_arls_lev.hpp:36-163) at one rank, thread per sample: the draw is the
+// first CDF entry >= u (lower_bound), the log weight log(sum) - log(l_idx)
+// is added mode by mode to -log J, then exponentiated.
+__global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const double* __restrict__ total,
+                                 const double* __restrict__ uni, const uint32_t* __restrict__ perms,
+                                 uint32_t* __restrict__ samples, double* __restrict__ weights,
+                                 DeviceStatus* status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J) return;
+    double w = 0.0 - log((double)J);
+    for (int k = 0; k < N; k++) {
+        if (k == n) continue;
+        const int64_t I = m.dims[k];
+        int64_t src = perms ? (int64_t)perms[(int64_t)k * J + t] : t;
+        if (src >= J) {
+            report(status, EXAFAC_ERR_DEVICE, 3, src, J);
+            src = t;
+        }
+        int64_t idx = 0;
+        if (I >= 2) {
+            const double u = uni[(int64_t)k * J + src];
+            const double* cdf = m.cdf[k];
+            int64_t lo = 0, hi = I;
+            while (lo < hi) {
+                int64_t mid = (lo + hi) >> 1;
+                if (cdf[mid] < u) lo = mid + 1;
+                else hi = mid;
+            }
+            idx = lo < I ? lo : I - 1;
+        }
+        const double lw = 0.0 + (log(total[k]) - log(m.scores[k][idx]));
+        samples[t * N + k] = (uint32_t)idx;
+        w += lw;
+    }
+    samples[t * N + n] = 0;
+    weights[t] = exp(w);
+}
+
+int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* perms, cudaStream_t st) {
+    ArlsModes m;
+    for (int k = 0; k < kMaxModes; k++) {
+        m.cdf[k] = k < s.N ? s.cdf[k] : nullptr;
+        m.scores[k] = k < s.N ? s.scores[k] : nullptr;
+        m.dims[k] = k < s.N ? s.dims[k] : 0;
+    }
+    arls_draw_kernel<<<(unsigned)ceil_div(J, 256), 256, 0, st>>>(s.N, n, J, m, s.cdf_total, uni, perms, s.samples,
+                                                                  s.weights, s.status);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// STS-CP
+// ---------------------------------------------------------------------------
+
+// STS_CP::computeM part 1 (sts_cp.hpp:81-102): suffix Hadamard products of
+// the factor Grams over the modes != n; chain[n] is cleared.
+__global__ void sts_chain_kernel(int N, int n, int R, const double* __restrict__ gram, double* __restrict__ chain) {
+    const int R2 = R * R;
+    for (int e = threadIdx.x; e < R2; e += blockDim.x) {
+        double last = 1.0;
+        for (int k = N - 1; k >= 0; k--) {
+            if (k == n) {
+                chain[(int64_t)k * R2 + e] = 0.0;
+                continue;
+            }
+            last = gram[(int64_t)k * R2 + e] * last;
+            chain[(int64_t)k * R2 + e] = last;
+        }
+    }
+}
+
+// computeM part 2 (sts_cp.hpp:118-153): W[:, R-1-v] = v-th eigenvector /
+// sqrt(lambda_v) (dropped at lambda_v <= 1e-8), Phi = W W^T, the rows of W^T
+// become E[N], and chain[k] *= Phi for k >= 1.
+__global__ void sts_phi_kernel(int N, int n, int R, const double* __restrict__ V0, const double* __restrict__ L0,
+                               double* __restrict__ chain, double* __restrict__ E, double* __restrict__ Phi,
+                               double* __restrict__ PhiP) {
+    extern __shared__ double W[];
+    const int R2 = R * R;
+    for (int e = threadIdx.x; e < R2; e += blockDim.x) {
+        int u = e / R, v = e % R;
+        double lam = L0[v];
+        W[u * R + (R - 1 - v)] = lam > 1e-8 ? V0[u * R + v] / sqrt(lam) : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R2; e += blockDim.x) {
+        int a = e / R, b = e % R;
+        E[(int64_t)N * R2 + a * R + b] = W[b * R + a];
+        double acc = 0.0;
+        for (int v = 0; v < R; v++) acc = fma(W[a * R + v], W[b * R + v], acc);
+        Phi[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R2; e += blockDim.x) {
+        int a = e / R, b = e % R;
+        double p = Phi[a <= b ? a * R + b : b * R + a];
+        if (a <= b) PhiP[packed_index(R, a, b)] = p;
+        for (int k = N - 1; k > 0; k--)
+            if (k != n) chain[(int64_t)k * R2 + e] *= p;
+    }
+}
+
+// computeM part 3 (sts_cp.hpp:156-176): E[k] row v = sqrt(lambda_v) * v-th
+// eigenvector of chain[k] (k = 1..N-1, k != n).
+__global__ void sts_emat_kernel(int N, int n, int R, const double* __restrict__ V, const double* __restrict__ L,
+                                double* __restrict__ E) {
+    const int R2 = R * R;
+    for (int k = 1; k < N; k++) {
+        if (k == n) continue;
+        for (int e = threadIdx.x; e < R2; e += blockDim.x) {
+            int v = e / R, u = e % R;
+            E[(int64_t)k * R2 + v * R + u] = V[(int64_t)k * R2 + u * R + v] * sqrt(L[(int64_t)k * R + v]);
+        }
+    }
+}
+
+// Eigen tree of each sampled mode k (sts_cp.hpp:179-187): PartitionTree over
+// the rows of E[next(k)] with one row per leaf, then every node times the
+// Gram of U_k.  One CTA per mode.
+__global__ void sts_eigen_tree_kernel(int N, int n, int R, TreeShape t, const double* __restrict__ E,
+                                      const double* __restrict__ gram, double* __restrict__ eigG) {
+    const int k = blockIdx.x;
+    if (k == n || k >= N) return;
+    int nxt = k + 1;
+    if (nxt == n) nxt++;
+    if (nxt > N) nxt = N;
+    const int P = packed_size(R);
+    const double* Ek = E + (int64_t)nxt * R * R;
+    double* G = eigG + (int64_t)k * t.node_count * P;
+    const int64_t first_leaf = t.node_count - t.leaf_count;
+    for (int64_t i = threadIdx.x; i < t.leaf_count * P; i += blockDim.x) {
+        int64_t li = i / P;
+        int e = (int)(i % P);
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        int b = a + rem;
+        int64_t v = tree_leaf_idx(t, first_leaf + li);
+        G[(first_leaf + li) * P + e] = Ek[v * R + a] * Ek[v * R + b];
+    }
+    __syncthreads();
+    int64_t start = t.nodes_before_lfill, end = first_leaf;
+    for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
+        for (int64_t i = threadIdx.x; i < (end - start) * P; i += blockDim.x) {
+            int64_t c = start + i / P;
+            int e = (int)(i % P);
+            G[c * P + e] = G[(2 * c + 1) * P + e] + G[(2 * c + 2) * P + e];
+        }
+        __syncthreads();
+        end = start;
+        start = ((start + 1) / 2) - 1;
+    }
+    const double* Gk = gram + (int64_t)k * R * R;
+    for (int64_t i = threadIdx.x; i < t.node_count * P; i += blockDim.x) {
+        int e = (int)(i % P);
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        G[i] *= Gk[a * R + a + rem];
+    }
+}
+
+int sts_compute_M(Session& s, int n, cudaStream_t st) {
+    const int N = s.N, R = s.R, R2 = R * R;
+    sts_chain_kernel<<<1, 256, 0, st>>>(N, n, R, s.gram, s.chain);
+    EXAFAC_CHECK_LAUNCH();
+    const int first = (n == 0) ? 1 : 0;
+    EXAFAC_TRY(launch_syev(R, s.chain + (int64_t)first * R2, 0, 1, s.eigV, s.eigL, 0, nullptr, 0.0, s.vt, st));
+    sts_phi_kernel<<<1, 256, sizeof(double) * R2, st>>>(N, n, R, s.eigV, s.eigL, s.chain, s.Emat, s.Phi, s.PhiP);
+    EXAFAC_CHECK_LAUNCH();
+    if (N > 1) {
+        // matrices 1..N-1 (chain[n] was cleared, its decomposition is trivial)
+        EXAFAC_TRY(launch_syev(R, s.chain + R2, R2, N - 1, s.eigV + R2, s.eigL + R, R2, nullptr, 0.0, s.vt, st));
+    }
+    sts_emat_kernel<<<1, 256, 0, st>>>(N, n, R, s.eigV, s.eigL, s.Emat);
+    EXAFAC_CHECK_LAUNCH();
+    sts_eigen_tree_kernel<<<N, 256, 0, st>>>(N, n, R, s.etree, s.Emat, s.gram, s.eigG);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+struct StsModes {
+    const double* treeG[kMaxModes];
+    const double* U[kMaxModes];
+    TreeShape rt[kMaxModes];
+    int next[kMaxModes];
+};
+
+// STS_CP::KRPDrawSamples (sts_cp.hpp:203-300) at one rank, warp per sample:
+// for each sampled mode k, an eigen-tree descent driven by h picks v and sets
+// scaled_h = h * E[next(k)][v]; a row-tree descent driven by scaled_h picks
+// the row and sets h *= U_k[row] (exact_leverage_tree.hpp:293-496 with no
+// distributed levels).  Weight = R / (J h^T Phi h).
+__global__ void sts_draw_kernel(int N, int n, int R, int64_t J, StsModes m, TreeShape et,
+                                const double* __restrict__ eigG, const double* __restrict__ E,
+                                const double* __restrict__ PhiP, const double* __restrict__ uni,
+                                uint32_t* __restrict__ samples, double* __restrict__ weights,
+                                DeviceStatus* status) {
+    extern __shared__ unsigned char smraw[];
+    const int P = packed_size(R);
+    const int warps = blockDim.x >> 5;
+    unsigned short* pa = reinterpret_cast<unsigned short*>(smraw);
+    unsigned short* pb = pa + P;
+    double* base = reinterpret_cast<double*>(smraw + align_up(2 * P * sizeof(unsigned short), 16));
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* h = base + (size_t)w * (P + 3 * R);
+    double* sh = h + R;
+    double* q = sh + R;
+    double* z = q + R;
+    block_build_pairs(R, pa, pb);
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * warps + w; i < J; i += (int64_t)gridDim.x * warps) {
+        for (int r = lane; r < R; r += 32) h[r] = 1.0;
+        __syncwarp();
+        for (int k = 0; k < N; k++) {
+            if (k == n) continue;
+            for (int r = lane; r < R; r += 32) sh[r] = h[r];
+            __syncwarp();
+            // Eigen tree: descent by h, leaf v, scaled_h = h * E_next[v].
+            const double* Ek = E + (int64_t)m.next[k] * R * R;
+            warp_build_z(R, h, pa, pb, z);
+            int64_t v = warp_descend(et, R, eigG + (int64_t)k * et.node_count * P, Ek, z, h, q,
+                                     uni[((int64_t)k * 2 + 0) * J + i]);
+            if (v >= R) {
+                report(status, EXAFAC_ERR_DEVICE, 1, v, R);
+                v = R - 1;
+            }
+            if (lane == 0) samples[i * N + n] = (uint32_t)v;
+            for (int r = lane; r < R; r += 32) sh[r] *= Ek[v * R + r];
+            __syncwarp();
+            // Row tree: descent by scaled_h, row, h *= U_k[row].
+            warp_build_z(R, sh, pa, pb, z);
+            int64_t row = warp_descend(m.rt[k], R, m.treeG[k], m.U[k], z, sh, q, uni[((int64_t)k * 2 + 1) * J + i]);
+            if (row >= m.rt[k].n) {
+                report(status, EXAFAC_ERR_DEVICE, 2, row, m.rt[k].n);
+                row = m.rt[k].n - 1;
+            }
+            if (lane == 0) samples[i * N + k] = (uint32_t)row;
+            for (int r = lane; r < R; r += 32) h[r] *= m.U[k][row * R + r];
+            __syncwarp();
+        }
+        warp_build_z(R, h, pa, pb, z);
+        double hq = warp_quad(R, z, PhiP);
+        if (lane == 0) weights[i] = (double)R / (hq * (double)J);
+        __syncwarp();
+    }
+}
+
+int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
+    const int N = s.N, R = s.R, P = s.P;
+    StsModes m;
+    for (int k = 0; k < kMaxModes; k++) {
+        if (k < N) {
+            m.treeG[k] = s.treeG[k];
+            m.U[k] = s.F.U[k];
+            m.rt[k] = s.rtree[k];
+            int nx = k + 1;
+            if (nx == n) nx++;
+            if (nx > N) nx = N;
+            m.next[k] = nx;
+        } else {
+            m.treeG[k] = nullptr;
+            m.U[k] = nullptr;
+            m.next[k] = 0;
+        }
+    }
+    int warps = 8;
+    size_t smem = align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * (P + 3 * R);
+    while (smem > 200 * 1024 && warps > 1) {
+        warps /= 2;
+        smem = align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * (P + 3 * R);
+    }
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(sts_draw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t blocks = std::min<int64_t>(ceil_div(J, warps), 152 * 16);
+    sts_draw_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), warps * 32, smem, st>>>(
+        N, n, R, J, m, s.etree, s.eigG, s.Emat, s.PhiP, uni, s.samples, s.weights, s.status);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+}  // namespace exafac

@@ -1,0 +1,603 @@
+// Kernels of one sampled-ALS step after the draw (accumulator_stationary.hpp:
+// 173-294 at one rank): deduplication, design rows + Gram, fiber lookup,
+// counting sort of the hits by output row, sampled MTTKRP fused with the
+// R x R solve, column renormalisation; plus the exact fit and exact MTTKRP.
+#include "dense.cuh"
+#include "engine.cuh"
+#include "prims.cuh"
+
+namespace exafac {
+
+constexpr int kGramRows = 32;  // rows per block in the Gram partial kernels
+
+struct FactorPtrs {
+    const double* U[kMaxModes];
+};
+
+static FactorPtrs factor_ptrs(const Session& s) {
+    FactorPtrs f;
+    for (int k = 0; k < kMaxModes; k++) f.U[k] = k < s.N ? s.F.U[k] : nullptr;
+    return f;
+}
+
+static int grid_cap(int64_t work, int threads, int64_t cap = 152 * 16) {
+    int64_t b = ceil_div(work, threads);
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+// ---------------------------------------------------------------------------
+// Deduplication (deduplicate_design_matrix, als_optimizer.hpp:130-206).
+// Unique rows are identified by a hash table keyed on the packed coordinates
+// of the modes != n; each unique row is represented by its first occurrence,
+// so the output order is the order of first occurrence.  Weight = the
+// representative's weight times the multiplicity.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool keys_equal(Key128 a, Key128 b) { return a.lo == b.lo && a.hi == b.hi; }
+
+__global__ void dedup_insert_kernel(KeySpec spec, int64_t J, const uint32_t* __restrict__ samples, int64_t mask,
+                                    int32_t* owner, int32_t* minj, int32_t* count, int32_t* __restrict__ slot_of) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J) return;
+    const Key128 key = pack_key(spec, samples + j * spec.N);
+    int64_t h = (int64_t)(hash_key(key) & (uint64_t)mask);
+    for (int64_t probe = 0; probe <= mask; probe++) {
+        int32_t o = atomicCAS(&owner[h], -1, (int32_t)j);
+        if (o == -1 || keys_equal(pack_key(spec, samples + (int64_t)o * spec.N), key)) break;
+        h = (h + 1) & mask;
+    }
+    atomicMin(&minj[h], (int32_t)j);
+    atomicAdd(&count[h], 1);
+    slot_of[j] = (int32_t)h;
+}
+
+__global__ void dedup_flag_kernel(int64_t J, const int32_t* __restrict__ minj, const int32_t* __restrict__ slot_of,
+                                  uint32_t* __restrict__ flags) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J) return;
+    flags[j] = minj[slot_of[j]] == (int32_t)j ? 1u : 0u;
+}
+
+__global__ void dedup_compact_kernel(int N, int64_t J, const uint32_t* __restrict__ flags,
+                                     const int64_t* __restrict__ pos, const int32_t* __restrict__ slot_of,
+                                     const int32_t* __restrict__ count, const uint32_t* __restrict__ samples,
+                                     const double* __restrict__ weights, uint32_t* __restrict__ sd,
+                                     double* __restrict__ wd) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J || !flags[j]) return;
+    const int64_t p = pos[j];
+    for (int k = 0; k < N; k++) sd[p * N + k] = samples[j * N + k];
+    wd[p] = weights[j] * (double)count[slot_of[j]];
+}
+
+int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.d_owner, 0xff, sizeof(int32_t) * s.dtab, st));
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.d_minj, 0x7f, sizeof(int32_t) * s.dtab, st));
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.d_count, 0, sizeof(int32_t) * s.dtab, st));
+    const unsigned blocks = (unsigned)ceil_div(J, 256);
+    dedup_insert_kernel<<<blocks, 256, 0, st>>>(s.look[n].spec, J, s.samples, s.dtab - 1, s.d_owner, s.d_minj,
+                                                s.d_count, s.slot_of);
+    dedup_flag_kernel<<<blocks, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags);
+    EXAFAC_CHECK_LAUNCH();
+    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, J, s.counters + 0, s.scan_sc, st));
+    dedup_compact_kernel<<<blocks, 256, 0, st>>>(s.N, J, s.flags, s.pos, s.slot_of, s.d_count, s.samples, s.weights,
+                                                 s.sd, s.wd);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Gram partials and their deterministic reduction.
+// ---------------------------------------------------------------------------
+__global__ void gram_reduce_kernel(const double* __restrict__ part, int64_t nblk, int R, double* __restrict__ out) {
+    __shared__ double red[256];
+    const int P = packed_size(R);
+    const int e = blockIdx.x;
+    if (e >= P) return;
+    double acc = 0.0;
+    for (int64_t b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[b * P + e];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        int b = a + rem;
+        out[a * R + b] = red[0];
+        out[b * R + a] = red[0];
+    }
+}
+
+// Gram of rows of A (all `rows`, or the first *count_dev entries of rowlist).
+__global__ void gram_partial_kernel(int R, const double* __restrict__ A, int64_t rows, const uint32_t* __restrict__ list,
+                                    const int64_t* __restrict__ count_dev, double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int P = packed_size(R);
+    const int64_t cnt = list ? *count_dev : rows;
+    const int64_t base = (int64_t)blockIdx.x * kGramRows;
+    for (int e = threadIdx.x; e < kGramRows * R; e += blockDim.x) {
+        int lr = e / R, c = e % R;
+        int64_t i = base + lr;
+        double v = 0.0;
+        if (i < cnt) {
+            int64_t r = list ? (int64_t)list[i] : i;
+            v = A[r * R + c];
+        }
+        sm[lr * R + c] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        int b = a + rem;
+        double acc = 0.0;
+        for (int lr = 0; lr < kGramRows; lr++) acc = fma(sm[lr * R + a], sm[lr * R + b], acc);
+        part[(int64_t)blockIdx.x * P + e] = acc;
+    }
+}
+
+int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist, const int64_t* count_dev,
+              double* out_full, cudaStream_t st) {
+    const int R = s.R;
+    int64_t nblk = std::max<int64_t>(1, ceil_div(rows, kGramRows));
+    if (nblk > s.part_rows) {
+        set_error("gram_rows: partial buffer too small");
+        return EXAFAC_ERR_WORKSPACE;
+    }
+    gram_partial_kernel<<<(unsigned)nblk, 128, sizeof(double) * kGramRows * R, st>>>(R, A, rows, rowlist, count_dev,
+                                                                                     s.part);
+    gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, out_full);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Design rows (accumulator_stationary.hpp:212-249): D_j = prod_{k!=n}
+// U_k[s_jk] (mode order, from 1.0), D_j *= sqrt(w_j); Gram of these rows;
+// the rows used by the MTTKRP are scaled by sqrt(w_j) once more.
+// ---------------------------------------------------------------------------
+__global__ void design_kernel(int N, int n, int R, const int64_t* __restrict__ ju_dev, const uint32_t* __restrict__ sd,
+                              const double* __restrict__ wd, FactorPtrs f, double* __restrict__ D,
+                              double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int P = packed_size(R);
+    const int64_t ju = *ju_dev;
+    const int64_t base = (int64_t)blockIdx.x * kGramRows;
+    for (int e = threadIdx.x; e < kGramRows * R; e += blockDim.x) {
+        int lr = e / R, c = e % R;
+        int64_t j = base + lr;
+        double v = 0.0;
+        if (j < ju) {
+            double d = 1.0;
+            for (int k = 0; k < N; k++) {
+                if (k == n) continue;
+                d *= f.U[k][(int64_t)sd[j * N + k] * R + c];
+            }
+            const double sw = sqrt(wd[j]);
+            d *= sw;
+            v = d;
+            D[j * R + c] = d * sw;
+        }
+        sm[lr * R + c] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        int b = a + rem;
+        double acc = 0.0;
+        for (int lr = 0; lr < kGramRows; lr++) acc = fma(sm[lr * R + a], sm[lr * R + b], acc);
+        part[(int64_t)blockIdx.x * P + e] = acc;
+    }
+}
+
+int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
+    const int R = s.R;
+    int64_t nblk = std::max<int64_t>(1, ceil_div(J, kGramRows));
+    design_kernel<<<(unsigned)nblk, 128, sizeof(double) * kGramRows * R, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
+                                                                               factor_ptrs(s), s.D, s.part);
+    gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram);
+    EXAFAC_CHECK_LAUNCH();
+    // compute_pinv_square (common.h:405-443), eigenvalue cut 1e-11.
+    return launch_syev(R, s.dgram, 0, 1, nullptr, nullptr, 0, s.dpinv, 1e-11, s.vt, st);
+}
+
+// ---------------------------------------------------------------------------
+// Fiber lookup + counting sort of the hits by output row
+// (csr_based_spmm lookup half and transpose, sort_lookup.hpp:279-345).
+// ---------------------------------------------------------------------------
+template <typename Slot>
+__device__ __forceinline__ bool slot_match(const Slot& sl, Key128 k);
+template <>
+__device__ __forceinline__ bool slot_match<Slot1>(const Slot1& sl, Key128 k) {
+    return sl.key == k.lo;
+}
+template <>
+__device__ __forceinline__ bool slot_match<Slot2>(const Slot2& sl, Key128 k) {
+    return sl.lo == k.lo && sl.hi == k.hi;
+}
+
+template <typename Slot>
+__global__ void lookup_kernel(KeySpec spec, int64_t J, const int64_t* __restrict__ ju_dev,
+                              const uint32_t* __restrict__ sd, const Slot* __restrict__ slots, int64_t mask,
+                              uint32_t* __restrict__ f_start, uint32_t* __restrict__ f_len) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J) return;
+    uint32_t start = 0, len = 0;
+    if (j < *ju_dev) {
+        const Key128 key = pack_key(spec, sd + j * spec.N);
+        int64_t h = (int64_t)(hash_key(key) & (uint64_t)mask);
+        for (int64_t probe = 0; probe <= mask; probe++) {
+            const Slot sl = slots[h];
+            if (sl.start == kEmpty) break;
+            if (slot_match(sl, key)) {
+                start = sl.start;
+                len = sl.len;
+                break;
+            }
+            h = (h + 1) & mask;
+        }
+    }
+    f_start[j] = start;
+    f_len[j] = len;
+}
+
+// Last j in [0, ju) with f_off[j] <= h.
+__device__ __forceinline__ int64_t hit_owner(const int64_t* __restrict__ f_off, int64_t ju, int64_t h) {
+    int64_t lo = 0, hi = ju;
+    while (hi - lo > 1) {
+        int64_t mid = (lo + hi) >> 1;
+        if (f_off[mid] <= h) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Hits beyond the hit buffers (possible only when the samples given to
+// exafac_als_sampled_mttkrp repeat) are reported and dropped.
+__device__ __forceinline__ int64_t capped_hits(const int64_t* counters, int64_t cap, DeviceStatus* status) {
+    const int64_t H = counters[1];
+    if (H > cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) report(status, EXAFAC_ERR_DEVICE, 4, H, cap);
+        return cap;
+    }
+    return H;
+}
+
+__global__ void hit_count_kernel(const int64_t* __restrict__ counters, const int64_t* __restrict__ f_off,
+                                 const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
+                                 uint32_t* __restrict__ rowcnt, int64_t cap, DeviceStatus* status) {
+    const int64_t ju = counters[0], H = capped_hits(counters, cap, status);
+    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < H; h += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = hit_owner(f_off, ju, h);
+        const uint32_t row = rows_n[(int64_t)f_start[j] + (h - f_off[j])];
+        atomicAdd(&rowcnt[row], 1u);
+    }
+}
+
+__global__ void hit_scatter_kernel(const int64_t* __restrict__ counters, const int64_t* __restrict__ f_off,
+                                   const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
+                                   const double* __restrict__ vals_n, const int64_t* __restrict__ rowoff,
+                                   uint32_t* __restrict__ rowfill, uint32_t* __restrict__ hit_j,
+                                   double* __restrict__ hit_val, int64_t cap) {
+    const int64_t ju = counters[0], H = counters[1] < cap ? counters[1] : cap;
+    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < H; h += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = hit_owner(f_off, ju, h);
+        const int64_t p = (int64_t)f_start[j] + (h - f_off[j]);
+        const uint32_t row = rows_n[p];
+        const int64_t dst = rowoff[row] + atomicAdd(&rowfill[row], 1u);
+        hit_j[dst] = (uint32_t)j;
+        hit_val[dst] = vals_n[p];
+    }
+}
+
+__global__ void row_flag_kernel(int64_t I, const uint32_t* __restrict__ rowcnt, uint32_t* __restrict__ flag) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < I; r += (int64_t)gridDim.x * blockDim.x)
+        flag[r] = rowcnt[r] > 0 ? 1u : 0u;
+}
+
+__global__ void row_compact_kernel(int64_t I, const uint32_t* __restrict__ flag, const int64_t* __restrict__ pos,
+                                   uint32_t* __restrict__ list) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < I; r += (int64_t)gridDim.x * blockDim.x)
+        if (flag[r]) list[pos[r]] = (uint32_t)r;
+}
+
+// counters[5] += counters[1]: running total of the hits (nonzeros_iterated).
+__global__ void accumulate_kernel(int64_t* total, const int64_t* add) { *total += *add; }
+
+int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
+    const Lookup& L = s.look[n];
+    const unsigned blocks = (unsigned)ceil_div(J, 256);
+    if (L.kw == 1)
+        lookup_kernel<Slot1><<<blocks, 256, 0, st>>>(L.spec, J, s.counters + 0, s.sd, (const Slot1*)L.slots,
+                                                    L.nslots - 1, s.f_start, s.f_len);
+    else
+        lookup_kernel<Slot2><<<blocks, 256, 0, st>>>(L.spec, J, s.counters + 0, s.sd, (const Slot2*)L.slots,
+                                                    L.nslots - 1, s.f_start, s.f_len);
+    EXAFAC_CHECK_LAUNCH();
+    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.f_len, s.f_off, J, s.counters + 1, s.scan_sc, st));
+    accumulate_kernel<<<1, 1, 0, st>>>(s.counters + 5, s.counters + 1);
+    const int64_t I = s.dims[n];
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowcnt, 0, sizeof(uint32_t) * I, st));
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowfill, 0, sizeof(uint32_t) * I, st));
+    const int hb = 152 * 8;
+    hit_count_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, s.rowcnt, s.nnz, s.status);
+    EXAFAC_CHECK_LAUNCH();
+    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.rowcnt, s.rowoff, I, s.counters + 3, s.scan_sc, st));
+    // Touched rows in increasing order: flags reuse the rowfill buffer's twin.
+    row_flag_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.rowcnt, s.flags);
+    EXAFAC_CHECK_LAUNCH();
+    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, I, s.counters + 2, s.scan_sc, st));
+    row_compact_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.flags, s.pos, s.touched);
+    hit_scatter_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, L.vals, s.rowoff, s.rowfill,
+                                           s.hit_j, s.hit_val, s.nnz);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sampled MTTKRP + solve (csr_based_spmm scatter half sort_lookup.hpp:347-371,
+// then parallel_dsymm accumulator_stationary.hpp:283-286): warp per touched
+// row, M_r = sum over the row's hits of val * D'[j], U_r = M_r * Phi.
+// ---------------------------------------------------------------------------
+__global__ void spmm_solve_kernel(int R, const int64_t* __restrict__ counters, const uint32_t* __restrict__ touched,
+                                  const int64_t* __restrict__ rowoff, const uint32_t* __restrict__ rowcnt,
+                                  const uint32_t* __restrict__ hit_j, const double* __restrict__ hit_val,
+                                  const double* __restrict__ D, const double* __restrict__ Phi, double* __restrict__ U) {
+    extern __shared__ double sm[];
+    const int warps = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* phi = sm;
+    double* msm = sm + R * R + w * R;
+    if (Phi)
+        for (int e = threadIdx.x; e < R * R; e += blockDim.x) phi[e] = Phi[e];
+    __syncthreads();
+    const int64_t nt = counters[2];
+    for (int64_t i = (int64_t)blockIdx.x * warps + w; i < nt; i += (int64_t)gridDim.x * warps) {
+        const int64_t r = touched[i];
+        const int64_t beg = rowoff[r], cnt = rowcnt[r];
+        for (int c = lane; c < R; c += 32) {
+            double acc = 0.0;
+            for (int64_t p = beg; p < beg + cnt; p++) acc += D[(int64_t)hit_j[p] * R + c] * hit_val[p];
+            msm[c] = acc;
+        }
+        __syncwarp();
+        for (int c = lane; c < R; c += 32) {
+            double acc;
+            if (Phi) {
+                acc = 0.0;
+                for (int k = 0; k < R; k++) acc = fma(msm[k], phi[k * R + c], acc);
+            } else {
+                acc = msm[c];
+            }
+            U[r * R + c] = acc;
+        }
+        __syncwarp();
+    }
+}
+
+int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStream_t st) {
+    const int R = s.R;
+    const int warps = 8;
+    size_t smem = sizeof(double) * ((size_t)R * R + warps * R);
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(spmm_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    spmm_solve_kernel<<<grid_cap(s.dims[n], warps * 32), warps * 32, smem, st>>>(
+        R, s.counters, s.touched, s.rowoff, s.rowcnt, s.hit_j, s.hit_val, s.D, Phi, out);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+int spmm_solve(Session& s, int n, cudaStream_t st) { return spmm_solve_into(s, n, s.dpinv, s.F.U[n], st); }
+
+// ---------------------------------------------------------------------------
+// Column renormalisation (DistMat1D::renormalize_columns, distmat.hpp:85-138).
+// ---------------------------------------------------------------------------
+__global__ void sigma_kernel(int R, const double* __restrict__ ugram, double* __restrict__ sigma,
+                             double* __restrict__ ngram, int* __restrict__ degenerate) {
+    __shared__ double sg[kMaxRank];
+    __shared__ int deg;
+    if (threadIdx.x == 0) deg = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < R; c += blockDim.x) {
+        double v = sqrt(ugram[c * R + c]);
+        sg[c] = v;
+        sigma[c] = v;
+        if (!(v > 0.0)) deg = 1;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) ngram[e] = ugram[e] / (sg[e / R] * sg[e % R]);
+    if (threadIdx.x == 0) *degenerate = deg;
+}
+
+__global__ void scale_rows_kernel(int R, int64_t I, const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
+                                  const double* __restrict__ sigma, const int* __restrict__ degenerate,
+                                  double* __restrict__ U) {
+    const bool all = *degenerate != 0 || list == nullptr;
+    const int64_t rows = all ? I : *cnt_dev;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < rows * R; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = e / R;
+        int c = (int)(e % R);
+        int64_t r = all ? i : (int64_t)list[i];
+        U[r * R + c] /= sigma[c];
+    }
+}
+
+int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st) {
+    const int R = s.R;
+    const uint32_t* list = all_rows ? nullptr : s.touched;
+    EXAFAC_TRY(gram_rows(s, s.F.U[n], s.dims[n], list, s.counters + 2, s.ugram, st));
+    int* deg = reinterpret_cast<int*>(s.counters + 6);
+    sigma_kernel<<<1, 256, 0, st>>>(R, s.ugram, s.F.sigma, s.ngram, deg);
+    scale_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.dims[n], list, s.counters + 2, s.F.sigma,
+                                                                     deg, s.F.U[n]);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+__global__ void zero_rows_kernel(int R, const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
+                                 double* __restrict__ U, double* __restrict__ scores) {
+    const int64_t cnt = *cnt_dev;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt * R; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = list[e / R];
+        U[r * R + e % R] = 0.0;
+        if (scores && e % R == 0) scores[r] = 0.0;
+    }
+}
+
+// Clears the rows of U_n (and their leverage scores) that the previous update
+// left nonzero; a factor that was never updated is cleared entirely.
+int zero_factor_rows(Session& s, int n, cudaStream_t st) {
+    const int R = s.R;
+    double* sc = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV ? s.scores[n] : nullptr;
+    if (s.dense[n]) {
+        EXAFAC_CUDA_TRY(cudaMemsetAsync(s.F.U[n], 0, sizeof(double) * s.dims[n] * R, st));
+        if (sc) EXAFAC_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * s.dims[n], st));
+    } else {
+        zero_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.F.U[n], sc);
+        EXAFAC_CHECK_LAUNCH();
+    }
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exact fit (SparseTensor::compute_exact_fit + compute_2bmb,
+// sparse_tensor.hpp:288-356, sort_lookup.hpp:377-438): sum over nonzeros of
+// x^2 - 2 x m(x) with m(x) = sum_u sigma_u prod_{k>=1} U_k[i_k,u] * U_0[i_0,u].
+// ---------------------------------------------------------------------------
+__global__ void fit_kernel(int N, int R, int64_t nnz, const uint32_t* __restrict__ idx, const double* __restrict__ vals,
+                           FactorPtrs f, const double* __restrict__ sigma, double* __restrict__ part) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t* c = idx + i * N;
+        double value = 0.0;
+        for (int u = 0; u < R; u++) {
+            double p = sigma[u];
+            for (int k = 1; k < N; k++) p *= f.U[k][(int64_t)c[k] * R + u];
+            value += p * f.U[0][(int64_t)c[0] * R + u];
+        }
+        const double x = vals[i];
+        acc += x * x - 2 * value * x;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void sum_kernel(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+int fit_residual(Session& s, double* out_dev, cudaStream_t st) {
+    const int blocks = 152 * 8;
+    fit_kernel<<<blocks, 256, 0, st>>>(s.N, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), s.F.sigma, s.fitpart);
+    sum_kernel<<<1, 256, 0, st>>>(s.fitpart, blocks, out_dev);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exact MTTKRP (execute_exact_mttkrp, sort_lookup.hpp:440-495): for every
+// nonzero, M[i_n] += (prod_{k != n} U_k[i_k]) * x.  Atomic accumulation.
+// ---------------------------------------------------------------------------
+__global__ void exact_mttkrp_kernel(int N, int n, int R, int64_t nnz, const uint32_t* __restrict__ idx,
+                                    const double* __restrict__ vals, FactorPtrs f, double* __restrict__ M) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz * R; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / R;
+        const int u = (int)(e % R);
+        const uint32_t* c = idx + i * N;
+        double p = 1.0;
+        for (int k = 0; k < N; k++) {
+            if (k == n) continue;
+            p *= f.U[k][(int64_t)c[k] * R + u];
+        }
+        atomicAdd(&M[(int64_t)c[n] * R + u], p * vals[i]);
+    }
+}
+
+int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st) {
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(M, 0, sizeof(double) * s.dims[n] * s.R, st));
+    exact_mttkrp_kernel<<<152 * 16, 256, 0, st>>>(s.N, n, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), M);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// U = M * Phi (parallel_dsymm with the full symmetric Phi), warp per row.
+__global__ void matmul_rows_kernel(int R, int64_t rows, const double* __restrict__ M, const double* __restrict__ Phi,
+                                   double* __restrict__ U) {
+    extern __shared__ double sm[];
+    const int warps = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* phi = sm;
+    double* msm = sm + R * R + w * R;
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) phi[e] = Phi[e];
+    __syncthreads();
+    for (int64_t r = (int64_t)blockIdx.x * warps + w; r < rows; r += (int64_t)gridDim.x * warps) {
+        for (int c = lane; c < R; c += 32) msm[c] = M[r * R + c];
+        __syncwarp();
+        for (int c = lane; c < R; c += 32) {
+            double acc = 0.0;
+            for (int k = 0; k < R; k++) acc = fma(msm[k], phi[k * R + c], acc);
+            U[r * R + c] = acc;
+        }
+        __syncwarp();
+    }
+}
+
+int matmul_rows_sym(Session& s, const double* M, const double* Phi, double* U, int64_t rows, cudaStream_t st) {
+    const int R = s.R, warps = 8;
+    size_t smem = sizeof(double) * ((size_t)R * R + warps * R);
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(matmul_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    matmul_rows_kernel<<<grid_cap(rows, warps), warps * 32, smem, st>>>(R, rows, M, Phi, U);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// Hadamard product of the per-mode Grams in s.gram, skipping `skip` (-1: none)
+// (chain_had_prod, common.h:521-545).
+__global__ void chain_kernel(int N, int R, int skip, const double* __restrict__ gram, double* __restrict__ out) {
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+        double acc = 1.0;
+        for (int k = 0; k < N; k++)
+            if (k != skip) acc *= gram[(int64_t)k * R * R + e];
+        out[e] = acc;
+    }
+}
+
+int chain_gram(Session& s, int skip, double* out, cudaStream_t st) {
+    chain_kernel<<<1, 256, 0, st>>>(s.N, s.R, skip, s.gram, out);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+}  // namespace exafac

@@ -1,0 +1,179 @@
+// PartitionTree build and PTSample kernels (partition_tree.hpp:117-380).
+#include "tree.cuh"
+
+namespace exafac {
+
+// Leaf Grams: one warp per leaf; the leaf's rows are staged in shared memory
+// and each lane owns a strided set of packed entries, summing over rows in
+// row order.
+__global__ void tree_leaf_gram_kernel(TreeShape t, int R, const double* __restrict__ U, double* __restrict__ G) {
+    extern __shared__ unsigned char smraw[];
+    const int P = packed_size(R);
+    const int warps = blockDim.x / 32;
+    unsigned short* pa = reinterpret_cast<unsigned short*>(smraw);
+    unsigned short* pb = pa + P;
+    double* ublk = reinterpret_cast<double*>(smraw + align_up(2 * P * sizeof(unsigned short), 16));
+    block_build_pairs(R, pa, pb);
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* u = ublk + (size_t)w * t.F * R;
+    const int64_t first_leaf = t.node_count - t.leaf_count;
+    for (int64_t li = (int64_t)blockIdx.x * warps + w; li < t.leaf_count; li += (int64_t)gridDim.x * warps) {
+        const int64_t c = first_leaf + li;
+        const int64_t leaf = tree_leaf_idx(t, c);
+        const int64_t rows = (t.n - leaf * t.F) < t.F ? (t.n - leaf * t.F) : t.F;
+        for (int64_t e = lane; e < rows * R; e += 32) u[e] = U[leaf * t.F * R + e];
+        __syncwarp();
+        double* g = G + c * P;
+        for (int e = lane; e < P; e += 32) {
+            const int a = pa[e], b = pb[e];
+            double acc = 0.0;
+            for (int64_t r = 0; r < rows; r++) acc = fma(u[r * R + a], u[r * R + b], acc);
+            g[e] = acc;
+        }
+        __syncwarp();
+    }
+}
+
+// One level of internal nodes: G[c] = G[2c+1] + G[2c+2] (the reference adds
+// both children to a zeroed node: 0 + (l + r) == l + r).
+__global__ void tree_level_kernel(int64_t start, int64_t end, int P, double* __restrict__ G) {
+    const int64_t total = (end - start) * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = start + i / P;
+        int e = (int)(i % P);
+        G[c * P + e] = G[(2 * c + 1) * P + e] + G[(2 * c + 2) * P + e];
+    }
+}
+
+__global__ void tree_hadamard_kernel(int64_t nodes, int R, double* __restrict__ G, const double* __restrict__ M) {
+    const int P = packed_size(R);
+    const int64_t total = nodes * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int e = (int)(i % P);
+        // e -> (a, b): walk rows (R <= 128, cheap).
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        int b = a + rem;
+        G[i] *= M[a * R + b];
+    }
+}
+
+__global__ void tree_sample_kernel(TreeShape t, int R, const double* __restrict__ G, const double* __restrict__ U,
+                                   int64_t J, const double* __restrict__ x, double* __restrict__ hmul,
+                                   const double* __restrict__ draws, uint32_t* __restrict__ out, int64_t out_stride) {
+    extern __shared__ unsigned char smraw[];
+    const int P = packed_size(R);
+    const int warps = blockDim.x / 32;
+    unsigned short* pa = reinterpret_cast<unsigned short*>(smraw);
+    unsigned short* pb = pa + P;
+    double* base = reinterpret_cast<double*>(smraw + align_up(2 * P * sizeof(unsigned short), 16));
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per_warp = P + R + (int)t.F;
+    double* z_sm = base + (size_t)w * per_warp;
+    double* x_sm = z_sm + P;
+    double* q_sm = x_sm + R;
+    block_build_pairs(R, pa, pb);
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * warps + w; i < J; i += (int64_t)gridDim.x * warps) {
+        for (int r = lane; r < R; r += 32) x_sm[r] = x[i * R + r];
+        __syncwarp();
+        warp_build_z(R, x_sm, pa, pb, z_sm);
+        int64_t row = warp_descend(t, R, G, U, z_sm, x_sm, q_sm, draws[i]);
+        if (lane == 0) out[i * out_stride] = (uint32_t)row;
+        if (row < t.n) {
+            for (int r = lane; r < R; r += 32) hmul[i * R + r] *= U[row * R + r];
+        }
+        __syncwarp();
+    }
+}
+
+static int grid_for(int64_t work, int threads) {
+    int64_t b = (work + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)b;
+}
+
+int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cudaStream_t stream) {
+    const int P = packed_size(R);
+    int warps = 4;
+    while (warps > 1 && sizeof(double) * warps * t.F * R > 160 * 1024) warps /= 2;
+    size_t smem = align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * t.F * R;
+    if (smem > 48 * 1024) {
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(tree_leaf_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    int blocks = (int)std::min<int64_t>((t.leaf_count + warps - 1) / warps, 152 * 8);
+    tree_leaf_gram_kernel<<<blocks, warps * 32, smem, stream>>>(t, R, U, G);
+    EXAFAC_CHECK_LAUNCH();
+    int64_t start = t.nodes_before_lfill, end = t.node_count - t.leaf_count;
+    for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
+        if (end > start) {
+            tree_level_kernel<<<grid_for((end - start) * P, 256), 256, 0, stream>>>(start, end, P, G);
+            EXAFAC_CHECK_LAUNCH();
+        }
+        end = start;
+        start = ((start + 1) / 2) - 1;
+    }
+    return EXAFAC_OK;
+}
+
+int launch_tree_hadamard(const TreeShape& t, int R, double* G, const double* M, cudaStream_t stream) {
+    tree_hadamard_kernel<<<grid_for(t.node_count * packed_size(R), 256), 256, 0, stream>>>(t.node_count, R, G, M);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+size_t tree_sample_smem(int R, int64_t F, int warps) {
+    const int P = packed_size(R);
+    return align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * (P + R + F);
+}
+
+int launch_tree_sample(const TreeShape& t, int R, const double* G, const double* U, int64_t J, const double* x,
+                       double* hmul, const double* draws, uint32_t* out, int64_t out_stride, cudaStream_t stream) {
+    int warps = 8;
+    size_t smem = tree_sample_smem(R, t.F, warps);
+    while (smem > 200 * 1024 && warps > 1) {
+        warps /= 2;
+        smem = tree_sample_smem(R, t.F, warps);
+    }
+    if (smem > 48 * 1024) {
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(tree_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    int64_t blocks = (J + warps - 1) / warps;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    tree_sample_kernel<<<(int)blocks, warps * 32, smem, stream>>>(t, R, G, U, J, x, hmul, draws, out, out_stride);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+}  // namespace exafac
+
+using namespace exafac;
+
+extern "C" int64_t exafac_tree_node_count(int64_t n, int32_t F) {
+    if (n < 1 || F < 1) return 0;
+    return make_tree_shape(n, F).node_count;
+}
+
+extern "C" int exafac_tree_build(int64_t n, int32_t F, int32_t R, const double* U, double* G, void* stream) {
+    EXAFAC_ARG(n >= 1 && F >= 1 && R >= 1 && R <= kMaxRank, "exafac_tree_build: bad shape");
+    EXAFAC_ARG(U && G, "exafac_tree_build: null pointer");
+    return launch_tree_build(make_tree_shape(n, F), R, U, G, (cudaStream_t)stream);
+}
+
+extern "C" int exafac_tree_sample(int64_t n, int32_t F, int32_t R, const double* G, const double* U, int64_t J,
+                                  const double* x, double* hmul, const double* draws, uint32_t* rows_out,
+                                  int64_t rows_stride, void* stream) {
+    EXAFAC_ARG(n >= 1 && F >= 1 && R >= 1 && R <= kMaxRank && J >= 0, "exafac_tree_sample: bad shape");
+    EXAFAC_ARG(G && U && x && hmul && draws && rows_out, "exafac_tree_sample: null pointer");
+    if (J == 0) return EXAFAC_OK;
+    return launch_tree_sample(make_tree_shape(n, F), R, G, U, J, x, hmul, draws, rows_out, rows_stride,
+                              (cudaStream_t)stream);
+}

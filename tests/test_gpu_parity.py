@@ -1,0 +1,224 @@
+"""GPU parity: the CUDA path (libexafac_gb300.so through its C ABI) against the
+reference's own outputs (golden fixtures) and the oracle.
+
+Bars: sampled indices bit-exact; weights and sampled MTTKRP within 1e-12
+relative (of the largest magnitude); factors, sigma and fits within 1e-8
+(they pass through the R x R pseudo-inverse, whose conditioning multiplies
+the ~1e-16 differences in summation order)."""
+import ctypes
+import json
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if b.size == 0:
+        return 0.0
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from rdist_tensor_gb300 import _lib
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return _lib
+
+
+def dev(a, dtype):
+    return torch.as_tensor(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype).contiguous()
+
+
+def P(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def unpack(Gp, R):
+    nodes = Gp.shape[0]
+    out = np.zeros((nodes, R, R))
+    iu = np.triu_indices(R)
+    out[:, iu[0], iu[1]] = Gp
+    out[:, iu[1], iu[0]] = Gp
+    return out
+
+
+@pytest.mark.parametrize("name", ["t_partial", "t_eigen", "t_rows", "t_single"])
+def test_tree_build_and_sample(lib, golden, name):
+    g = golden("units.npz")
+    U, F, x, draws = g[f"{name}_U"], int(g[f"{name}_F"]), g[f"{name}_x"], g[f"{name}_draws"]
+    n, R = U.shape
+    J = x.shape[0]
+    nodes = lib.load().exafac_tree_node_count(n, F)
+    Ud = dev(U, torch.float64)
+    G = torch.zeros((nodes, R * (R + 1) // 2), dtype=torch.float64, device="cuda")
+    lib.call("exafac_tree_build", n, F, R, P(Ud), P(G), None)
+    Gref = g[f"{name}_G"].reshape(-1, R, R)
+    iu = np.triu_indices(R)
+    assert rel_err(G.cpu().numpy(), Gref[:, iu[0], iu[1]]) < 1e-13
+    xd = dev(x, torch.float64)
+    h = torch.ones((J, R), dtype=torch.float64, device="cuda")
+    dd = dev(draws, torch.float64)
+    rows = torch.zeros(J, dtype=torch.int32, device="cuda")
+    lib.call("exafac_tree_sample", n, F, R, P(G), P(Ud), J, P(xd), P(h), P(dd), P(rows), 1, None)
+    torch.cuda.synchronize()
+    assert np.array_equal(rows.cpu().numpy().astype(np.uint32), g[f"{name}_idx"])
+    assert np.array_equal(h.cpu().numpy(), g[f"{name}_h"])
+
+
+@pytest.mark.parametrize("case", ["full", "deficient"])
+def test_pinv_square(lib, golden, case):
+    g = golden("units.npz")
+    A = g[f"pinv_{case}_in"]
+    R = A.shape[0]
+    Ad = dev(A, torch.float64)
+    out = torch.zeros((R, R), dtype=torch.float64, device="cuda")
+    nbytes = lib.load().exafac_dense_workspace_bytes(R)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    lib.call("exafac_pinv_square", R, P(Ad), P(out), ctypes.c_double(1e-11), P(ws), ctypes.c_size_t(nbytes), None)
+    ref = g[f"pinv_{case}_out"]
+    iu = np.triu_indices(R)
+    assert rel_err(out.cpu().numpy()[iu], ref[iu]) < 1e-10
+
+
+def test_syev_matches_lapack(lib):
+    rng = np.random.default_rng(3)
+    for R in (1, 2, 5, 25, 32, 64):
+        A = rng.standard_normal((R + 7, R))
+        M = A.T @ A
+        lam_ref, V_ref = np.linalg.eigh(M)
+        Md = dev(M, torch.float64)
+        V = torch.zeros((R, R), dtype=torch.float64, device="cuda")
+        lam = torch.zeros(R, dtype=torch.float64, device="cuda")
+        nbytes = lib.load().exafac_dense_workspace_bytes(R)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        lib.call("exafac_syev", R, P(Md), P(V), P(lam), P(ws), ctypes.c_size_t(nbytes), None)
+        lam_g, V_g = lam.cpu().numpy(), V.cpu().numpy()
+        assert rel_err(lam_g, lam_ref) < 1e-13
+        # eigenvectors up to sign
+        dots = np.abs(np.sum(V_g * V_ref, axis=0))
+        assert np.max(np.abs(dots - 1.0)) < 1e-10
+
+
+STEP_CASES = ["c3_cp_arls_lev", "c3_sts_cp", "c4_cp_arls_lev", "c4_sts_cp", "dup_cp_arls_lev", "dup_sts_cp",
+              "one_cp_arls_lev", "one_sts_cp", "logc_cp_arls_lev"]
+
+
+def make_optimizer(dims, idx, vals, factors, sampler, J_max, preprocessing="none"):
+    from exafac.cpp_ext.py_module import (AccumulatorStationary, CP_ARLS_LEV, Grid, LowRankTensor, STS_CP,
+                                          SparseTensor, TensorGrid)
+
+    N = len(dims)
+    grid = Grid(np.ones(N, dtype=np.int32))
+    tg = TensorGrid(np.asarray(dims, dtype=np.int32), grid)
+    st = SparseTensor(tg, np.asarray(idx, dtype=np.uint32), np.asarray(vals, dtype=np.float64), preprocessing)
+    lr = LowRankTensor(factors[0].shape[1], tg)
+    lr.set_factors(factors)
+    s = CP_ARLS_LEV(lr) if sampler == "cp_arls_lev" else STS_CP(lr)
+    opt = AccumulatorStationary(st, lr, s, max_samples=J_max)
+    opt.initialize_ground_truth_for_als()
+    return opt, lr
+
+
+def lex_sorted(a, cols):
+    order = np.lexsort(tuple(a[:, k] for k in reversed(cols)))
+    return order
+
+
+@pytest.mark.parametrize("key", STEP_CASES)
+def test_sweep_matches_reference(lib, golden, key):
+    g = golden("steps.npz")
+    meta = json.loads(str(g["meta"]))
+    m = meta[key]
+    base = key.split("_")[0]
+    dims, J = m["dims"], m["J"]
+    N = len(dims)
+    factors = [g[f"{base}_U{k}"] for k in range(N)]
+    opt, lr = make_optimizer(dims, g[f"{base}_idx"], g[f"{base}_vals"], factors, m["sampler"], J,
+                             m.get("preprocessing", "none"))
+    assert abs(opt.compute_exact_fit() - float(g[f"{key}_fit0"])) < 1e-10
+    for t in range(m["steps"]):
+        n = t % N
+        uni = dev(g[f"{key}_s{t}_uniforms"], torch.float64)
+        perms = dev(g[f"{key}_s{t}_perms"].astype(np.int32), torch.int32) if m["sampler"] == "cp_arls_lev" else None
+        if f"{key}_s{t}_samples" in g:
+            samples, weights = opt.draw(n, J, uni, perms)
+            assert np.array_equal(samples.cpu().numpy().astype(np.uint32), g[f"{key}_s{t}_samples"]), f"step {t}"
+            assert rel_err(weights.cpu().numpy(), g[f"{key}_s{t}_weights"]) < 1e-12
+            sd_ref = g[f"{key}_s{t}_samples_dedup"]
+            M = opt.sampled_mttkrp(n, sd_ref, g[f"{key}_s{t}_spmm_design"])
+            assert rel_err(M.cpu().numpy(), g[f"{key}_s{t}_spmm_out"]) < 1e-12
+            assert opt.step_info().hits == int(g[f"{key}_s{t}_spmm_found"])
+        opt.execute_ALS_step(n, J, uni, perms)
+        info = opt.step_info()
+        assert info.hits == int(g[f"{key}_s{t}_hits"])
+        if f"{key}_s{t}_samples_dedup" in g:
+            sd, wd, _, _ = opt.last_dedup()
+            sd, wd = sd.cpu().numpy().astype(np.uint32), wd.cpu().numpy()
+            ref_sd, ref_wd = g[f"{key}_s{t}_samples_dedup"], g[f"{key}_s{t}_weights_dedup"]
+            cols = [k for k in range(N) if k != n]
+            o1, o2 = lex_sorted(sd, cols), lex_sorted(ref_sd, cols)
+            assert np.array_equal(sd[o1][:, cols], ref_sd[o2][:, cols])
+            assert rel_err(wd[o1], ref_wd[o2]) < 1e-12
+        assert rel_err(lr.factors[n].data.cpu().numpy(), g[f"{key}_s{t}_factor"]) < 1e-8, f"step {t}"
+        assert rel_err(lr.sigma.cpu().numpy(), g[f"{key}_s{t}_sigma"]) < 1e-8
+    assert abs(opt.compute_exact_fit() - float(g[f"{key}_fit1"])) < 1e-8
+    opt.deinitialize()
+
+
+def test_workload1_sweep_matches_reference(lib, golden, oracle_mod):
+    """2000^3 planted tensor, 2e6 nonzeros, R=25, J=65536, STS-CP: one sweep on
+    the GPU against the reference (tensor and uniform stream regenerated)."""
+    from rdist_tensor_gb300 import synthetic
+
+    g = golden("workload1.npz")
+    dims, idx, vals = synthetic.planted_uniform(seed=0)
+    R, J = int(g["R"]), int(g["J"])
+    factors = synthetic.gaussian_factors(dims, R, seed=1)
+    opt, lr = make_optimizer(dims, idx, vals, factors, "sts_cp", J)
+    assert abs(opt.compute_exact_fit() - float(g["fit0"])) < 1e-10
+    streams = oracle_mod.sts_uniform_stream(int(g["seeds"][0]), 3, J, 3)
+    for t in range(3):
+        opt.execute_ALS_step(t, J, dev(streams[t], torch.float64))
+        assert opt.step_info().hits == int(g[f"s{t}_hits"])
+        assert rel_err(lr.factors[t].data.cpu().numpy(), g[f"s{t}_factor"]) < 1e-8
+        assert rel_err(lr.sigma.cpu().numpy(), g[f"s{t}_sigma"]) < 1e-8
+    assert abs(opt.compute_exact_fit() - float(g["fit1"])) < 1e-8
+    opt.deinitialize()
+
+
+@pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
+def test_exact_then_sampled_against_oracle(lib, oracle_mod, sampler):
+    """One exact-ALS sweep (the -p exact preprocessing) then a sampled sweep
+    with the GPU's own uniforms, replayed through the oracle."""
+    from rdist_tensor_gb300 import synthetic
+
+    dims, idx, vals = synthetic.zipf_tensor((3000, 2500, 300, 60), 60000, alpha=1.2, seed=4)
+    vals = vals.astype(np.float64)
+    R, J = 8, 4096
+    factors = synthetic.gaussian_factors(dims, R, seed=5)
+    opt, lr = make_optimizer(dims, idx, vals, factors, sampler, J)
+    ora = oracle_mod.OracleALS(dims, idx, vals, factors, sampler)
+    for n in range(4):
+        opt.exact_step(n)
+    oracle_mod.exact_als_sweep(ora, 1)
+    for n in range(4):
+        assert rel_err(lr.factors[n].data.cpu().numpy(), ora.factors[n]) < 1e-9
+    assert abs(opt.compute_exact_fit() - ora.fit()) < 1e-9
+    rng = np.random.default_rng(11)
+    for n in range(4):
+        shape = (4, J) if sampler == "cp_arls_lev" else (4, 2, J)
+        uni = rng.random(shape)
+        opt.execute_ALS_step(n, J, dev(uni, torch.float64))
+        out = ora.step(n, J, uni)
+        assert opt.step_info().hits == out["hits"]
+        assert rel_err(lr.factors[n].data.cpu().numpy(), out["factor"]) < 1e-8
+    assert abs(opt.compute_exact_fit() - ora.fit()) < 1e-8
+    opt.deinitialize()
