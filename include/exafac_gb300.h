@@ -56,6 +56,9 @@ enum { EXAFAC_PRE_NONE = 0, EXAFAC_PRE_LOG_COUNT = 1, EXAFAC_PRE_ONES = 2 };
 const char* exafac_last_error(void);
 int exafac_abi_version(void);
 
+/* Number of kernels this library has launched since it was loaded. */
+long long exafac_kernel_launches(void);
+
 /* ---------------------------------------------------------------------------
  * Single routines (stateless).  They exist so each reference routine can be
  * checked on its own; the session API below chains them.

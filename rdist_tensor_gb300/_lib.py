@@ -48,6 +48,7 @@ _SZ = ctypes.c_size_t
 SIGNATURES = {
     "exafac_last_error": (ctypes.c_char_p, []),
     "exafac_abi_version": (ctypes.c_int, []),
+    "exafac_kernel_launches": (ctypes.c_longlong, []),
     "exafac_tree_node_count": (_I64, [_I64, _I32]),
     "exafac_tree_build": (ctypes.c_int, [_I64, _I32, _I32, _P, _P, _P]),
     "exafac_tree_sample": (ctypes.c_int, [_I64, _I32, _I32, _P, _P, _I64, _P, _P, _P, _P, _I64, _P]),

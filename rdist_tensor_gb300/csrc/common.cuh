@@ -18,6 +18,9 @@ constexpr int kMaxRank = 128;
 // Last-error text for the C-ABI (thread-local).
 void set_error(const std::string& msg);
 
+// Kernel launches issued by the library since load (exafac_kernel_launches).
+void count_launch();
+
 #define EXAFAC_CUDA_TRY(expr)                                                                     \
     do {                                                                                          \
         cudaError_t _e = (expr);                                                                  \

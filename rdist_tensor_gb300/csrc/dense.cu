@@ -185,7 +185,7 @@ int launch_syev(int R, const double* A, int64_t a_stride, int batch, double* V, 
         EXAFAC_CUDA_TRY(cudaFuncSetAttribute(syev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     int threads = R <= 32 ? 256 : 512;
-    syev_kernel<<<batch, threads, smem, stream>>>(R, A, a_stride, V, lam, v_stride, pinv, tol, vt_scratch);
+    syev_kernel<<<batch, threads, smem, stream>>>(R, A, a_stride, V, lam, v_stride, pinv, tol, vt_scratch); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

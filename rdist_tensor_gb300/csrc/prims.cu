@@ -128,9 +128,9 @@ static int scan_impl(const Tin* in, Tacc* out, int64_t n, Tacc* total, void* scr
     }
     int64_t nb = ceil_div(n, kScanTile);
     Tacc* partial = reinterpret_cast<Tacc*>(scratch);
-    scan_block_sums<Tin, Tacc><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial);
-    scan_partials_kernel<Tacc><<<1, 1024, 0, s>>>(partial, nb, total);
-    scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial);
+    scan_block_sums<Tin, Tacc><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial); count_launch();
+    scan_partials_kernel<Tacc><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
+    scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -261,11 +261,11 @@ int radix_sort_pairs(int64_t count, int bits, int kw, const uint64_t* lo_in, con
         uint32_t* dp = to_out ? pay_out : pay_tmp;
         (void)last;
         radix_hist_kernel<<<(unsigned)nb, kRadixThreads, 0, s>>>(src_lo, has_hi ? src_hi : nullptr, count, p * 8, hist,
-                                                                 nb);
+                                                                 nb); count_launch();
         EXAFAC_CHECK_LAUNCH();
         EXAFAC_TRY(scan_exclusive_u32_to_i64(hist, offs, 256 * nb, nullptr, scan_sc, s));
         radix_scatter_kernel<<<(unsigned)nb, kRadixThreads, 0, s>>>(src_lo, has_hi ? src_hi : nullptr, src_p, count,
-                                                                    p * 8, offs, nb, dlo, dhi, dp);
+                                                                    p * 8, offs, nb, dlo, dhi, dp); count_launch();
         EXAFAC_CHECK_LAUNCH();
         src_lo = dlo;
         src_hi = dhi;

@@ -40,7 +40,7 @@ __global__ void philox_uniform_kernel(double* out, int64_t count, uint64_t seed,
 int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st) {
     if (count <= 0) return EXAFAC_OK;
     int64_t threads = (count + 1) / 2;
-    philox_uniform_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(out, count, s.seed, s.counter++);
+    philox_uniform_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(out, count, s.seed, s.counter++); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -86,18 +86,18 @@ int arls_build_cdf(Session& s, int k, cudaStream_t st) {
     const int64_t n = s.dims[k];
     if (n < 2) {
         // A one-row distribution always yields row 0 and consumes no draw.
-        cdf_sequential_kernel<<<1, 32, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k);
+        cdf_sequential_kernel<<<1, 32, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k); count_launch();
         EXAFAC_CHECK_LAUNCH();
         return EXAFAC_OK;
     }
     if (n <= kExactCdfMax) {
-        cdf_sequential_kernel<<<1, 256, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k);
+        cdf_sequential_kernel<<<1, 256, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k); count_launch();
         EXAFAC_CHECK_LAUNCH();
         return EXAFAC_OK;
     }
     EXAFAC_TRY(scan_inclusive_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st));
     int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
-    cdf_normalize_kernel<<<blocks, 256, 0, st>>>(s.cdf[k], n, s.cdf_total + k);
+    cdf_normalize_kernel<<<blocks, 256, 0, st>>>(s.cdf[k], n, s.cdf_total + k); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -140,7 +140,7 @@ int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStre
     int64_t rows = all_rows ? s.dims[k] : s.dims[k];
     int blocks = (int)std::min<int64_t>(ceil_div(rows, warps), 152 * 16);
     leverage_kernel<<<blocks, warps * 32, smem, st>>>(R, s.F.U[k], pinv, s.dims[k], all_rows ? nullptr : s.touched,
-                                                      s.counters + 2, s.scores[k]);
+                                                      s.counters + 2, s.scores[k]); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -198,7 +198,7 @@ int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* p
         m.dims[k] = k < s.N ? s.dims[k] : 0;
     }
     arls_draw_kernel<<<(unsigned)ceil_div(J, 256), 256, 0, st>>>(s.N, n, J, m, s.cdf_total, uni, perms, s.samples,
-                                                                  s.weights, s.status);
+                                                                  s.weights, s.status); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -321,19 +321,19 @@ __global__ void sts_eigen_tree_kernel(int N, int n, int R, TreeShape t, const do
 
 int sts_compute_M(Session& s, int n, cudaStream_t st) {
     const int N = s.N, R = s.R, R2 = R * R;
-    sts_chain_kernel<<<1, 256, 0, st>>>(N, n, R, s.gram, s.chain);
+    sts_chain_kernel<<<1, 256, 0, st>>>(N, n, R, s.gram, s.chain); count_launch();
     EXAFAC_CHECK_LAUNCH();
     const int first = (n == 0) ? 1 : 0;
     EXAFAC_TRY(launch_syev(R, s.chain + (int64_t)first * R2, 0, 1, s.eigV, s.eigL, 0, nullptr, 0.0, s.vt, st));
-    sts_phi_kernel<<<1, 256, sizeof(double) * R2, st>>>(N, n, R, s.eigV, s.eigL, s.chain, s.Emat, s.Phi, s.PhiP);
+    sts_phi_kernel<<<1, 256, sizeof(double) * R2, st>>>(N, n, R, s.eigV, s.eigL, s.chain, s.Emat, s.Phi, s.PhiP); count_launch();
     EXAFAC_CHECK_LAUNCH();
     if (N > 1) {
         // matrices 1..N-1 (chain[n] was cleared, its decomposition is trivial)
         EXAFAC_TRY(launch_syev(R, s.chain + R2, R2, N - 1, s.eigV + R2, s.eigL + R, R2, nullptr, 0.0, s.vt, st));
     }
-    sts_emat_kernel<<<1, 256, 0, st>>>(N, n, R, s.eigV, s.eigL, s.Emat);
+    sts_emat_kernel<<<1, 256, 0, st>>>(N, n, R, s.eigV, s.eigL, s.Emat); count_launch();
     EXAFAC_CHECK_LAUNCH();
-    sts_eigen_tree_kernel<<<N, 256, 0, st>>>(N, n, R, s.etree, s.Emat, s.gram, s.eigG);
+    sts_eigen_tree_kernel<<<N, 256, 0, st>>>(N, n, R, s.etree, s.Emat, s.gram, s.eigG); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -433,7 +433,7 @@ int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
         EXAFAC_CUDA_TRY(cudaFuncSetAttribute(sts_draw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int64_t blocks = std::min<int64_t>(ceil_div(J, warps), 152 * 16);
     sts_draw_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), warps * 32, smem, st>>>(
-        N, n, R, J, m, s.etree, s.eigG, s.Emat, s.PhiP, uni, s.samples, s.weights, s.status);
+        N, n, R, J, m, s.etree, s.eigG, s.Emat, s.PhiP, uni, s.samples, s.weights, s.status); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

@@ -5,6 +5,7 @@
 // synchronisation: data-dependent sizes (unique samples, hits, touched rows)
 // stay on the device and kernels read them from there, so a sweep can be
 // captured in a CUDA graph.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -17,6 +18,9 @@ namespace exafac {
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static int64_t next_pow2(int64_t x) {
     int64_t p = 1;
@@ -220,6 +224,7 @@ extern "C" int exafac_als_region_times(exafac_als_t h, double* out7) {
 
 extern "C" const char* exafac_last_error(void) { return g_last_error.c_str(); }
 extern "C" int exafac_abi_version(void) { return EXAFAC_ABI_VERSION; }
+extern "C" long long exafac_kernel_launches(void) { return g_launches.load(); }
 
 extern "C" int exafac_als_workspace_size(const exafac_als_config* cfg, size_t* persistent_bytes, size_t* setup_b) {
     Session s;
@@ -411,7 +416,7 @@ extern "C" int exafac_als_fit(exafac_als_t h, double* fit, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     EXAFAC_TRY(all_grams(s, st));
     EXAFAC_TRY(chain_gram(s, -1, s.dgram, st));
-    fit_finish_kernel<<<1, 32, 0, st>>>(s.R, s.dgram, s.F.sigma, s.scal + 1);
+    fit_finish_kernel<<<1, 32, 0, st>>>(s.R, s.dgram, s.F.sigma, s.scal + 1); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(fit_residual(s, s.scal + 2, st));
     double v[2];

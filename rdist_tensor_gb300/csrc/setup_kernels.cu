@@ -42,8 +42,8 @@ __global__ void sum_parts_kernel(const double* __restrict__ part, int n, double*
 
 int preprocess_values(Session& s, const double* vals_in, cudaStream_t st) {
     const int blocks = 152 * 8;
-    preprocess_kernel<<<blocks, 256, 0, st>>>(s.nnz, s.cfg.preprocessing, vals_in, s.vals, s.fitpart);
-    sum_parts_kernel<<<1, 256, 0, st>>>(s.fitpart, blocks, s.scal + 0);
+    preprocess_kernel<<<blocks, 256, 0, st>>>(s.nnz, s.cfg.preprocessing, vals_in, s.vals, s.fitpart); count_launch();
+    sum_parts_kernel<<<1, 256, 0, st>>>(s.fitpart, blocks, s.scal + 0); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -171,18 +171,19 @@ int build_lookup(Session& s, int n, void* setup, size_t setup_sz, cudaStream_t s
     const int kw = L.kw;
     const int blocks = 152 * 8;
     pack_keys_kernel<<<blocks, 256, 0, st>>>(L.spec, nnz, s.idx, b.lo, kw == 2 ? b.hi : nullptr, b.pay, s.status,
-                                             s.dims_dev);
+                                             s.dims_dev); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(radix_sort_pairs(nnz, L.spec.bits, kw, b.lo, b.hi, b.pay, b.lo_s, b.hi_s, b.pay_s, b.lo_t, b.hi_t,
                                 b.pay_t, b.radix_sc, st));
-    gather_sorted_kernel<<<blocks, 256, 0, st>>>(s.N, n, nnz, b.pay_s, s.idx, s.vals, L.rows, L.vals);
-    fiber_flag_kernel<<<blocks, 256, 0, st>>>(nnz, b.lo_s, kw == 2 ? b.hi_s : nullptr, b.flag);
+    gather_sorted_kernel<<<blocks, 256, 0, st>>>(s.N, n, nnz, b.pay_s, s.idx, s.vals, L.rows, L.vals); count_launch();
+    fiber_flag_kernel<<<blocks, 256, 0, st>>>(nnz, b.lo_s, kw == 2 ? b.hi_s : nullptr, b.flag); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(b.flag, b.fid, nnz, b.nf, b.scan_sc, st));
-    fiber_compact_kernel<<<blocks, 256, 0, st>>>(nnz, b.flag, b.fid, b.fstart, b.nf);
+    fiber_compact_kernel<<<blocks, 256, 0, st>>>(nnz, b.flag, b.fid, b.fstart, b.nf); count_launch();
     EXAFAC_CHECK_LAUNCH();
     const size_t slot_bytes = kw == 1 ? sizeof(Slot1) : sizeof(Slot2);
     EXAFAC_CUDA_TRY(cudaMemsetAsync(L.slots, 0xff, slot_bytes * (size_t)L.nslots, st));
+    count_launch();
     if (kw == 1)
         fiber_insert_kernel<Slot1><<<blocks, 256, 0, st>>>(b.nf, b.fstart, b.lo_s, nullptr, (Slot1*)L.slots,
                                                            L.nslots - 1, s.status);

@@ -77,12 +77,12 @@ int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.d_count, 0, sizeof(int32_t) * s.dtab, st));
     const unsigned blocks = (unsigned)ceil_div(J, 256);
     dedup_insert_kernel<<<blocks, 256, 0, st>>>(s.look[n].spec, J, s.samples, s.dtab - 1, s.d_owner, s.d_minj,
-                                                s.d_count, s.slot_of);
-    dedup_flag_kernel<<<blocks, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags);
+                                                s.d_count, s.slot_of); count_launch();
+    dedup_flag_kernel<<<blocks, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, J, s.counters + 0, s.scan_sc, st));
     dedup_compact_kernel<<<blocks, 256, 0, st>>>(s.N, J, s.flags, s.pos, s.slot_of, s.d_count, s.samples, s.weights,
-                                                 s.sd, s.wd);
+                                                 s.sd, s.wd); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -155,8 +155,8 @@ int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist
         return EXAFAC_ERR_WORKSPACE;
     }
     gram_partial_kernel<<<(unsigned)nblk, 128, sizeof(double) * kGramRows * R, st>>>(R, A, rows, rowlist, count_dev,
-                                                                                     s.part);
-    gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, out_full);
+                                                                                     s.part); count_launch();
+    gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, out_full); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -208,8 +208,8 @@ int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
     const int R = s.R;
     int64_t nblk = std::max<int64_t>(1, ceil_div(J, kGramRows));
     design_kernel<<<(unsigned)nblk, 128, sizeof(double) * kGramRows * R, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
-                                                                               factor_ptrs(s), s.D, s.part);
-    gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram);
+                                                                               factor_ptrs(s), s.D, s.part); count_launch();
+    gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram); count_launch();
     EXAFAC_CHECK_LAUNCH();
     // compute_pinv_square (common.h:405-443), eigenvalue cut 1e-11.
     return launch_syev(R, s.dgram, 0, 1, nullptr, nullptr, 0, s.dpinv, 1e-11, s.vt, st);
@@ -321,6 +321,7 @@ __global__ void accumulate_kernel(int64_t* total, const int64_t* add) { *total +
 int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
     const Lookup& L = s.look[n];
     const unsigned blocks = (unsigned)ceil_div(J, 256);
+    count_launch();
     if (L.kw == 1)
         lookup_kernel<Slot1><<<blocks, 256, 0, st>>>(L.spec, J, s.counters + 0, s.sd, (const Slot1*)L.slots,
                                                     L.nslots - 1, s.f_start, s.f_len);
@@ -329,21 +330,21 @@ int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
                                                     L.nslots - 1, s.f_start, s.f_len);
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.f_len, s.f_off, J, s.counters + 1, s.scan_sc, st));
-    accumulate_kernel<<<1, 1, 0, st>>>(s.counters + 5, s.counters + 1);
+    accumulate_kernel<<<1, 1, 0, st>>>(s.counters + 5, s.counters + 1); count_launch();
     const int64_t I = s.dims[n];
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowcnt, 0, sizeof(uint32_t) * I, st));
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowfill, 0, sizeof(uint32_t) * I, st));
     const int hb = 152 * 8;
-    hit_count_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, s.rowcnt, s.nnz, s.status);
+    hit_count_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, s.rowcnt, s.nnz, s.status); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.rowcnt, s.rowoff, I, s.counters + 3, s.scan_sc, st));
     // Touched rows in increasing order: flags reuse the rowfill buffer's twin.
-    row_flag_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.rowcnt, s.flags);
+    row_flag_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.rowcnt, s.flags); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, I, s.counters + 2, s.scan_sc, st));
-    row_compact_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.flags, s.pos, s.touched);
+    row_compact_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.flags, s.pos, s.touched); count_launch();
     hit_scatter_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, L.vals, s.rowoff, s.rowfill,
-                                           s.hit_j, s.hit_val, s.nnz);
+                                           s.hit_j, s.hit_val, s.nnz); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -397,7 +398,7 @@ int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStrea
         EXAFAC_CUDA_TRY(
             cudaFuncSetAttribute(spmm_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     spmm_solve_kernel<<<grid_cap(s.dims[n], warps * 32), warps * 32, smem, st>>>(
-        R, s.counters, s.touched, s.rowoff, s.rowcnt, s.hit_j, s.hit_val, s.D, Phi, out);
+        R, s.counters, s.touched, s.rowoff, s.rowcnt, s.hit_j, s.hit_val, s.D, Phi, out); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -442,9 +443,9 @@ int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st) {
     const uint32_t* list = all_rows ? nullptr : s.touched;
     EXAFAC_TRY(gram_rows(s, s.F.U[n], s.dims[n], list, s.counters + 2, s.ugram, st));
     int* deg = reinterpret_cast<int*>(s.counters + 6);
-    sigma_kernel<<<1, 256, 0, st>>>(R, s.ugram, s.F.sigma, s.ngram, deg);
+    sigma_kernel<<<1, 256, 0, st>>>(R, s.ugram, s.F.sigma, s.ngram, deg); count_launch();
     scale_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.dims[n], list, s.counters + 2, s.F.sigma,
-                                                                     deg, s.F.U[n]);
+                                                                     deg, s.F.U[n]); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -468,7 +469,7 @@ int zero_factor_rows(Session& s, int n, cudaStream_t st) {
         EXAFAC_CUDA_TRY(cudaMemsetAsync(s.F.U[n], 0, sizeof(double) * s.dims[n] * R, st));
         if (sc) EXAFAC_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * s.dims[n], st));
     } else {
-        zero_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.F.U[n], sc);
+        zero_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.F.U[n], sc); count_launch();
         EXAFAC_CHECK_LAUNCH();
     }
     return EXAFAC_OK;
@@ -518,8 +519,8 @@ __global__ void sum_kernel(const double* __restrict__ part, int n, double* __res
 
 int fit_residual(Session& s, double* out_dev, cudaStream_t st) {
     const int blocks = 152 * 8;
-    fit_kernel<<<blocks, 256, 0, st>>>(s.N, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), s.F.sigma, s.fitpart);
-    sum_kernel<<<1, 256, 0, st>>>(s.fitpart, blocks, out_dev);
+    fit_kernel<<<blocks, 256, 0, st>>>(s.N, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), s.F.sigma, s.fitpart); count_launch();
+    sum_kernel<<<1, 256, 0, st>>>(s.fitpart, blocks, out_dev); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -545,7 +546,7 @@ __global__ void exact_mttkrp_kernel(int N, int n, int R, int64_t nnz, const uint
 
 int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st) {
     EXAFAC_CUDA_TRY(cudaMemsetAsync(M, 0, sizeof(double) * s.dims[n] * s.R, st));
-    exact_mttkrp_kernel<<<152 * 16, 256, 0, st>>>(s.N, n, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), M);
+    exact_mttkrp_kernel<<<152 * 16, 256, 0, st>>>(s.N, n, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), M); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -578,7 +579,7 @@ int matmul_rows_sym(Session& s, const double* M, const double* Phi, double* U, i
     if (smem > 48 * 1024)
         EXAFAC_CUDA_TRY(
             cudaFuncSetAttribute(matmul_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    matmul_rows_kernel<<<grid_cap(rows, warps), warps * 32, smem, st>>>(R, rows, M, Phi, U);
+    matmul_rows_kernel<<<grid_cap(rows, warps), warps * 32, smem, st>>>(R, rows, M, Phi, U); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -595,7 +596,7 @@ __global__ void chain_kernel(int N, int R, int skip, const double* __restrict__ 
 }
 
 int chain_gram(Session& s, int skip, double* out, cudaStream_t st) {
-    chain_kernel<<<1, 256, 0, st>>>(s.N, s.R, skip, s.gram, out);
+    chain_kernel<<<1, 256, 0, st>>>(s.N, s.R, skip, s.gram, out); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

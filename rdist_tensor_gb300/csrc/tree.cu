@@ -108,12 +108,12 @@ int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cud
             cudaFuncSetAttribute(tree_leaf_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     int blocks = (int)std::min<int64_t>((t.leaf_count + warps - 1) / warps, 152 * 8);
-    tree_leaf_gram_kernel<<<blocks, warps * 32, smem, stream>>>(t, R, U, G);
+    tree_leaf_gram_kernel<<<blocks, warps * 32, smem, stream>>>(t, R, U, G); count_launch();
     EXAFAC_CHECK_LAUNCH();
     int64_t start = t.nodes_before_lfill, end = t.node_count - t.leaf_count;
     for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
         if (end > start) {
-            tree_level_kernel<<<grid_for((end - start) * P, 256), 256, 0, stream>>>(start, end, P, G);
+            tree_level_kernel<<<grid_for((end - start) * P, 256), 256, 0, stream>>>(start, end, P, G); count_launch();
             EXAFAC_CHECK_LAUNCH();
         }
         end = start;
@@ -123,7 +123,7 @@ int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cud
 }
 
 int launch_tree_hadamard(const TreeShape& t, int R, double* G, const double* M, cudaStream_t stream) {
-    tree_hadamard_kernel<<<grid_for(t.node_count * packed_size(R), 256), 256, 0, stream>>>(t.node_count, R, G, M);
+    tree_hadamard_kernel<<<grid_for(t.node_count * packed_size(R), 256), 256, 0, stream>>>(t.node_count, R, G, M); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -148,7 +148,7 @@ int launch_tree_sample(const TreeShape& t, int R, const double* G, const double*
     int64_t blocks = (J + warps - 1) / warps;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
-    tree_sample_kernel<<<(int)blocks, warps * 32, smem, stream>>>(t, R, G, U, J, x, hmul, draws, out, out_stride);
+    tree_sample_kernel<<<(int)blocks, warps * 32, smem, stream>>>(t, R, G, U, J, x, hmul, draws, out, out_stride); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

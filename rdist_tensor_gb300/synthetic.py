@@ -91,6 +91,76 @@ def zipf_tensor(dims, nnz, alpha=1.2, values="lognormal", seed=0, max_rounds=8):
     return np.array(dims, dtype=np.int64), np.ascontiguousarray(have), vals
 
 
+def zipf_tensor_device(dims, nnz, alpha=1.2, values="lognormal", seed=0, max_rounds=12, device="cuda"):
+    """Same construction as ``zipf_tensor`` with torch on a CUDA device (the
+    1e8-nonzero workloads take minutes in numpy): per-mode exact truncated
+    Zipf(alpha) by inverse-CDF search, deduplicated on a packed 128-bit key,
+    first occurrences kept, oversampled in rounds until ``nnz`` unique
+    coordinates exist (or ``max_rounds`` ran; the returned count is then what
+    was reached).  Deterministic for a seed on a given torch build.  Returns
+    (dims int64 numpy, idx int32 [nnz, N] device tensor, values float32 device
+    tensor)."""
+    import torch
+
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    dims = [int(d) for d in dims]
+    N = len(dims)
+    bits = [max(1, int(np.ceil(np.log2(d)))) for d in dims]
+    if sum(bits) > 126:
+        raise ValueError("coordinates need more than 126 key bits")
+    cdfs = []
+    for d in dims:
+        k = torch.arange(1, d + 1, dtype=torch.float64, device=device)
+        c = torch.cumsum(k.pow(-alpha), 0)
+        cdfs.append(c / c[-1])
+
+    def pack(idx):
+        hi = torch.zeros(idx.shape[0], dtype=torch.int64, device=device)
+        lo = torch.zeros(idx.shape[0], dtype=torch.int64, device=device)
+        total = 0
+        for k in range(N - 1, -1, -1):
+            c = idx[:, k].to(torch.int64)
+            if total < 63 and total + bits[k] <= 63:
+                lo |= c << total
+            elif total >= 63:
+                hi |= c << (total - 63)
+            else:
+                lo |= (c & ((1 << (63 - total)) - 1)) << total
+                hi |= c >> (63 - total)
+            total += bits[k]
+        return hi, lo
+
+    have = torch.zeros((0, N), dtype=torch.int32, device=device)
+    want = int(nnz)
+    for _ in range(max_rounds):
+        m = int(want * 1.3) + 1024
+        cand = torch.stack([torch.clamp(torch.searchsorted(cdfs[k], torch.rand(m, dtype=torch.float64, device=device,
+                                                                                 generator=gen), right=True),
+                                        max=dims[k] - 1).to(torch.int32) for k in range(N)], dim=1)
+        allc = torch.cat([have, cand])
+        hi, lo = pack(allc)
+        pos = torch.arange(allc.shape[0], device=device)
+        # stable two-key sort: by lo, then by hi
+        o = torch.sort(lo, stable=True).indices
+        o = o[torch.sort(hi[o], stable=True).indices]
+        hs, ls, ps = hi[o], lo[o], pos[o]
+        first = torch.ones_like(hs, dtype=torch.bool)
+        first[1:] = (hs[1:] != hs[:-1]) | (ls[1:] != ls[:-1])
+        keep = torch.sort(ps[first]).values  # first occurrences in draw order
+        have = allc[keep]
+        del allc, hi, lo, pos, o, hs, ls, ps, first, keep, cand
+        if have.shape[0] >= nnz:
+            break
+        want = int(nnz) - have.shape[0]
+    have = have[:nnz].contiguous()
+    if values == "lognormal":
+        vals = torch.exp(torch.randn(have.shape[0], dtype=torch.float32, device=device, generator=gen))
+    else:
+        vals = torch.randn(have.shape[0], dtype=torch.float32, device=device, generator=gen)
+    return np.array(dims, dtype=np.int64), have, vals
+
+
 def _pack(idx, bits):
     """Packs coordinates into two uint64 words per row (most significant mode first)."""
     hi = np.zeros(len(idx), dtype=np.uint64)
