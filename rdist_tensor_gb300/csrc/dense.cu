@@ -54,7 +54,9 @@ __device__ void jacobi_block(int R, const double* __restrict__ A, double* a, dou
                 if (q < R) {
                     double apq = a[p * Re + q];
                     double app = a[p * Re + p], aqq = a[q * Re + q];
-                    if (apq != 0.0 && fabs(apq) > 1e-18 * sqrt(fabs(app * aqq))) {
+                    // Rotate unless a_pq is negligible relative to the
+                    // diagonal (Demmel-Veselic criterion, tol = R * eps).
+                    if (apq != 0.0 && fabs(apq) > (double)R * 2.220446049250313e-16 * sqrt(fabs(app * aqq))) {
                         double tau = (aqq - app) / (2.0 * apq);
                         double tt;
                         if (fabs(tau) > 1e150) {
@@ -119,12 +121,12 @@ __device__ void ascending_ranks(int R, const double* a, int Re, int* rank) {
     }
 }
 
-// One CTA per matrix.  Outputs (any may be null):
+// Eigendecomposition / pseudo-inverse of one matrix by the calling CTA.
+// Outputs (any may be null):
 //   V[u*R + v]    eigenvector v (ascending eigenvalues), lam[v]
 //   pinv          sum over lam_v > tol of v v^T / lam_v  (full symmetric)
-__global__ void syev_kernel(int R, const double* __restrict__ A, int64_t a_stride, double* V, double* lam,
-                            int64_t v_stride, double* pinv, double tol, double* vt_scratch) {
-    extern __shared__ double smem[];
+__device__ void syev_block(int R, const double* __restrict__ A, double* V, double* lam, double* pinv, double tol,
+                           double* vt, double* smem) {
     const int Re = R + (R & 1);
     double* a = smem;
     double* rc = a + Re * Re;
@@ -132,9 +134,9 @@ __global__ void syev_kernel(int R, const double* __restrict__ A, int64_t a_strid
     int* rank = reinterpret_cast<int*>(rs + Re / 2 + 1);
     int* order = rank + Re;
     int* flag = order + Re;
-    const int b = blockIdx.x;
-    double* vt = vt_scratch + (int64_t)b * Re * Re;
-    jacobi_block(R, A + b * a_stride, a, vt, rc, rs, flag);
+    const int b = 0;
+    const int64_t v_stride = 0;
+    jacobi_block(R, A, a, vt, rc, rs, flag);
     __syncthreads();
     ascending_ranks(R, a, Re, rank);
     __syncthreads();
@@ -166,6 +168,104 @@ __global__ void syev_kernel(int R, const double* __restrict__ A, int64_t a_strid
             pinv[b * (int64_t)R * R + e] = acc;
         }
     }
+}
+
+// One CTA per matrix (matrix b at A + b * a_stride).
+__global__ void syev_kernel(int R, const double* __restrict__ A, int64_t a_stride, double* V, double* lam,
+                            int64_t v_stride, double* pinv, double tol, double* vt_scratch) {
+    extern __shared__ double smem[];
+    const int Re = R + (R & 1);
+    const int b = blockIdx.x;
+    syev_block(R, A + b * a_stride, V ? V + b * v_stride : nullptr, lam ? lam + (int64_t)b * R : nullptr,
+               pinv ? pinv + (int64_t)b * R * R : nullptr, tol, vt_scratch + (int64_t)b * Re * Re, smem);
+}
+
+// Symmetric pseudo-inverse, fast path: Cholesky A = L L^T, L^{-1} by
+// substitution, A^{-1} = L^{-T} L^{-1}.  A^{-1} equals the thresholded
+// pseudo-inverse when every eigenvalue exceeds tol; the path is taken only
+// when lambda_min >= 1 / ||A^{-1}||_F > 10 tol (a guaranteed lower bound,
+// with margin for rounding).  Otherwise — not positive definite, or possibly
+// an eigenvalue near or below tol — the same CTA computes the Jacobi
+// pseudo-inverse (compute_pinv_square semantics).
+__global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
+                                double* vt_scratch) {
+    extern __shared__ double smem[];
+    __shared__ int fail;
+    __shared__ double fro;
+    double* L = smem;
+    double* Li = smem + R * R;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < R * R; e += nt) {
+        int i = e / R, j = e % R;
+        L[e] = (i <= j) ? A[i * R + j] : A[j * R + i];
+        Li[e] = 0.0;
+    }
+    if (tid == 0) {
+        fail = 0;
+        fro = 0.0;
+    }
+    __syncthreads();
+    for (int k = 0; k < R; k++) {
+        if (tid == 0) {
+            double d = L[k * R + k];
+            if (!(d > 0.0) || !isfinite(d)) fail = 1;
+            else L[k * R + k] = sqrt(d);
+        }
+        __syncthreads();
+        if (fail) break;
+        const double lkk = L[k * R + k];
+        for (int i = k + 1 + tid; i < R; i += nt) L[i * R + k] /= lkk;
+        __syncthreads();
+        const int m = R - k - 1;
+        for (int e = tid; e < m * m; e += nt) {
+            int i = k + 1 + e / m, j = k + 1 + e % m;
+            if (j <= i) L[i * R + j] -= L[i * R + k] * L[j * R + k];
+        }
+        __syncthreads();
+    }
+    if (!fail) {
+        for (int c = tid; c < R; c += nt) {
+            for (int i = c; i < R; i++) {
+                double s = (i == c) ? 1.0 : 0.0;
+                for (int t = c; t < i; t++) s -= L[i * R + t] * Li[t * R + c];
+                Li[i * R + c] = s / L[i * R + i];
+            }
+        }
+        __syncthreads();
+        double part = 0.0;
+        for (int e = tid; e < R * R; e += nt) {
+            int a = e / R, b = e % R;
+            int k0 = a > b ? a : b;
+            double acc = 0.0;
+            for (int k = k0; k < R; k++) acc = fma(Li[k * R + a], Li[k * R + b], acc);
+            out[e] = acc;
+            part += acc * acc;
+        }
+        part = warp_sum(part);
+        if ((tid & 31) == 0) atomicAdd(&fro, part);
+        __syncthreads();
+        const double bound = 1.0 / sqrt(fro);
+        if (isfinite(fro) && bound > 10.0 * tol) return;
+        __syncthreads();
+    }
+    syev_block(R, A, nullptr, nullptr, out, tol, vt_scratch, smem);
+}
+
+size_t pinv_smem_bytes(int R) {
+    size_t chol = sizeof(double) * 2 * (size_t)R * R;
+    int Re = R + (R & 1);
+    size_t jac = sizeof(double) * ((size_t)Re * Re + Re + 2) + sizeof(int) * (2 * Re + 1) + 16;
+    return chol > jac ? chol : jac;
+}
+
+int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream) {
+    size_t smem = pinv_smem_bytes(R);
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(spd_pinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    spd_pinv_kernel<<<1, R <= 32 ? 256 : 512, smem, stream>>>(R, A, out, tol, vt_scratch);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
 }
 
 size_t syev_smem_bytes(int R) {
@@ -212,5 +312,5 @@ extern "C" int exafac_pinv_square(int32_t R, const double* A, double* out, doubl
     EXAFAC_ARG(R >= 1 && R <= kMaxRank, "exafac_pinv_square: R out of range");
     EXAFAC_ARG(A && out && workspace, "exafac_pinv_square: null pointer");
     EXAFAC_ARG(workspace_bytes >= exafac_dense_workspace_bytes(R), "exafac_pinv_square: workspace too small");
-    return launch_syev(R, A, 0, 1, nullptr, nullptr, 0, out, tol, (double*)workspace, (cudaStream_t)stream);
+    return launch_pinv(R, A, out, tol, (double*)workspace, (cudaStream_t)stream);
 }

@@ -13,4 +13,8 @@ size_t syev_scratch_doubles(int R, int batch);
 int launch_syev(int R, const double* A, int64_t a_stride, int batch, double* V, double* lam, int64_t v_stride,
                 double* pinv, double tol, double* vt_scratch, cudaStream_t stream);
 
+// Symmetric pseudo-inverse (eigenvalues <= tol dropped) of one matrix:
+// Cholesky inverse when provably well conditioned, Jacobi otherwise.
+int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
+
 }  // namespace exafac

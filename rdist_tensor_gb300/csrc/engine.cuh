@@ -112,6 +112,15 @@ struct Session {
     int64_t* dims_dev = nullptr;  // [kMaxModes]
     double* Mexact = nullptr;     // Imax x R (exact MTTKRP)
     double* scal = nullptr;       // [8] device scalars (norms, fit terms)
+    // load-balanced MTTKRP
+    uint32_t* ex_row = nullptr;   // nnz: hits in sample order
+    uint32_t* ex_j = nullptr;
+    double* ex_val = nullptr;
+    uint32_t* hit_row = nullptr;  // nnz: output row of each row-grouped hit
+    double* Mc = nullptr;         // Imax x R: MTTKRP rows by touched-row index
+    double* carry_first = nullptr;
+    double* carry_last = nullptr;
+    float* Df = nullptr;          // Jmax x R design rows (mixed forms)
 
     uint64_t seed = 0x5eed;
     uint64_t counter = 0;
@@ -131,6 +140,18 @@ int design_gram(Session& s, int n, int64_t J, cudaStream_t st);
 int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist, const int64_t* count_dev,
               double* out_full, cudaStream_t st);
 int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st);
+int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st);
+int touched_rows(Session& s, int64_t I, cudaStream_t st);
+int gram_reduce_to(Session& s, int64_t nblk, double* out, cudaStream_t st);
+int sigma_and_gram(Session& s, cudaStream_t st);
+int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st);
+
+// ---- load-balanced MTTKRP and post-processing, R <= 32 (post_kernels.cu)
+constexpr int kSegChunkHits = 128;
+int mttkrp_rows_balanced(Session& s, int n, cudaStream_t st);
+int mttkrp_solve_balanced(Session& s, int n, cudaStream_t st);
+int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st);
+int mttkrp_scatter_out(Session& s, double* out, cudaStream_t st);
 int spmm_solve(Session& s, int n, cudaStream_t st);
 int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStream_t st);
 int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st);

@@ -95,6 +95,15 @@ static void carve(Session& s) {
     s.dims_dev = a.take<int64_t>(kMaxModes);
     s.Mexact = a.take<double>(I * R);
     s.scal = a.take<double>(8);
+    s.ex_row = a.take<uint32_t>(nnz);
+    s.ex_j = a.take<uint32_t>(nnz);
+    s.ex_val = a.take<double>(nnz);
+    s.hit_row = a.take<uint32_t>(nnz);
+    s.Mc = a.take<double>(I * R);
+    const int64_t chunks = ceil_div(nnz, kSegChunkHits) + 1;
+    s.carry_first = a.take<double>(chunks * R);
+    s.carry_last = a.take<double>(chunks * R);
+    s.Df = a.take<float>(J * R);
 }
 
 static int plan(const exafac_als_config* cfg, Session& s) {
@@ -128,7 +137,9 @@ static int plan(const exafac_als_config* cfg, Session& s) {
     for (int k = 0; k < s.N; k++) s.rtree[k] = make_tree_shape(s.dims[k], s.R);
     s.etree = make_tree_shape(s.R, 1);
     s.dtab = next_pow2(std::max<int64_t>(2 * s.Jmax, 16));
-    s.part_rows = std::max<int64_t>(ceil_div(std::max(s.Jmax, s.Imax), 32), 1);
+    // Gram partials: one per 32-row block of the row kernels, and one per CTA
+    // of the tiled solve (152 * 2 CTAs).
+    s.part_rows = std::max<int64_t>(ceil_div(std::max(s.Jmax, s.Imax), 32), 1024);
     return EXAFAC_OK;
 }
 
@@ -152,7 +163,7 @@ static int refresh_sampler(Session& s, int k, bool all_rows, cudaStream_t st) {
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.gram + (int64_t)k * R * R, s.ngram, sizeof(double) * R * R,
                                     cudaMemcpyDeviceToDevice, st));
     if (s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV) {
-        EXAFAC_TRY(launch_syev(R, s.ngram, 0, 1, nullptr, nullptr, 0, s.upinv, 1e-11, s.vt, st));
+        EXAFAC_TRY(launch_pinv(R, s.ngram, s.upinv, 1e-11, s.vt, st));
         if (all_rows) EXAFAC_CUDA_TRY(cudaMemsetAsync(s.scores[k], 0, sizeof(double) * s.dims[k], st));
         EXAFAC_TRY(arls_leverage(s, k, all_rows, s.upinv, st));
         EXAFAC_TRY(arls_build_cdf(s, k, st));
@@ -336,17 +347,35 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     EXAFAC_TRY(dedup(s, n, J, st));
     EXAFAC_TRY(design_gram(s, n, J, st));
     EXAFAC_TRY(mark(h, 2, st));
-    // R4: fiber lookup, hits grouped by output row, MTTKRP fused with the
-    // R x R solve on the touched rows (the other rows are zero).
+    // R4: fiber lookup, hits grouped by output row, MTTKRP rows, then
+    // U = MTTKRP * Phi on the touched rows (the other rows are zero).
+    const bool arls = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV;
+    const bool tiled = s.R <= 32;
     EXAFAC_TRY(lookup_hits(s, n, J, st));
-    EXAFAC_TRY(zero_factor_rows(s, n, st));
-    EXAFAC_TRY(spmm_solve(s, n, st));
+    if (tiled) {
+        EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
+    } else {
+        EXAFAC_TRY(zero_factor_rows(s, n, st));
+        EXAFAC_TRY(spmm_solve(s, n, st));
+    }
     EXAFAC_TRY(mark(h, 3, st));
-    // R5 (dense reduce) is empty at one rank.  R6: renormalise.
-    EXAFAC_TRY(normalize_factor(s, n, false, st));
+    // R5 (dense reduce) is empty at one rank.  R6: renormalise (and, for
+    // CP-ARLS-LEV, the new leverage scores of the touched rows).
+    if (tiled) {
+        EXAFAC_TRY(normalize_balanced(s, n, arls, st));
+    } else {
+        EXAFAC_TRY(normalize_factor(s, n, false, st));
+        if (arls) {
+            EXAFAC_TRY(launch_pinv(s.R, s.ngram, s.upinv, 1e-11, s.vt, st));
+            EXAFAC_TRY(arls_leverage(s, n, false, s.upinv, st));
+        }
+    }
     EXAFAC_TRY(mark(h, 4, st));
-    // R7: sampler update.
-    EXAFAC_TRY(refresh_sampler(s, n, false, st));
+    // R7: sampler update (CDF of the new scores, or the row tree).
+    EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.gram + (int64_t)n * s.R * s.R, s.ngram, sizeof(double) * s.R * s.R,
+                                    cudaMemcpyDeviceToDevice, st));
+    if (arls) EXAFAC_TRY(arls_build_cdf(s, n, st));
+    else EXAFAC_TRY(launch_tree_build(s.rtree[n], s.R, s.F.U[n], s.treeG[n], st));
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.nzrows[n], s.touched, sizeof(uint32_t) * s.dims[n], cudaMemcpyDeviceToDevice, st));
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.nzcount + n, s.counters + 2, sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
     s.dense[n] = false;
@@ -378,7 +407,8 @@ extern "C" int exafac_als_sampled_mttkrp(exafac_als_t h, int32_t n, int64_t Ju, 
     }
     EXAFAC_TRY(lookup_hits(s, n, std::max<int64_t>(Ju, 1), st));
     EXAFAC_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * s.dims[n] * s.R, st));
-    EXAFAC_TRY(spmm_solve_into(s, n, nullptr, out, st));
+    if (s.R <= 32) EXAFAC_TRY(mttkrp_scatter_out(s, out, st));
+    else EXAFAC_TRY(spmm_solve_into(s, n, nullptr, out, st));
     // The host value of Ju above must outlive the async copy.
     EXAFAC_CUDA_TRY(cudaStreamSynchronize(st));
     return EXAFAC_OK;
@@ -392,7 +422,7 @@ extern "C" int exafac_als_exact_step(exafac_als_t h, int32_t n, void* stream) {
     const int R = s.R;
     EXAFAC_TRY(all_grams(s, st));
     EXAFAC_TRY(chain_gram(s, n, s.dgram, st));
-    EXAFAC_TRY(launch_syev(R, s.dgram, 0, 1, nullptr, nullptr, 0, s.dpinv, 1e-11, s.vt, st));
+    EXAFAC_TRY(launch_pinv(R, s.dgram, s.dpinv, 1e-11, s.vt, st));
     EXAFAC_TRY(exact_mttkrp(s, n, s.Mexact, st));
     EXAFAC_TRY(matmul_rows_sym(s, s.Mexact, s.dpinv, s.F.U[n], s.dims[n], st));
     EXAFAC_TRY(normalize_factor(s, n, true, st));

@@ -212,7 +212,7 @@ int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
     gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram); count_launch();
     EXAFAC_CHECK_LAUNCH();
     // compute_pinv_square (common.h:405-443), eigenvalue cut 1e-11.
-    return launch_syev(R, s.dgram, 0, 1, nullptr, nullptr, 0, s.dpinv, 1e-11, s.vt, st);
+    return launch_pinv(R, s.dgram, s.dpinv, 1e-11, s.vt, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -255,55 +255,6 @@ __global__ void lookup_kernel(KeySpec spec, int64_t J, const int64_t* __restrict
     f_len[j] = len;
 }
 
-// Last j in [0, ju) with f_off[j] <= h.
-__device__ __forceinline__ int64_t hit_owner(const int64_t* __restrict__ f_off, int64_t ju, int64_t h) {
-    int64_t lo = 0, hi = ju;
-    while (hi - lo > 1) {
-        int64_t mid = (lo + hi) >> 1;
-        if (f_off[mid] <= h) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Hits beyond the hit buffers (possible only when the samples given to
-// exafac_als_sampled_mttkrp repeat) are reported and dropped.
-__device__ __forceinline__ int64_t capped_hits(const int64_t* counters, int64_t cap, DeviceStatus* status) {
-    const int64_t H = counters[1];
-    if (H > cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) report(status, EXAFAC_ERR_DEVICE, 4, H, cap);
-        return cap;
-    }
-    return H;
-}
-
-__global__ void hit_count_kernel(const int64_t* __restrict__ counters, const int64_t* __restrict__ f_off,
-                                 const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
-                                 uint32_t* __restrict__ rowcnt, int64_t cap, DeviceStatus* status) {
-    const int64_t ju = counters[0], H = capped_hits(counters, cap, status);
-    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < H; h += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = hit_owner(f_off, ju, h);
-        const uint32_t row = rows_n[(int64_t)f_start[j] + (h - f_off[j])];
-        atomicAdd(&rowcnt[row], 1u);
-    }
-}
-
-__global__ void hit_scatter_kernel(const int64_t* __restrict__ counters, const int64_t* __restrict__ f_off,
-                                   const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
-                                   const double* __restrict__ vals_n, const int64_t* __restrict__ rowoff,
-                                   uint32_t* __restrict__ rowfill, uint32_t* __restrict__ hit_j,
-                                   double* __restrict__ hit_val, int64_t cap) {
-    const int64_t ju = counters[0], H = counters[1] < cap ? counters[1] : cap;
-    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < H; h += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = hit_owner(f_off, ju, h);
-        const int64_t p = (int64_t)f_start[j] + (h - f_off[j]);
-        const uint32_t row = rows_n[p];
-        const int64_t dst = rowoff[row] + atomicAdd(&rowfill[row], 1u);
-        hit_j[dst] = (uint32_t)j;
-        hit_val[dst] = vals_n[p];
-    }
-}
-
 __global__ void row_flag_kernel(int64_t I, const uint32_t* __restrict__ rowcnt, uint32_t* __restrict__ flag) {
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < I; r += (int64_t)gridDim.x * blockDim.x)
         flag[r] = rowcnt[r] > 0 ? 1u : 0u;
@@ -318,7 +269,7 @@ __global__ void row_compact_kernel(int64_t I, const uint32_t* __restrict__ flag,
 // counters[5] += counters[1]: running total of the hits (nonzeros_iterated).
 __global__ void accumulate_kernel(int64_t* total, const int64_t* add) { *total += *add; }
 
-int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
+int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st) {
     const Lookup& L = s.look[n];
     const unsigned blocks = (unsigned)ceil_div(J, 256);
     count_launch();
@@ -331,22 +282,24 @@ int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.f_len, s.f_off, J, s.counters + 1, s.scan_sc, st));
     accumulate_kernel<<<1, 1, 0, st>>>(s.counters + 5, s.counters + 1); count_launch();
-    const int64_t I = s.dims[n];
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowcnt, 0, sizeof(uint32_t) * I, st));
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowfill, 0, sizeof(uint32_t) * I, st));
-    const int hb = 152 * 8;
-    hit_count_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, s.rowcnt, s.nnz, s.status); count_launch();
     EXAFAC_CHECK_LAUNCH();
-    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.rowcnt, s.rowoff, I, s.counters + 3, s.scan_sc, st));
-    // Touched rows in increasing order: flags reuse the rowfill buffer's twin.
+    return EXAFAC_OK;
+}
+
+// Rows with at least one hit, in increasing order (touched list), and each
+// row's index in that list (pos, the exclusive scan of the flags).
+int touched_rows(Session& s, int64_t I, cudaStream_t st) {
     row_flag_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.rowcnt, s.flags); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, I, s.counters + 2, s.scan_sc, st));
     row_compact_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.flags, s.pos, s.touched); count_launch();
-    hit_scatter_kernel<<<hb, 256, 0, st>>>(s.counters, s.f_off, s.f_start, L.rows, L.vals, s.rowoff, s.rowfill,
-                                           s.hit_j, s.hit_val, s.nnz); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
+}
+
+int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
+    EXAFAC_TRY(lookup_fibers(s, n, J, st));
+    return mttkrp_rows_balanced(s, n, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -427,7 +380,8 @@ __global__ void sigma_kernel(int R, const double* __restrict__ ugram, double* __
 
 __global__ void scale_rows_kernel(int R, int64_t I, const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
                                   const double* __restrict__ sigma, const int* __restrict__ degenerate,
-                                  double* __restrict__ U) {
+                                  double* __restrict__ U, int only_degenerate) {
+    if (only_degenerate && *degenerate == 0) return;
     const bool all = *degenerate != 0 || list == nullptr;
     const int64_t rows = all ? I : *cnt_dev;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < rows * R; e += (int64_t)gridDim.x * blockDim.x) {
@@ -445,7 +399,31 @@ int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st) {
     int* deg = reinterpret_cast<int*>(s.counters + 6);
     sigma_kernel<<<1, 256, 0, st>>>(R, s.ugram, s.F.sigma, s.ngram, deg); count_launch();
     scale_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.dims[n], list, s.counters + 2, s.F.sigma,
-                                                                     deg, s.F.U[n]); count_launch();
+                                                                     deg, s.F.U[n], 0); count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+int gram_reduce_to(Session& s, int64_t nblk, double* out, cudaStream_t st) {
+    gram_reduce_kernel<<<packed_size(s.R), 256, 0, st>>>(s.part, nblk, s.R, out); count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+int sigma_and_gram(Session& s, cudaStream_t st) {
+    sigma_kernel<<<1, 256, 0, st>>>(s.R, s.ugram, s.F.sigma, s.ngram, reinterpret_cast<int*>(s.counters + 6));
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// The reference divides every row by the column norms; when a norm is zero
+// the rows outside the touched list turn into NaN there too.  Exits at once
+// unless a norm is zero.
+int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st) {
+    scale_rows_kernel<<<152 * 4, 256, 0, st>>>(s.R, s.dims[n], nullptr, s.counters + 2, s.F.sigma,
+                                               reinterpret_cast<int*>(s.counters + 6), s.F.U[n], 1);
+    count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
