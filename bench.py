@@ -261,29 +261,42 @@ def run_gpu(args, w):
     dims, idx, vals = make_workload(w, seed=args.seed + rank)
     N, R, J = len(dims), w["R"], w["J"]
     nnz = int(idx.shape[0])
-    opt, lr, st = build_optimizer(w, dims, idx, vals, J, args.precision)
-    for _ in range(args.warmup):
-        sweep(opt, N, J)
-    torch.cuda.synchronize()
 
-    # ---- timed region: K sweeps, tensor resident -------------------------
+    def timed(opt, clocks=None):
+        for _ in range(args.warmup):
+            sweep(opt, N, J)
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        l0 = lib.exafac_kernel_launches()
+        barrier(ws)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            sweep(opt, N, J)
+        e1.record()
+        torch.cuda.synchronize()
+        barrier(ws)
+        el = max_over_ranks(e0.elapsed_time(e1) * 1e-3, ws)
+        return el, lib.exafac_kernel_launches() - l0, opt.compute_exact_fit()
+
+    # ---- the FP64 form (the reference's arithmetic) -----------------------
+    ref_form = None
+    if args.precision != "fp64":
+        opt64, _, _ = build_optimizer(w, dims, idx, vals, J, "fp64")
+        el64, _, fit64 = timed(opt64)
+        opt64.deinitialize()
+        del opt64
+        torch.cuda.empty_cache()
+        ref_form = {"precision": "fp64", "sweeps_per_s": ws * args.steps / el64, "fit_after": fit64}
+
+    # ---- timed region: K sweeps of the measured form, tensor resident -----
+    opt, lr, st = build_optimizer(w, dims, idx, vals, J, args.precision)
     clocks = ClockSampler(local)
-    clocks.start()
-    launches0 = lib.exafac_kernel_launches()
-    barrier(ws)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        sweep(opt, N, J)
-    e1.record()
-    torch.cuda.synchronize()
-    barrier(ws)
-    launches = lib.exafac_kernel_launches() - launches0
-    elapsed = max_over_ranks(e0.elapsed_time(e1) * 1e-3, ws)
+    elapsed, launches, fit = timed(opt, clocks)
     clk = clocks.stop()
     value = ws * args.steps / elapsed
-    fit = opt.compute_exact_fit()
 
     # ---- roofline of the sampled MTTKRP (region timers, one sweep) -------
     _lib.call("exafac_als_enable_timing", opt._h, 1)
@@ -339,15 +352,20 @@ def run_gpu(args, w):
     opt.deinitialize()
     if rank != 0:
         return 0
+    dtype = "f64" if args.precision == "fp64" else f"{args.precision} design Gram, fp32 row products, fp64 solve/CDF"
+    cfg = {"workload": w["desc"], "nnz": nnz, "R": R, "J": J, "sampler": w["sampler"], "precision": args.precision,
+           "preprocessing": "one exact-ALS sweep, untimed", "parallelism": f"{ws} independent replica(s)",
+           "l2": "inputs larger than L2 (per-mode sorted copies and hash tables, tens of GB)", "fit_after": fit}
+    if ref_form is not None:
+        cfg["fp64_form"] = ref_form
+        cfg["speedup_vs_fp64_form"] = value / ref_form["sweeps_per_s"]
+        cfg["fit_gap_vs_fp64_form"] = abs(fit - ref_form["fit_after"])
+        cfg["equal_fit_1e-3"] = bool(abs(fit - ref_form["fit_after"]) <= 1e-3)
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else args.precision,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded Zipf coordinates, log-normal values; no public dataset)",
-            "config": {"workload": w["desc"], "nnz": nnz, "R": R, "J": J, "sampler": w["sampler"],
-                       "precision": args.precision, "preprocessing": "one exact-ALS sweep, untimed",
-                       "parallelism": f"{ws} independent replica(s)",
-                       "l2": "inputs larger than L2 (per-mode sorted copies and hash tables, tens of GB)",
-                       "fit_after": fit},
+            "config": cfg,
             "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
     if cpu is not None:
         line["cpu_baseline"] = cpu
@@ -362,7 +380,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="zipf4", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16"])
+    ap.add_argument("--precision", default="tf32", choices=["fp64", "tf32", "bf16"],
+                    help="form timed for `value`; a mixed form is also compared with the FP64 form")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sweeps", type=int, default=3)

@@ -187,8 +187,37 @@ __global__ void syev_kernel(int R, const double* __restrict__ A, int64_t a_strid
 // with margin for rounding).  Otherwise — not positive definite, or possibly
 // an eigenvalue near or below tol — the same CTA computes the Jacobi
 // pseudo-inverse (compute_pinv_square semantics).
+// One Newton step on an (pseudo-)inverse X of A: X <- 2X - X A X, in FP64.
+// A pseudo-inverse is a fixed point of the step.  smem: 3 R^2 doubles.
+__device__ void newton_refine(int R, const double* __restrict__ A, double* __restrict__ out, double* smem) {
+    double* X = smem;
+    double* As = smem + R * R;
+    double* T = smem + 2 * R * R;
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+        X[e] = out[e];
+        int i = e / R, j = e % R;
+        As[e] = (i <= j) ? A[i * R + j] : A[j * R + i];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {  // T = A X
+        int i = e / R, j = e % R;
+        double acc = 0.0;
+        for (int k = 0; k < R; k++) acc = fma(As[i * R + k], X[k * R + j], acc);
+        T[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {  // out = 2X - X T
+        int i = e / R, j = e % R;
+        double acc = 0.0;
+        for (int k = 0; k < R; k++) acc = fma(X[i * R + k], T[k * R + j], acc);
+        out[e] = 2.0 * X[e] - acc;
+    }
+    __syncthreads();
+}
+
 __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
-                                double* vt_scratch) {
+                                double* vt_scratch, int refine) {
     extern __shared__ double smem[];
     __shared__ int fail;
     __shared__ double fro;
@@ -245,27 +274,40 @@ __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __r
         if ((tid & 31) == 0) atomicAdd(&fro, part);
         __syncthreads();
         const double bound = 1.0 / sqrt(fro);
-        if (isfinite(fro) && bound > 10.0 * tol) return;
+        if (isfinite(fro) && bound > 10.0 * tol) {
+            if (refine) newton_refine(R, A, out, smem);
+            return;
+        }
         __syncthreads();
     }
     syev_block(R, A, nullptr, nullptr, out, tol, vt_scratch, smem);
+    if (refine) newton_refine(R, A, out, smem);
 }
 
 size_t pinv_smem_bytes(int R) {
-    size_t chol = sizeof(double) * 2 * (size_t)R * R;
+    size_t chol = sizeof(double) * 3 * (size_t)R * R;
     int Re = R + (R & 1);
     size_t jac = sizeof(double) * ((size_t)Re * Re + Re + 2) + sizeof(int) * (2 * Re + 1) + 16;
     return chol > jac ? chol : jac;
 }
 
-int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream) {
+static int launch_pinv_impl(int R, const double* A, double* out, double tol, double* vt_scratch, int refine,
+                            cudaStream_t stream) {
     size_t smem = pinv_smem_bytes(R);
     if (smem > 48 * 1024)
         EXAFAC_CUDA_TRY(cudaFuncSetAttribute(spd_pinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    spd_pinv_kernel<<<1, R <= 32 ? 256 : 512, smem, stream>>>(R, A, out, tol, vt_scratch);
+    spd_pinv_kernel<<<1, R <= 32 ? 256 : 512, smem, stream>>>(R, A, out, tol, vt_scratch, refine);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
+}
+
+int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream) {
+    return launch_pinv_impl(R, A, out, tol, vt_scratch, 0, stream);
+}
+
+int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream) {
+    return launch_pinv_impl(R, A, out, tol, vt_scratch, 1, stream);
 }
 
 size_t syev_smem_bytes(int R) {

@@ -17,4 +17,8 @@ int launch_syev(int R, const double* A, int64_t a_stride, int batch, double* V, 
 // Cholesky inverse when provably well conditioned, Jacobi otherwise.
 int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
 
+// The same followed by one Newton step X <- 2X - X A X (the refinement the
+// mixed forms apply to the solve).
+int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
+
 }  // namespace exafac

@@ -248,9 +248,13 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
     __shared__ double sg[32];
     __shared__ TA tile[kNormWarps][32][33];  // a warp's 32 rows, padded
     if (*degenerate) return;        // handled over all rows by scale_rows
+    // P is symmetric: u^T P u = sum_a u_a (P_aa u_a + 2 sum_{b>a} P_ab u_b);
+    // psm holds P_aa on the diagonal and 2 P_ab above it.
     for (int e = threadIdx.x; e < R * R; e += blockDim.x)
-        if (Pm) psm[e] = (TA)Pm[e];
-    for (int c = threadIdx.x; c < R; c += blockDim.x) sg[c] = sigma[c];
+        if (Pm) psm[e] = (TA)((e / R == e % R) ? Pm[e] : 2.0 * Pm[e]);
+    // Multiplying by 1/sigma differs from the reference's division by at
+    // most one rounding.
+    for (int c = threadIdx.x; c < R; c += blockDim.x) sg[c] = 1.0 / sigma[c];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     TA (*ut)[33] = tile[w];
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
         if (i < nt) {
             const int64_t row = touched[i];
             for (int k = 0; k < R; k++) {
-                const double v = U[row * R + k] / sg[k];
+                const double v = U[row * R + k] * sg[k];
                 U[row * R + k] = v;
                 ut[lane][k] = (TA)v;
             }
@@ -273,7 +277,7 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
             for (int a = 0; a < R; a++) {
                 TA y = 0;
 #pragma unroll 8
-                for (int b = 0; b < R; b++) y = fma(psm[a * R + b], ut[lane][b], y);
+                for (int b = a; b < R; b++) y = fma(psm[a * R + b], ut[lane][b], y);
                 acc = fma(ut[lane][a], y, acc);
             }
             scores[touched[i]] = (double)acc;

@@ -113,7 +113,10 @@ static int plan(const exafac_als_config* cfg, Session& s) {
     EXAFAC_ARG(cfg->nnz >= 1 && cfg->nnz < (int64_t)0xffffffffll, "nnz must be in [1, 2^32 - 1)");
     EXAFAC_ARG(cfg->J_max >= 1 && cfg->J_max < ((int64_t)1 << 31), "J_max must be in [1, 2^31)");
     EXAFAC_ARG(cfg->sampler == EXAFAC_SAMPLER_CP_ARLS_LEV || cfg->sampler == EXAFAC_SAMPLER_STS_CP, "bad sampler");
-    EXAFAC_ARG(cfg->precision == EXAFAC_PREC_FP64, "only the FP64 form is available in this build");
+    EXAFAC_ARG(cfg->precision == EXAFAC_PREC_FP64 || cfg->precision == EXAFAC_PREC_TF32 ||
+                   cfg->precision == EXAFAC_PREC_BF16,
+               "precision must be FP64, TF32 or BF16");
+    EXAFAC_ARG(cfg->precision == EXAFAC_PREC_FP64 || cfg->R <= 32, "the mixed forms support R <= 32 in this build");
     EXAFAC_ARG(cfg->preprocessing >= 0 && cfg->preprocessing <= 2, "bad preprocessing");
     s.cfg = *cfg;
     s.N = cfg->N;

@@ -2,6 +2,8 @@
 // 173-294 at one rank): deduplication, design rows + Gram, fiber lookup,
 // counting sort of the hits by output row, sampled MTTKRP fused with the
 // R x R solve, column renormalisation; plus the exact fit and exact MTTKRP.
+#include <cuda_bf16.h>
+
 #include "dense.cuh"
 #include "engine.cuh"
 #include "prims.cuh"
@@ -204,9 +206,78 @@ __global__ void design_kernel(int N, int n, int R, const int64_t* __restrict__ j
     }
 }
 
+// Mixed forms: the same design rows, the MTTKRP operand D' kept in FP32, and
+// the Gram of the sqrt(w)-scaled rows from inputs rounded to TF32 (10-bit
+// mantissa, round to nearest) or BF16 (7-bit), products accumulated in FP32
+// within a block of 32 rows — the arithmetic of a tensor-core MMA with FP32
+// accumulation; blocks are summed in FP64.
+__device__ __forceinline__ float round_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+__device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+template <int kRound>  // 1: TF32, 2: BF16
+__global__ void design_mixed_kernel(int N, int n, int R, const int64_t* __restrict__ ju_dev,
+                                    const uint32_t* __restrict__ sd, const double* __restrict__ wd, FactorPtrs f,
+                                    float* __restrict__ Df, double* __restrict__ part) {
+    __shared__ float sm[kGramRows * 32];
+    const int P = packed_size(R);
+    const int64_t ju = *ju_dev;
+    const int64_t base = (int64_t)blockIdx.x * kGramRows;
+    for (int e = threadIdx.x; e < kGramRows * R; e += blockDim.x) {
+        int lr = e / R, c = e % R;
+        int64_t j = base + lr;
+        float v = 0.f;
+        if (j < ju) {
+            double d = 1.0;
+            for (int k = 0; k < N; k++) {
+                if (k == n) continue;
+                d *= f.U[k][(int64_t)sd[j * N + k] * R + c];
+            }
+            const double sw = sqrt(wd[j]);
+            d *= sw;
+            Df[j * R + c] = (float)(d * sw);
+            v = kRound == 1 ? round_tf32((float)d) : round_bf16((float)d);
+        }
+        sm[lr * R + c] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            a++;
+        }
+        int b = a + rem;
+        float acc = 0.f;
+        for (int lr = 0; lr < kGramRows; lr++) acc = fmaf(sm[lr * R + a], sm[lr * R + b], acc);
+        part[(int64_t)blockIdx.x * P + e] = (double)acc;
+    }
+}
+
 int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
     const int R = s.R;
     int64_t nblk = std::max<int64_t>(1, ceil_div(J, kGramRows));
+    if (s.cfg.precision != EXAFAC_PREC_FP64) {
+        if (R > 32) {
+            set_error("mixed precision supports R <= 32 in this build");
+            return EXAFAC_ERR_UNSUPPORTED;
+        }
+        if (s.cfg.precision == EXAFAC_PREC_TF32)
+            design_mixed_kernel<1><<<(unsigned)nblk, 128, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
+                                                                    factor_ptrs(s), s.Df, s.part);
+        else
+            design_mixed_kernel<2><<<(unsigned)nblk, 128, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
+                                                                    factor_ptrs(s), s.Df, s.part);
+        count_launch();
+        gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram); count_launch();
+        EXAFAC_CHECK_LAUNCH();
+        // FP64 Cholesky / pseudo-inverse of the FP32-accumulated Gram, plus
+        // one Newton step X <- X (2I - G X) on the solve.
+        return launch_pinv_refined(R, s.dgram, s.dpinv, 1e-11, s.vt, st);
+    }
     design_kernel<<<(unsigned)nblk, 128, sizeof(double) * kGramRows * R, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
                                                                                factor_ptrs(s), s.D, s.part); count_launch();
     gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram); count_launch();

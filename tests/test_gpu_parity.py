@@ -222,3 +222,70 @@ def test_exact_then_sampled_against_oracle(lib, oracle_mod, sampler):
         assert rel_err(lr.factors[n].data.cpu().numpy(), out["factor"]) < 1e-8
     assert abs(opt.compute_exact_fit() - ora.fit()) < 1e-8
     opt.deinitialize()
+
+
+def make_optimizer_prec(dims, idx, vals, factors, sampler, J_max, precision):
+    from exafac.cpp_ext.py_module import (AccumulatorStationary, CP_ARLS_LEV, Grid, LowRankTensor, STS_CP,
+                                          SparseTensor, TensorGrid)
+
+    N = len(dims)
+    grid = Grid(np.ones(N, dtype=np.int32))
+    tg = TensorGrid(np.asarray(dims, dtype=np.int32), grid)
+    st = SparseTensor(tg, np.asarray(idx, dtype=np.uint32), np.asarray(vals, dtype=np.float64), "none")
+    lr = LowRankTensor(factors[0].shape[1], tg)
+    lr.set_factors(factors)
+    s = CP_ARLS_LEV(lr) if sampler == "cp_arls_lev" else STS_CP(lr)
+    opt = AccumulatorStationary(st, lr, s, max_samples=J_max, precision=precision)
+    opt.initialize_ground_truth_for_als()
+    return opt, lr
+
+
+@pytest.mark.parametrize("precision", ["tf32", "bf16"])
+@pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
+def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler):
+    """First step of the mixed forms (same samples as FP64: the initial
+    sampler state is FP64) against the oracle.  The MTTKRP is accumulated in
+    FP32 from FP32 design rows (relative error ~1e-6); the factor also passes
+    through Phi, the pseudo-inverse of a Gram formed from TF32 (10-bit) or
+    BF16 (7-bit mantissa) products: factor within 1e-3 (TF32) / 2e-2 (BF16)."""
+    from rdist_tensor_gb300 import synthetic
+
+    dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
+    R, J = 16, 8192
+    factors = synthetic.gaussian_factors(dims, R, seed=5)
+    opt, lr = make_optimizer_prec(dims, idx, vals, factors, sampler, J, precision)
+    ora = oracle_mod.OracleALS(dims, idx, vals, factors, sampler)
+    rng = np.random.default_rng(12)
+    shape = (3, J) if sampler == "cp_arls_lev" else (3, 2, J)
+    uni = rng.random(shape)
+    opt.execute_ALS_step(0, J, dev(uni, torch.float64))
+    out = ora.step(0, J, uni)
+    assert opt.step_info().hits == out["hits"]
+    tol = 1e-3 if precision == "tf32" else 2e-2
+    err_u = rel_err(lr.factors[0].data.cpu().numpy(), out["factor"])
+    err_s = rel_err(lr.sigma.cpu().numpy(), out["sigma"])
+    print(f"{precision} {sampler}: factor {err_u:.2e} sigma {err_s:.2e}")
+    assert err_u < tol and err_s < tol
+    opt.deinitialize()
+
+
+@pytest.mark.parametrize("precision", ["tf32", "bf16"])
+@pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
+def test_mixed_equal_fit(lib, precision, sampler):
+    """Fit after 6 sweeps of a sparse sample of a planted rank-5 tensor: mixed
+    form within 1e-3 of the FP64 form driven by the same uniform stream."""
+    from rdist_tensor_gb300 import synthetic
+
+    dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
+    R, J = 8, 8192
+    factors = synthetic.gaussian_factors(dims, R, seed=6)
+    fits = {}
+    for prec in ("fp64", precision):
+        opt, lr = make_optimizer_prec(dims, idx, vals, factors, sampler, J, prec)
+        for _ in range(6):
+            for n in range(3):
+                opt.execute_ALS_step(n, J)
+        fits[prec] = opt.compute_exact_fit()
+        opt.deinitialize()
+    assert np.isfinite(fits["fp64"]) and fits["fp64"] > 0.0
+    assert abs(fits[precision] - fits["fp64"]) < 1e-3, fits
