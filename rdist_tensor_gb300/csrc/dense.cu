@@ -217,13 +217,17 @@ __device__ void newton_refine(int R, const double* __restrict__ A, double* __res
 }
 
 __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
-                                double* vt_scratch, int refine) {
+                                double* vt_scratch, int refine, int fast) {
     extern __shared__ double smem[];
     __shared__ int fail;
     __shared__ double fro;
     double* L = smem;
     double* Li = smem + R * R;
     const int tid = threadIdx.x, nt = blockDim.x;
+    if (!fast) {  // the Cholesky buffers do not fit in shared memory
+        syev_block(R, A, nullptr, nullptr, out, tol, vt_scratch, smem);
+        return;
+    }
     for (int e = tid; e < R * R; e += nt) {
         int i = e / R, j = e % R;
         L[e] = (i <= j) ? A[i * R + j] : A[j * R + i];
@@ -284,19 +288,26 @@ __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __r
     if (refine) newton_refine(R, A, out, smem);
 }
 
+// Shared memory of the Cholesky path (L, L^{-1}, and the Newton step's
+// third matrix).  The Cholesky path is used when its buffers fit under
+// kPinvSmemCap (R <= 92); larger ranks go straight to Jacobi, unrefined
+// (refinement is only requested by the mixed forms, which need R <= 32).
+static size_t chol_smem_bytes(int R) { return sizeof(double) * 3 * (size_t)R * R; }
+constexpr size_t kPinvSmemCap = 200 * 1024;
+
 size_t pinv_smem_bytes(int R) {
-    size_t chol = sizeof(double) * 3 * (size_t)R * R;
-    int Re = R + (R & 1);
-    size_t jac = sizeof(double) * ((size_t)Re * Re + Re + 2) + sizeof(int) * (2 * Re + 1) + 16;
-    return chol > jac ? chol : jac;
+    size_t jac = syev_smem_bytes(R);
+    if (chol_smem_bytes(R) > kPinvSmemCap) return jac;
+    return std::max(chol_smem_bytes(R), jac);
 }
 
 static int launch_pinv_impl(int R, const double* A, double* out, double tol, double* vt_scratch, int refine,
                             cudaStream_t stream) {
+    const int fast = chol_smem_bytes(R) <= kPinvSmemCap;
     size_t smem = pinv_smem_bytes(R);
     if (smem > 48 * 1024)
         EXAFAC_CUDA_TRY(cudaFuncSetAttribute(spd_pinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    spd_pinv_kernel<<<1, R <= 32 ? 256 : 512, smem, stream>>>(R, A, out, tol, vt_scratch, refine);
+    spd_pinv_kernel<<<1, R <= 32 ? 256 : 512, smem, stream>>>(R, A, out, tol, vt_scratch, fast ? refine : 0, fast);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

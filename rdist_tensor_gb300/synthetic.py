@@ -20,7 +20,7 @@ from __future__ import annotations
 import numpy as np
 
 
-def planted_uniform(dims=(2000, 2000, 2000), nnz=2_000_000, rank=10, noise_var=0.01, seed=0):
+def planted_uniform(dims=(2000, 2000, 2000), nnz=2_000_000, rank=10, noise_var=0.01, seed=0, nonneg=True):
     rng = np.random.default_rng(seed)
     dims = tuple(int(d) for d in dims)
     total = int(np.prod(np.array(dims, dtype=np.float64)))
@@ -34,7 +34,9 @@ def planted_uniform(dims=(2000, 2000, 2000), nnz=2_000_000, rank=10, noise_var=0
         lin = cand[np.sort(first)]
     lin = lin[:nnz]
     idx = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.uint32)
-    A = [np.abs(rng.standard_normal((d, rank))) for d in dims]
+    A = [rng.standard_normal((d, rank)) for d in dims]
+    if nonneg:
+        A = [np.abs(a) for a in A]
     model = np.ones((nnz, rank))
     for k, Ak in enumerate(A):
         model *= Ak[idx[:, k]]

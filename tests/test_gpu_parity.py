@@ -88,6 +88,22 @@ def test_pinv_square(lib, golden, case):
     assert rel_err(out.cpu().numpy()[iu], ref[iu]) < 1e-10
 
 
+@pytest.mark.parametrize("R,rank", [(92, 92), (93, 93), (128, 128), (128, 70)])
+def test_pinv_square_large_rank(lib, R, rank):
+    """Ranks on both sides of the largest one whose Cholesky buffers fit in
+    shared memory (92); above it the Jacobi path runs alone."""
+    rng = np.random.default_rng(R + rank)
+    B = rng.standard_normal((R + 5, rank))
+    A = B[:R] @ B[:R].T if rank < R else B.T @ B
+    Ad = dev(A, torch.float64)
+    out = torch.zeros((R, R), dtype=torch.float64, device="cuda")
+    nbytes = lib.load().exafac_dense_workspace_bytes(R)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    lib.call("exafac_pinv_square", R, P(Ad), P(out), ctypes.c_double(1e-11), P(ws), ctypes.c_size_t(nbytes), None)
+    ref = np.linalg.pinv(A, rcond=1e-10, hermitian=True)
+    assert rel_err(out.cpu().numpy(), ref) < 1e-9
+
+
 def test_syev_matches_lapack(lib):
     rng = np.random.default_rng(3)
     for R in (1, 2, 5, 25, 32, 64):
@@ -272,20 +288,21 @@ def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler):
 @pytest.mark.parametrize("precision", ["tf32", "bf16"])
 @pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
 def test_mixed_equal_fit(lib, precision, sampler):
-    """Fit after 6 sweeps of a sparse sample of a planted rank-5 tensor: mixed
-    form within 1e-3 of the FP64 form driven by the same uniform stream."""
+    """Fit after 20 sweeps on a planted rank-5 tensor (signed factors) with 5/6
+    of its entries observed (the fit converges, so sampling noise is small):
+    mixed form within 1e-3 of the FP64 form driven by the same uniforms."""
     from rdist_tensor_gb300 import synthetic
 
-    dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
-    R, J = 8, 8192
+    dims, idx, vals = synthetic.planted_uniform(dims=(60, 50, 40), nnz=100000, rank=5, seed=3, nonneg=False)
+    R, J = 5, 4096
     factors = synthetic.gaussian_factors(dims, R, seed=6)
     fits = {}
     for prec in ("fp64", precision):
         opt, lr = make_optimizer_prec(dims, idx, vals, factors, sampler, J, prec)
-        for _ in range(6):
+        for _ in range(20):
             for n in range(3):
                 opt.execute_ALS_step(n, J)
         fits[prec] = opt.compute_exact_fit()
         opt.deinitialize()
-    assert np.isfinite(fits["fp64"]) and fits["fp64"] > 0.0
+    assert fits["fp64"] > 0.5, fits
     assert abs(fits[precision] - fits["fp64"]) < 1e-3, fits
