@@ -94,6 +94,15 @@ int exafac_pinv_square(int32_t R, const double* A_dev, double* out_dev, double t
 /* Device workspace bytes exafac_syev / exafac_pinv_square need for rank R. */
 size_t exafac_dense_workspace_bytes(int32_t R);
 
+/* exafac_pinv_square without a workspace argument, for callers that cannot
+ * allocate device memory (their memory belongs to another framework's pool,
+ * or allocation is not allowed where they run).  No counterpart in the
+ * reference.  Scratch is a static 128 KiB device array shared by all calls
+ * on a device: R must be <= 128; calls that overlap on the GPU race on it.
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress), so make it before any stream capture. */
+int exafac_pinv_square_static(int32_t R, const double* A_dev, double* out_dev, double tol, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Session: SparseTensor + LowRankTensor + Sampler + AccumulatorStationary
  * (py_module.cpp:37-77) on one GPU.

@@ -55,6 +55,7 @@ SIGNATURES = {
     "exafac_syev": (ctypes.c_int, [_I32, _P, _P, _P, _P, _SZ, _P]),
     "exafac_pinv_square": (ctypes.c_int, [_I32, _P, _P, ctypes.c_double, _P, _SZ, _P]),
     "exafac_dense_workspace_bytes": (_SZ, [_I32]),
+    "exafac_pinv_square_static": (ctypes.c_int, [_I32, _P, _P, ctypes.c_double, _P]),
     "exafac_als_workspace_size": (ctypes.c_int, [ctypes.POINTER(AlsConfig), ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
     "exafac_als_create": (ctypes.c_int, [ctypes.POINTER(AlsConfig), _P, _SZ, ctypes.POINTER(_P)]),
     "exafac_als_destroy": (ctypes.c_int, [_P]),
