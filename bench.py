@@ -283,7 +283,7 @@ def run_gpu(args, w):
 
     # ---- the FP64 form (the reference's arithmetic) -----------------------
     ref_form = None
-    if args.precision != "fp64":
+    if args.precision != "fp64" and not args.no_fp64_form:
         opt64, _, _ = build_optimizer(w, dims, idx, vals, J, "fp64")
         el64, _, fit64 = timed(opt64)
         opt64.deinitialize()
@@ -385,6 +385,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sweeps", type=int, default=3)
+    ap.add_argument("--no-fp64-form", action="store_true",
+                    help="skip timing the FP64 form beside a mixed form (for kernel profiling runs)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

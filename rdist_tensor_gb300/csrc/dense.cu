@@ -288,6 +288,114 @@ __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __r
     if (refine) newton_refine(R, A, out, smem);
 }
 
+// R <= 32: the symmetric sweep operator (Gauss-Jordan with diagonal pivots,
+// stable without pivoting on a positive-definite matrix) with the upper
+// triangle held in registers, kSmallPinvEpt elements per thread, and one
+// barrier per pivot.  Sweeping every pivot leaves -A^{-1}.  A non-positive
+// pivot means A is not positive definite.  The same acceptance test as the
+// Cholesky path (lambda_min >= 1/||A^{-1}||_F > 10 tol) guards the result;
+// otherwise the CTA computes the Jacobi pseudo-inverse.
+//
+// The refinement (refine != 0) is the Newton step written as
+// X + X (I - A X): the residual I - A X is formed in FP64 and the small
+// correction X (I - A X) in FP32, which keeps the FP64 pipe (the scarce one
+// on this part) to a single R^3 product.
+constexpr int kSmallPinvThreads = 128;
+constexpr int kSmallPinvMaxR = 32;
+constexpr int kSmallPinvEpt = (kSmallPinvMaxR * (kSmallPinvMaxR + 1) / 2 + kSmallPinvThreads - 1) / kSmallPinvThreads;
+
+__global__ void __launch_bounds__(kSmallPinvThreads)
+    spd_pinv_small_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
+                          double* vt_scratch, int refine) {
+    extern __shared__ double smem[];  // Jacobi fallback / FP64 Newton step
+    __shared__ double rowbuf[2][kSmallPinvMaxR];
+    __shared__ double Xs[kSmallPinvMaxR][kSmallPinvMaxR + 1];
+    __shared__ double Es[kSmallPinvMaxR][kSmallPinvMaxR + 1];
+    __shared__ double fro;
+    const int tid = threadIdx.x;
+    const int P = R * (R + 1) / 2;
+    int ii[kSmallPinvEpt], jj[kSmallPinvEpt];
+    double a[kSmallPinvEpt];
+#pragma unroll
+    for (int m = 0; m < kSmallPinvEpt; m++) {
+        const int e = tid + kSmallPinvThreads * m;
+        int i = 0, base = 0;
+        while (i < R - 1 && e >= base + (R - i)) {
+            base += R - i;
+            i++;
+        }
+        ii[m] = (e < P) ? i : -1;
+        jj[m] = (e < P) ? i + (e - base) : -1;
+        a[m] = (e < P) ? A[i * R + jj[m]] : 0.0;
+    }
+    if (tid < R) rowbuf[0][tid] = A[tid];
+    if (tid == 0) fro = 0.0;
+    __syncthreads();
+    bool ok = true;
+    for (int k = 0; k < R; k++) {
+        const double* r = rowbuf[k & 1];
+        double* nr = rowbuf[(k + 1) & 1];
+        const double piv = r[k];  // same value in every thread: the exit is uniform
+        if (!(piv > 0.0) || !isfinite(piv)) {
+            ok = false;
+            break;
+        }
+        const double p = 1.0 / piv;
+#pragma unroll
+        for (int m = 0; m < kSmallPinvEpt; m++) {
+            const int i = ii[m], j = jj[m];
+            if (i < 0) continue;
+            double v;
+            if (i != k && j != k) v = fma(-r[i] * p, r[j], a[m]);
+            else if (i == k && j == k) v = -p;
+            else v = r[i == k ? j : i] * p;
+            a[m] = v;
+            if (i == k + 1) nr[j] = v;
+            else if (j == k + 1) nr[i] = v;
+        }
+        __syncthreads();
+    }
+    if (ok) {
+        double part = 0.0;
+#pragma unroll
+        for (int m = 0; m < kSmallPinvEpt; m++) {
+            if (ii[m] < 0) continue;
+            const double x = -a[m];
+            a[m] = x;
+            part += (ii[m] == jj[m] ? 1.0 : 2.0) * x * x;
+            Xs[ii[m]][jj[m]] = x;
+            Xs[jj[m]][ii[m]] = x;
+        }
+        part = warp_sum(part);
+        if ((tid & 31) == 0) atomicAdd(&fro, part);
+        __syncthreads();
+        ok = isfinite(fro) && 1.0 / sqrt(fro) > 10.0 * tol;
+    }
+    if (ok) {
+        if (!refine) {
+            for (int e = tid; e < R * R; e += kSmallPinvThreads) out[e] = Xs[e / R][e % R];
+            return;
+        }
+        for (int e = tid; e < R * R; e += kSmallPinvThreads) {  // E = I - A X
+            const int i = e / R, j = e % R;
+            double acc = (i == j) ? 1.0 : 0.0;
+            for (int t = 0; t < R; t++) acc = fma(-A[(i <= t) ? i * R + t : t * R + i], Xs[t][j], acc);
+            Es[i][j] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < R * R; e += kSmallPinvThreads) {  // out = X + X E
+            const int i = e / R, j = e % R;
+            float c = 0.0f;
+            for (int t = 0; t < R; t++) c = fmaf((float)Xs[i][t], (float)Es[t][j], c);
+            out[e] = Xs[i][j] + (double)c;
+        }
+        return;
+    }
+    __syncthreads();
+    syev_block(R, A, nullptr, nullptr, out, tol, vt_scratch, smem);
+    if (refine) newton_refine(R, A, out, smem);
+}
+
 // Shared memory of the Cholesky path (L, L^{-1}, and the Newton step's
 // third matrix).  The Cholesky path is used when its buffers fit under
 // kPinvSmemCap (R <= 92); larger ranks go straight to Jacobi, unrefined
@@ -303,6 +411,13 @@ size_t pinv_smem_bytes(int R) {
 
 static int launch_pinv_impl(int R, const double* A, double* out, double tol, double* vt_scratch, int refine,
                             cudaStream_t stream) {
+    if (R <= kSmallPinvMaxR) {
+        const size_t smem = std::max(syev_smem_bytes(R), chol_smem_bytes(R));
+        spd_pinv_small_kernel<<<1, kSmallPinvThreads, smem, stream>>>(R, A, out, tol, vt_scratch, refine);
+        count_launch();
+        EXAFAC_CHECK_LAUNCH();
+        return EXAFAC_OK;
+    }
     const int fast = chol_smem_bytes(R) <= kPinvSmemCap;
     size_t smem = pinv_smem_bytes(R);
     if (smem > 48 * 1024)

@@ -97,12 +97,8 @@ struct Session {
     uint32_t* f_start = nullptr;
     uint32_t* f_len = nullptr;
     int64_t* f_off = nullptr;
-    uint32_t* rowcnt = nullptr;   // Imax
-    uint32_t* rowfill = nullptr;  // Imax
-    int64_t* rowoff = nullptr;    // Imax
-    uint32_t* hit_j = nullptr;    // nnz
-    double* hit_val = nullptr;    // nnz
-    uint32_t* touched = nullptr;  // Imax
+    uint32_t* touched = nullptr;  // Imax: rows with hits, increasing
+    int64_t* seg_start = nullptr; // Imax + 1: first sorted hit of each touched row, then H
     double* ugram = nullptr;      // R x R
     double* ngram = nullptr;      // R x R normalised factor Gram
     double* upinv = nullptr;      // R x R
@@ -112,14 +108,21 @@ struct Session {
     int64_t* dims_dev = nullptr;  // [kMaxModes]
     double* Mexact = nullptr;     // Imax x R (exact MTTKRP)
     double* scal = nullptr;       // [8] device scalars (norms, fit terms)
-    // load-balanced MTTKRP
-    uint32_t* ex_row = nullptr;   // nnz: hits in sample order
-    uint32_t* ex_j = nullptr;
-    double* ex_val = nullptr;
-    uint32_t* hit_row = nullptr;  // nnz: output row of each row-grouped hit
-    double* Mc = nullptr;         // Imax x R: MTTKRP rows by touched-row index
-    double* carry_first = nullptr;
-    double* carry_last = nullptr;
+    // hits: sample order (ex_*), then sorted by row (hitsort.cu)
+    uint32_t* ex_j = nullptr;         // nnz: sample of hit h
+    double* ex_val = nullptr;         // nnz: value of hit h
+    uint32_t* hit_key[2] = {nullptr, nullptr};  // nnz each: output rows (sort ping-pong)
+    uint32_t* hit_pay[2] = {nullptr, nullptr};  // nnz each: hit indices (sort ping-pong)
+    const uint32_t* key_sorted = nullptr;       // the sorted rows of the current step
+    const uint32_t* pay_sorted = nullptr;       // their hit indices
+    uint32_t* hs_cnt = nullptr;       // 256 x tile stride: digit counts per tile
+    uint32_t* hs_tot = nullptr;       // 256: digit totals
+    uint32_t* head_cnt = nullptr;     // chunks: touched-row starts per chunk of sorted hits
+    int64_t* head_base = nullptr;     // chunks: their exclusive scan
+    double* Mc = nullptr;             // Imax x R: MTTKRP rows, indexed by row
+    double* carry_first = nullptr;  // chunks x kCarryStride
+    double* carry_last = nullptr;   // chunks x kCarryStride
+    uint32_t* carry_row = nullptr;  // chunks: row continuing past the chunk, or 0xffffffff
     float* Df = nullptr;          // Jmax x R design rows (mixed forms)
 
     uint64_t seed = 0x5eed;
@@ -141,14 +144,17 @@ int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist
               double* out_full, cudaStream_t st);
 int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st);
 int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st);
-int touched_rows(Session& s, int64_t I, cudaStream_t st);
 int gram_reduce_to(Session& s, int64_t nblk, double* out, cudaStream_t st);
 int sigma_and_gram(Session& s, cudaStream_t st);
 int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st);
 
 // ---- load-balanced MTTKRP and post-processing, R <= 32 (post_kernels.cu)
 constexpr int kSegChunkHits = 128;
-int mttkrp_rows_balanced(Session& s, int n, cudaStream_t st);
+constexpr int kCarryStride = 32;  // carry rows padded to 32 columns (R <= 32)
+
+// ---- hits grouped by output row (hitsort.cu)
+size_t hitsort_tile_stride(int64_t nnz);
+int hits_by_row(Session& s, int n, cudaStream_t st);
 int mttkrp_solve_balanced(Session& s, int n, cudaStream_t st);
 int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st);
 int mttkrp_scatter_out(Session& s, double* out, cudaStream_t st);

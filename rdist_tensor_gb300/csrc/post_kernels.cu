@@ -1,8 +1,6 @@
-// Sampled MTTKRP and post-processing, load-balanced (R <= 32 path):
+// Sampled MTTKRP and post-processing, load-balanced (R <= 32 path), on the
+// hits sorted by output row (hitsort.cu):
 //
-//   expand   hits in sample order: owner sample by one restricted binary search
-//            per warp chunk; counts hits per output row
-//   scatter  hits grouped by output row (counting sort)
 //   segred   M rows from fixed-size chunks of row-grouped hits: rows inside a
 //            chunk are written directly, rows crossing a chunk border leave a
 //            per-chunk carry (csr_based_spmm's row-chunked AXPYs,
@@ -18,131 +16,145 @@
 
 namespace exafac {
 
-constexpr int kExpandChunk = 256;  // hits per warp chunk in the expansion
-constexpr int kSegChunk = 128;     // hits per warp chunk in the segmented reduction
+constexpr int kSegChunk = kSegChunkHits;  // hits per warp chunk in the segmented reduction
 
 static int grid_capped(int64_t work, int threads, int64_t cap = 152 * 16) {
     int64_t b = ceil_div(work, threads);
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
 }
 
-__device__ __forceinline__ int64_t owner_in(const int64_t* __restrict__ f_off, int64_t lo, int64_t hi, int64_t h) {
-    // last j in [lo, hi) with f_off[j] <= h (f_off[lo] <= h guaranteed)
-    while (hi - lo > 1) {
-        int64_t mid = (lo + hi) >> 1;
-        if (f_off[mid] <= h) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t cap, const int64_t* __restrict__ f_off,
-                                  const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
-                                  const double* __restrict__ vals_n, uint32_t* __restrict__ ex_row,
-                                  uint32_t* __restrict__ ex_j, double* __restrict__ ex_val,
-                                  uint32_t* __restrict__ rowcnt, DeviceStatus* status) {
-    const int64_t ju = counters[0];
-    int64_t H = counters[1];
-    if (H > cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) report(status, EXAFAC_ERR_DEVICE, 4, H, cap);
-        H = cap;
-    }
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t c = warp; c * kExpandChunk < H; c += nwarps) {
-        const int64_t h0 = c * kExpandChunk;
-        const int64_t h1 = min(H, h0 + kExpandChunk);
-        // Owners of the chunk's first and last hits bound every owner in it.
-        int64_t jlo = 0, jhi = 0;
-        if (lane == 0) jlo = owner_in(f_off, 0, ju, h0);
-        if (lane == 1) jhi = owner_in(f_off, 0, ju, h1 - 1) + 1;
-        jlo = __shfl_sync(0xffffffffu, jlo, 0);
-        jhi = __shfl_sync(0xffffffffu, jhi, 1);
-        for (int64_t h = h0 + lane; h < h1; h += 32) {
-            const int64_t j = owner_in(f_off, jlo, jhi, h);
-            const int64_t p = (int64_t)f_start[j] + (h - f_off[j]);
-            const uint32_t row = rows_n[p];
-            ex_row[h] = row;
-            ex_j[h] = (uint32_t)j;
-            ex_val[h] = vals_n[p];
-            atomicAdd(&rowcnt[row], 1u);
-        }
-    }
-}
-
-__global__ void hit_group_kernel(const int64_t* __restrict__ counters, int64_t cap, const uint32_t* __restrict__ ex_row,
-                                 const uint32_t* __restrict__ ex_j, const double* __restrict__ ex_val,
-                                 const int64_t* __restrict__ rowoff, uint32_t* __restrict__ rowfill,
-                                 uint32_t* __restrict__ hit_row, uint32_t* __restrict__ hit_j,
-                                 double* __restrict__ hit_val) {
-    const int64_t H = min(counters[1], cap);
-    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < H; h += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t row = ex_row[h];
-        const int64_t dst = rowoff[row] + atomicAdd(&rowfill[row], 1u);
-        hit_row[dst] = row;
-        hit_j[dst] = ex_j[h];
-        hit_val[dst] = ex_val[h];
-    }
-}
-
-// Segmented reduction over row-grouped hits, lane = column (R <= 32).
-// Mc[i] (i = compact index of the touched row = pos[row]) receives rows that
-// lie inside one chunk; crossing rows leave carries:
+// Segmented reduction over the row-sorted hits, lane = column (R <= 32).
+// A warp takes a chunk of kSegChunk hits and stages them 32 at a time: each
+// lane loads one hit (row, sample, value), a ballot marks where a new row
+// starts, and every lane issues the group's 32 design-row loads before the
+// first FMA, so the gathers overlap instead of forming one dependent chain
+// per hit.  Mc[row] receives rows that lie inside one chunk; crossing rows
+// leave carries (kCarryStride columns):
 //   carry_first[c]: the chunk's first row when it started in an earlier chunk
-//   carry_last[c]:  the chunk's last row when it continues in a later chunk
+//   carry_last[c]:  the chunk's last row when it continues in a later chunk,
+//                   whose row goes to carry_row[c] (kNoRow when there is none)
+constexpr uint32_t kNoRow = 0xffffffffu;  // rows are < 2^32 - 1
+
 template <typename TD, typename TA>
-__global__ void segreduce_kernel(int R, const int64_t* __restrict__ counters, int64_t cap,
-                                 const uint32_t* __restrict__ hit_row, const uint32_t* __restrict__ hit_j,
-                                 const double* __restrict__ hit_val, const int64_t* __restrict__ rowoff,
-                                 const uint32_t* __restrict__ rowcnt, const int64_t* __restrict__ pos,
-                                 const TD* __restrict__ D, TA* __restrict__ Mc, TA* __restrict__ carry_first,
-                                 TA* __restrict__ carry_last) {
+__global__ void __launch_bounds__(256) segreduce_kernel(int R, const int64_t* __restrict__ counters, int64_t cap,
+                                                        const uint32_t* __restrict__ keys,
+                                                        const uint32_t* __restrict__ pay,
+                                                        const uint32_t* __restrict__ ex_j,
+                                                        const double* __restrict__ ex_val, const TD* __restrict__ D,
+                                                        TA* __restrict__ Mc, TA* __restrict__ carry_first,
+                                                        TA* __restrict__ carry_last, uint32_t* __restrict__ carry_row) {
     const int64_t H = min(counters[1], cap);
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned full = 0xffffffffu;
     for (int64_t c = warp; c * kSegChunk < H; c += nwarps) {
         const int64_t cs = c * kSegChunk;
         const int64_t ce = min(H, cs + kSegChunk);
-        int64_t h = cs;
-        while (h < ce) {
-            const uint32_t row = hit_row[h];
-            const int64_t rs = rowoff[row], re = rs + rowcnt[row];
-            const int64_t e = min(re, ce);
-            TA acc = 0;
-            if (lane < R) {
-                for (int64_t p = h; p < e; p++) acc += (TA)D[(int64_t)hit_j[p] * R + lane] * (TA)hit_val[p];
+        uint32_t prev_row = kNoRow, next_row = kNoRow, first_row = kNoRow;
+        if (lane == 0 && cs > 0) prev_row = keys[cs - 1];
+        if (lane == 1 && ce < H) next_row = keys[ce];
+        if (lane == 2) first_row = keys[cs];
+        prev_row = __shfl_sync(full, prev_row, 0);
+        next_row = __shfl_sync(full, next_row, 1);
+        uint32_t cur = __shfl_sync(full, first_row, 2);  // row of the open segment
+        bool first_seg = true;
+        TA acc = 0;
+        for (int64_t g = cs; g < ce; g += 32) {
+            const int n = (int)min((int64_t)32, ce - g);
+            uint32_t hj = 0, hr = kNoRow;
+            TA hv = 0;
+            if (lane < n) {
+                hr = keys[g + lane];
+                const uint32_t h = pay[g + lane];
+                hj = ex_j[h];
+                hv = (TA)ex_val[h];
             }
-            if (lane < R) {
-                if (rs >= cs && re <= ce) Mc[pos[row] * R + lane] = acc;
-                else if (rs < cs) carry_first[c * R + lane] = acc;
-                else carry_last[c * R + lane] = acc;
+            uint32_t up = __shfl_up_sync(full, hr, 1);
+            if (lane == 0) up = cur;
+            const unsigned brk = __ballot_sync(full, lane < n && hr != up);
+            TA d[32];
+#pragma unroll
+            for (int t = 0; t < 32; t++) {
+                const uint32_t jt = __shfl_sync(full, hj, t);
+                d[t] = (t < n && lane < R) ? (TA)D[(int64_t)jt * R + lane] : (TA)0;
             }
-            h = e;
+#pragma unroll
+            for (int t = 0; t < 32; t++) {
+                if (t < n) {
+                    if ((brk >> t) & 1u) {  // the open segment ends inside the chunk
+                        if (lane < R) {
+                            if (first_seg && cur == prev_row) carry_first[c * kCarryStride + lane] = acc;
+                            else Mc[(int64_t)cur * R + lane] = acc;
+                        }
+                        first_seg = false;
+                        cur = __shfl_sync(full, hr, t);
+                        acc = 0;
+                    }
+                    acc = fma(d[t], __shfl_sync(full, hv, t), acc);
+                }
+            }
         }
+        const bool started_before = first_seg && cur == prev_row;
+        const bool continues = cur == next_row;
+        if (lane < R) {
+            if (started_before) carry_first[c * kCarryStride + lane] = acc;
+            else if (continues) carry_last[c * kCarryStride + lane] = acc;
+            else Mc[(int64_t)cur * R + lane] = acc;
+        }
+        if (lane == 0) carry_row[c] = (!started_before && continues) ? cur : kNoRow;
     }
 }
 
-// Crossing rows: sum their carries in chunk order.  Warp per touched row;
-// rows inside one chunk are skipped.
+// Crossing rows, one warp per chunk c0 whose last row continues: the row's
+// carries carry_last[c0] + sum over c in (c0, c1] of carry_first[c], c1 the
+// last chunk that starts inside the row (the chunks that do form a prefix of
+// c0+1, c0+2, ..., found 32 at a time by ballot).  Lane l sums chunks
+// c0+1+l, c0+1+l+32, ... over all 32 padded columns, then a butterfly
+// reduce-scatter leaves column l's total in lane l (a fixed order, so results
+// are reproducible run to run).
 template <typename TA>
-__global__ void segfix_kernel(int R, const int64_t* __restrict__ counters, const uint32_t* __restrict__ touched,
-                              const int64_t* __restrict__ rowoff, const uint32_t* __restrict__ rowcnt,
-                              const TA* __restrict__ carry_first, const TA* __restrict__ carry_last,
-                              TA* __restrict__ Mc) {
-    const int64_t nt = counters[2];
+__global__ void __launch_bounds__(256) segfix_kernel(int R, const int64_t* __restrict__ counters, int64_t cap,
+                                                     const uint32_t* __restrict__ carry_row,
+                                                     const uint32_t* __restrict__ keys,
+                                                     const TA* __restrict__ carry_first,
+                                                     const TA* __restrict__ carry_last, TA* __restrict__ Mc) {
+    const int64_t H = min(counters[1], cap);
+    const int64_t nchunks = (H + kSegChunk - 1) / kSegChunk;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = warp; i < nt; i += nwarps) {
-        const uint32_t row = touched[i];
-        const int64_t rs = rowoff[row], re = rs + rowcnt[row];
-        const int64_t c0 = rs / kSegChunk, c1 = (re - 1) / kSegChunk;
-        if (c0 == c1 || lane >= R) continue;
-        TA acc = carry_last[c0 * R + lane];
-        for (int64_t c = c0 + 1; c <= c1; c++) acc += carry_first[c * R + lane];
-        Mc[i * R + lane] = acc;
+    const unsigned full = 0xffffffffu;
+    for (int64_t c0 = warp; c0 < nchunks; c0 += nwarps) {
+        const uint32_t row = carry_row[c0];
+        if (row == kNoRow) continue;
+        int64_t c1 = c0;
+        for (int64_t b = c0 + 1;; b += 32) {
+            const int64_t m = b + lane;
+            const bool on = m < nchunks && keys[m * kSegChunk] == row;
+            const unsigned bal = __ballot_sync(full, on);
+            c1 = b + __popc(bal) - 1;
+            if (bal != full) break;
+        }
+        TA acc[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) acc[k] = 0;
+        for (int64_t m = c0 + 1 + lane; m <= c1; m += 32) {
+            const TA* src = carry_first + m * kCarryStride;
+#pragma unroll
+            for (int k = 0; k < 32; k++) acc[k] += src[k];
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const bool upper = (lane & off) != 0;
+#pragma unroll
+            for (int k = 0; k < off; k++) {
+                const TA send = upper ? acc[k] : acc[k + off];
+                const TA keep = upper ? acc[k + off] : acc[k];
+                acc[k] = keep + __shfl_xor_sync(full, send, off);
+            }
+        }
+        if (lane < R) Mc[(int64_t)row * R + lane] = carry_last[c0 * kCarryStride + lane] + acc[0];
     }
 }
 
@@ -193,9 +205,10 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_kernel(int R, con
         const int64_t i = base + lane;
         TA m[32];
         if (i < nt) {
+            const int64_t mrow = touched[i];
 #pragma unroll
             for (int k = 0; k < 32; k++)
-                if (k < R) m[k] = Mc[i * R + k];
+                if (k < R) m[k] = Mc[mrow * R + k];
         }
         for (int cc = 0; cc < R; cc++) {
             TA acc = 0;
@@ -289,25 +302,6 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-int mttkrp_rows_balanced(Session& s, int n, cudaStream_t st) {
-    const Lookup& L = s.look[n];
-    const int64_t I = s.dims[n];
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowcnt, 0, sizeof(uint32_t) * I, st));
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowfill, 0, sizeof(uint32_t) * I, st));
-    const int hb = 152 * 8;
-    hit_expand_kernel<<<hb, 256, 0, st>>>(s.counters, s.nnz, s.f_off, s.f_start, L.rows, L.vals, s.ex_row, s.ex_j,
-                                          s.ex_val, s.rowcnt, s.status);
-    count_launch();
-    EXAFAC_CHECK_LAUNCH();
-    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.rowcnt, s.rowoff, I, s.counters + 3, s.scan_sc, st));
-    EXAFAC_TRY(touched_rows(s, I, st));
-    hit_group_kernel<<<hb, 256, 0, st>>>(s.counters, s.nnz, s.ex_row, s.ex_j, s.ex_val, s.rowoff, s.rowfill,
-                                         s.hit_row, s.hit_j, s.hit_val);
-    count_launch();
-    EXAFAC_CHECK_LAUNCH();
-    return EXAFAC_OK;
-}
-
 constexpr int kSolveBlocks = 152 * 2;
 
 template <typename TA>
@@ -318,15 +312,265 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
     TA* cf = reinterpret_cast<TA*>(s.carry_first);
     TA* cl = reinterpret_cast<TA*>(s.carry_last);
     if (std::is_same<TA, double>::value)
-        segreduce_kernel<double, double><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.hit_row, s.hit_j, s.hit_val,
-                                                             s.rowoff, s.rowcnt, s.pos, (const double*)s.D,
-                                                             (double*)Mc, (double*)cf, (double*)cl);
+        segreduce_kernel<double, double><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.ex_j,
+                                                             s.ex_val, (const double*)s.D, (double*)Mc, (double*)cf,
+                                                             (double*)cl, s.carry_row);
     else
-        segreduce_kernel<float, float><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.hit_row, s.hit_j, s.hit_val,
-                                                           s.rowoff, s.rowcnt, s.pos, (const float*)s.Df, (float*)Mc,
-                                                           (float*)cf, (float*)cl);
+        segreduce_kernel<float, float><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.ex_j,
+                                                           s.ex_val, (const float*)s.Df, (float*)Mc, (float*)cf,
+                                                           (float*)cl, s.carry_row);
     count_launch();
-    segfix_kernel<TA><<<hb, 256, 0, st>>>(R, s.counters, s.touched, s.rowoff, s.rowcnt, cf, cl, Mc);
+    segfix_kernel<TA><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.carry_row, s.key_sorted, cf, cl, Mc);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 forms of solve + Gram and normalize + leverage (mixed precisions).
+// A warp owns 32 touched rows at a time, staged in shared memory with rows
+// padded to KC floats (KC a multiple of 4, >= R):
+//   * rows move between HBM and the tile one row per instruction (lane =
+//     column), so each global access is one contiguous row;
+//   * row products run thread per row, the R x R operand read as float4
+//     broadcasts from shared memory;
+//   * the Gram of the solved rows is accumulated in 4 x 4 register blocks of
+//     the lower triangle (NB blocks per lane), in FP32 within a 32-row tile
+//     and in FP64 across tiles, then summed over the block's warps in warp
+//     order (reproducible).
+// ---------------------------------------------------------------------------
+constexpr int kTileStride = 36;  // floats per staged row (16-byte aligned rows)
+
+template <int KC>
+struct TileShape {
+    static constexpr int kBlk = KC / 4;                        // 4-column blocks per side
+    static constexpr int kTri = kBlk * (kBlk + 1) / 2;         // lower-triangle blocks
+    static constexpr int kNB = (kTri + 31) / 32;               // blocks per lane
+};
+
+template <int KC>
+__global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R, const int64_t* __restrict__ counters,
+                                                                         const uint32_t* __restrict__ touched,
+                                                                         const float* __restrict__ Mc,
+                                                                         const double* __restrict__ Phi,
+                                                                         double* __restrict__ U,
+                                                                         double* __restrict__ part) {
+    using S = TileShape<KC>;
+    __shared__ __align__(16) float phi[KC][KC];
+    __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
+    __shared__ double red[32 * 33 / 2];
+    const int P = R * (R + 1) / 2;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
+        const int a = e / KC, b = e % KC;
+        phi[a][b] = (a < R && b < R) ? (float)Phi[a * R + b] : 0.0f;
+    }
+    for (int e = threadIdx.x; e < P; e += blockDim.x) red[e] = 0.0;
+    // this lane's lower-triangle 4x4 blocks
+    int bi[S::kNB], bj[S::kNB];
+#pragma unroll
+    for (int q = 0; q < S::kNB; q++) {
+        int blk = lane + 32 * q, i = 0;
+        while (blk > i) {
+            blk -= i + 1;
+            i++;
+        }
+        bi[q] = (lane + 32 * q < S::kTri) ? i : -1;
+        bj[q] = blk;
+    }
+    double gd[S::kNB][16];
+#pragma unroll
+    for (int q = 0; q < S::kNB; q++)
+#pragma unroll
+        for (int x = 0; x < 16; x++) gd[q][x] = 0.0;
+    __syncthreads();
+    float (*t)[kTileStride] = tile[w];
+    const int64_t nt = counters[2];
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < nt; base += nwarps * 32) {
+        const int nrow = (int)min((int64_t)32, nt - base);
+        const uint32_t myrow = lane < nrow ? touched[base + lane] : 0u;
+        float v[32];  // stage M rows (all 32 loads in flight), zero padding
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
+            v[r] = (r < nrow && lane < R) ? Mc[row * R + lane] : 0.0f;
+        }
+#pragma unroll
+        for (int r = 0; r < 32; r++)
+            if (lane < KC) t[r][lane] = v[r];
+        __syncwarp();
+        float m[KC], u[KC];
+#pragma unroll
+        for (int c = 0; c < KC; c += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(&t[lane][c]);
+            m[c] = v.x;
+            m[c + 1] = v.y;
+            m[c + 2] = v.z;
+            m[c + 3] = v.w;
+            u[c] = u[c + 1] = u[c + 2] = u[c + 3] = 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < KC; k++) {
+            if (k < R) {
+#pragma unroll
+                for (int c = 0; c < KC; c += 4) {
+                    const float4 p = *reinterpret_cast<const float4*>(&phi[k][c]);
+                    u[c] = fmaf(m[k], p.x, u[c]);
+                    u[c + 1] = fmaf(m[k], p.y, u[c + 1]);
+                    u[c + 2] = fmaf(m[k], p.z, u[c + 2]);
+                    u[c + 3] = fmaf(m[k], p.w, u[c + 3]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < KC; c += 4)
+            *reinterpret_cast<float4*>(&t[lane][c]) = make_float4(u[c], u[c + 1], u[c + 2], u[c + 3]);
+        __syncwarp();
+        for (int r = 0; r < nrow; r++) {  // store U rows (FP64 factor)
+            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
+            if (lane < R) U[row * R + lane] = (double)t[r][lane];
+        }
+#pragma unroll
+        for (int q = 0; q < S::kNB; q++) {
+            if (bi[q] >= 0) {
+                float g[16];
+#pragma unroll
+                for (int x = 0; x < 16; x++) g[x] = 0.0f;
+                for (int r = 0; r < 32; r++) {
+                    const float4 a = *reinterpret_cast<const float4*>(&t[r][4 * bi[q]]);
+                    const float4 b = *reinterpret_cast<const float4*>(&t[r][4 * bj[q]]);
+                    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                    for (int x = 0; x < 4; x++)
+#pragma unroll
+                        for (int y = 0; y < 4; y++) g[x * 4 + y] = fmaf(av[x], bv[y], g[x * 4 + y]);
+                }
+#pragma unroll
+                for (int x = 0; x < 16; x++) gd[q][x] += (double)g[x];
+            }
+        }
+        __syncwarp();
+    }
+    for (int ww = 0; ww < kSolveWarps; ww++) {  // block sum in warp order
+        if (w == ww) {
+#pragma unroll
+            for (int q = 0; q < S::kNB; q++) {
+                if (bi[q] < 0) continue;
+#pragma unroll
+                for (int x = 0; x < 4; x++)
+#pragma unroll
+                    for (int y = 0; y < 4; y++) {
+                        const int a = 4 * bi[q] + x, b = 4 * bj[q] + y;  // b's block <= a's block
+                        if (a < R && b < R && b <= a) red[packed_index(R, b, a)] += gd[q][x * 4 + y];
+                    }
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
+}
+
+// u_r = U_r / sigma and, when P != null, l_r = u_r^T P u_r, FP32 row
+// products; rows staged as in solve_gram_f32_kernel.
+template <int KC>
+__global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, const int64_t* __restrict__ counters,
+                                                                      const uint32_t* __restrict__ touched,
+                                                                      const double* __restrict__ sigma,
+                                                                      const double* __restrict__ Pm,
+                                                                      const int* __restrict__ degenerate,
+                                                                      double* __restrict__ U,
+                                                                      double* __restrict__ scores) {
+    __shared__ __align__(16) float psm[KC][KC];
+    __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
+    __shared__ double sg[32];
+    if (*degenerate) return;  // handled over all rows by scale_rows
+    for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
+        const int a = e / KC, b = e % KC;
+        psm[a][b] = (Pm && a < R && b < R) ? (float)Pm[a * R + b] : 0.0f;
+    }
+    // Multiplying by 1/sigma differs from the reference's division by at
+    // most one rounding.
+    for (int c = threadIdx.x; c < 32; c += blockDim.x) sg[c] = c < R ? 1.0 / sigma[c] : 0.0;
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float (*t)[kTileStride] = tile[w];
+    const double sgl = sg[lane];
+    const int64_t nt = counters[2];
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < nt; base += nwarps * 32) {
+        const int nrow = (int)min((int64_t)32, nt - base);
+        const uint32_t myrow = lane < nrow ? touched[base + lane] : 0u;
+#pragma unroll
+        for (int h = 0; h < 32; h += 16) {  // 16 row loads in flight at a time
+            double x[16];
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                const int64_t row = __shfl_sync(0xffffffffu, myrow, h + r);
+                x[r] = (h + r < nrow && lane < R) ? U[row * R + lane] : 0.0;
+            }
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                const int64_t row = __shfl_sync(0xffffffffu, myrow, h + r);
+                const double y = x[r] * sgl;
+                if (h + r < nrow && lane < R) U[row * R + lane] = y;
+                if (lane < KC) t[h + r][lane] = (float)y;
+            }
+        }
+        __syncwarp();
+        if (Pm && lane < nrow) {
+            float u[KC];
+#pragma unroll
+            for (int c = 0; c < KC; c += 4) {
+                const float4 v = *reinterpret_cast<const float4*>(&t[lane][c]);
+                u[c] = v.x;
+                u[c + 1] = v.y;
+                u[c + 2] = v.z;
+                u[c + 3] = v.w;
+            }
+            float acc = 0.0f;
+#pragma unroll
+            for (int a = 0; a < KC; a++) {
+                if (a < R) {
+                    float y = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < KC; c += 4) {
+                        const float4 p = *reinterpret_cast<const float4*>(&psm[a][c]);
+                        y = fmaf(p.x, u[c], y);
+                        y = fmaf(p.y, u[c + 1], y);
+                        y = fmaf(p.z, u[c + 2], y);
+                        y = fmaf(p.w, u[c + 3], y);
+                    }
+                    acc = fmaf(u[a], y, acc);
+                }
+            }
+            scores[myrow] = (double)acc;
+        }
+        __syncwarp();
+    }
+}
+
+template <int KC>
+static void launch_solve_f32(Session& s, int n, cudaStream_t st) {
+    solve_gram_f32_kernel<KC><<<kSolveBlocks, kSolveWarps * 32, 0, st>>>(
+        s.R, s.counters, s.touched, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.F.U[n], s.part);
+}
+
+template <int KC>
+static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
+    normlev_f32_kernel<KC><<<kSolveBlocks, kSolveWarps * 32, 0, st>>>(
+        s.R, s.counters, s.touched, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
+        s.F.U[n], arls ? s.scores[n] : nullptr);
+}
+
+static int solve_f32(Session& s, int n, cudaStream_t st) {
+    EXAFAC_TRY(segmented_mttkrp<float>(s, st));
+    EXAFAC_TRY(zero_factor_rows(s, n, st));
+    if (s.R <= 16) launch_solve_f32<16>(s, n, st);
+    else if (s.R <= 28) launch_solve_f32<28>(s, n, st);
+    else launch_solve_f32<32>(s, n, st);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
@@ -374,19 +618,28 @@ static int normalize_typed(Session& s, int n, bool arls, cudaStream_t st) {
 
 int mttkrp_solve_balanced(Session& s, int n, cudaStream_t st) {
     if (s.cfg.precision == EXAFAC_PREC_FP64) return solve_typed<double>(s, n, st);
-    return solve_typed<float>(s, n, st);
+    return solve_f32(s, n, st);
 }
 
 int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st) {
     if (s.cfg.precision == EXAFAC_PREC_FP64) return normalize_typed<double>(s, n, arls, st);
-    return normalize_typed<float>(s, n, arls, st);
+    const int R = s.R;
+    EXAFAC_TRY(gram_reduce_to(s, kSolveBlocks, s.ugram, st));
+    EXAFAC_TRY(sigma_and_gram(s, st));
+    if (arls) EXAFAC_TRY(launch_pinv(R, s.ngram, s.upinv, 1e-11, s.vt, st));
+    if (R <= 16) launch_normlev_f32<16>(s, n, arls, st);
+    else if (R <= 28) launch_normlev_f32<28>(s, n, arls, st);
+    else launch_normlev_f32<32>(s, n, arls, st);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return scale_rows_if_degenerate(s, n, st);
 }
 
 __global__ void scatter_rows_kernel(int R, const int64_t* __restrict__ counters, const uint32_t* __restrict__ touched,
                                     const double* __restrict__ Mc, double* __restrict__ out) {
     const int64_t nt = counters[2];
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nt * R; e += (int64_t)gridDim.x * blockDim.x)
-        out[(int64_t)touched[e / R] * R + e % R] = Mc[e];
+        out[(int64_t)touched[e / R] * R + e % R] = Mc[(int64_t)touched[e / R] * R + e % R];
 }
 
 // MTTKRP rows (FP64) written to a dense dims[n] x R output (zeroed by the caller).

@@ -68,8 +68,8 @@ static void carve(Session& s) {
     s.d_minj = a.take<int32_t>(s.dtab);
     s.d_count = a.take<int32_t>(s.dtab);
     s.slot_of = a.take<int32_t>(J);
-    s.flags = a.take<uint32_t>(std::max(J, I));
-    s.pos = a.take<int64_t>(std::max(J, I));
+    s.flags = a.take<uint32_t>(J);
+    s.pos = a.take<int64_t>(J);
     s.sd = a.take<uint32_t>(J * N);
     s.wd = a.take<double>(J);
     s.counters = a.take<int64_t>(16);
@@ -80,11 +80,7 @@ static void carve(Session& s) {
     s.f_start = a.take<uint32_t>(J);
     s.f_len = a.take<uint32_t>(J);
     s.f_off = a.take<int64_t>(J);
-    s.rowcnt = a.take<uint32_t>(I);
-    s.rowfill = a.take<uint32_t>(I);
-    s.rowoff = a.take<int64_t>(I);
-    s.hit_j = a.take<uint32_t>(nnz);
-    s.hit_val = a.take<double>(nnz);
+    s.seg_start = a.take<int64_t>(I + 1);
     s.touched = a.take<uint32_t>(I);
     s.ugram = a.take<double>(R2);
     s.ngram = a.take<double>(R2);
@@ -95,14 +91,21 @@ static void carve(Session& s) {
     s.dims_dev = a.take<int64_t>(kMaxModes);
     s.Mexact = a.take<double>(I * R);
     s.scal = a.take<double>(8);
-    s.ex_row = a.take<uint32_t>(nnz);
     s.ex_j = a.take<uint32_t>(nnz);
     s.ex_val = a.take<double>(nnz);
-    s.hit_row = a.take<uint32_t>(nnz);
+    for (int b = 0; b < 2; b++) {
+        s.hit_key[b] = a.take<uint32_t>(nnz);
+        s.hit_pay[b] = a.take<uint32_t>(nnz);
+    }
+    s.hs_cnt = a.take<uint32_t>(256 * (int64_t)hitsort_tile_stride(nnz));
+    s.hs_tot = a.take<uint32_t>(256);
     s.Mc = a.take<double>(I * R);
     const int64_t chunks = ceil_div(nnz, kSegChunkHits) + 1;
-    s.carry_first = a.take<double>(chunks * R);
-    s.carry_last = a.take<double>(chunks * R);
+    s.head_cnt = a.take<uint32_t>(chunks);
+    s.head_base = a.take<int64_t>(chunks);
+    s.carry_first = a.take<double>(chunks * kCarryStride);
+    s.carry_last = a.take<double>(chunks * kCarryStride);
+    s.carry_row = a.take<uint32_t>(chunks);
     s.Df = a.take<float>(J * R);
 }
 

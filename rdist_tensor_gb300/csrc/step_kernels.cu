@@ -326,17 +326,6 @@ __global__ void lookup_kernel(KeySpec spec, int64_t J, const int64_t* __restrict
     f_len[j] = len;
 }
 
-__global__ void row_flag_kernel(int64_t I, const uint32_t* __restrict__ rowcnt, uint32_t* __restrict__ flag) {
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < I; r += (int64_t)gridDim.x * blockDim.x)
-        flag[r] = rowcnt[r] > 0 ? 1u : 0u;
-}
-
-__global__ void row_compact_kernel(int64_t I, const uint32_t* __restrict__ flag, const int64_t* __restrict__ pos,
-                                   uint32_t* __restrict__ list) {
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < I; r += (int64_t)gridDim.x * blockDim.x)
-        if (flag[r]) list[pos[r]] = (uint32_t)r;
-}
-
 // counters[5] += counters[1]: running total of the hits (nonzeros_iterated).
 __global__ void accumulate_kernel(int64_t* total, const int64_t* add) { *total += *add; }
 
@@ -357,20 +346,9 @@ int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st) {
     return EXAFAC_OK;
 }
 
-// Rows with at least one hit, in increasing order (touched list), and each
-// row's index in that list (pos, the exclusive scan of the flags).
-int touched_rows(Session& s, int64_t I, cudaStream_t st) {
-    row_flag_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.rowcnt, s.flags); count_launch();
-    EXAFAC_CHECK_LAUNCH();
-    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, I, s.counters + 2, s.scan_sc, st));
-    row_compact_kernel<<<grid_cap(I, 256), 256, 0, st>>>(I, s.flags, s.pos, s.touched); count_launch();
-    EXAFAC_CHECK_LAUNCH();
-    return EXAFAC_OK;
-}
-
 int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
     EXAFAC_TRY(lookup_fibers(s, n, J, st));
-    return mttkrp_rows_balanced(s, n, st);
+    return hits_by_row(s, n, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -379,8 +357,8 @@ int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
 // row, M_r = sum over the row's hits of val * D'[j], U_r = M_r * Phi.
 // ---------------------------------------------------------------------------
 __global__ void spmm_solve_kernel(int R, const int64_t* __restrict__ counters, const uint32_t* __restrict__ touched,
-                                  const int64_t* __restrict__ rowoff, const uint32_t* __restrict__ rowcnt,
-                                  const uint32_t* __restrict__ hit_j, const double* __restrict__ hit_val,
+                                  const int64_t* __restrict__ seg_start, const uint32_t* __restrict__ pay,
+                                  const uint32_t* __restrict__ ex_j, const double* __restrict__ ex_val,
                                   const double* __restrict__ D, const double* __restrict__ Phi, double* __restrict__ U) {
     extern __shared__ double sm[];
     const int warps = blockDim.x >> 5;
@@ -393,10 +371,13 @@ __global__ void spmm_solve_kernel(int R, const int64_t* __restrict__ counters, c
     const int64_t nt = counters[2];
     for (int64_t i = (int64_t)blockIdx.x * warps + w; i < nt; i += (int64_t)gridDim.x * warps) {
         const int64_t r = touched[i];
-        const int64_t beg = rowoff[r], cnt = rowcnt[r];
+        const int64_t beg = seg_start[i], end = seg_start[i + 1];
         for (int c = lane; c < R; c += 32) {
             double acc = 0.0;
-            for (int64_t p = beg; p < beg + cnt; p++) acc += D[(int64_t)hit_j[p] * R + c] * hit_val[p];
+            for (int64_t p = beg; p < end; p++) {
+                const uint32_t h = pay[p];
+                acc += D[(int64_t)ex_j[h] * R + c] * ex_val[h];
+            }
             msm[c] = acc;
         }
         __syncwarp();
@@ -422,7 +403,7 @@ int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStrea
         EXAFAC_CUDA_TRY(
             cudaFuncSetAttribute(spmm_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     spmm_solve_kernel<<<grid_cap(s.dims[n], warps * 32), warps * 32, smem, st>>>(
-        R, s.counters, s.touched, s.rowoff, s.rowcnt, s.hit_j, s.hit_val, s.D, Phi, out); count_launch();
+        R, s.counters, s.touched, s.seg_start, s.pay_sorted, s.ex_j, s.ex_val, s.D, Phi, out); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -499,13 +480,22 @@ int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st) {
     return EXAFAC_OK;
 }
 
+// Warp per 32 listed rows: indices loaded together, then one row per store
+// instruction (lane = column).
 __global__ void zero_rows_kernel(int R, const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
                                  double* __restrict__ U, double* __restrict__ scores) {
     const int64_t cnt = *cnt_dev;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt * R; e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t r = list[e / R];
-        U[r * R + e % R] = 0.0;
-        if (scores && e % R == 0) scores[r] = 0.0;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < cnt; base += nwarps * 32) {
+        const int n = (int)min((int64_t)32, cnt - base);
+        const uint32_t myrow = lane < n ? list[base + lane] : 0u;
+        if (scores && lane < n) scores[myrow] = 0.0;
+        for (int r = 0; r < n; r++) {
+            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
+            for (int c = lane; c < R; c += 32) U[row * R + c] = 0.0;
+        }
     }
 }
 
@@ -518,7 +508,7 @@ int zero_factor_rows(Session& s, int n, cudaStream_t st) {
         EXAFAC_CUDA_TRY(cudaMemsetAsync(s.F.U[n], 0, sizeof(double) * s.dims[n] * R, st));
         if (sc) EXAFAC_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * s.dims[n], st));
     } else {
-        zero_rows_kernel<<<grid_cap(s.dims[n] * R, 256), 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.F.U[n], sc); count_launch();
+        zero_rows_kernel<<<152 * 8, 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.F.U[n], sc); count_launch();
         EXAFAC_CHECK_LAUNCH();
     }
     return EXAFAC_OK;
