@@ -18,6 +18,7 @@ namespace exafac {
 
 constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr int64_t kExactCdfMax = 16384;  // CDFs up to this length are summed strictly in order
+constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a power of two)
 
 struct Slot1 {
     unsigned long long key;
@@ -38,6 +39,10 @@ struct Lookup {
     KeySpec spec;
 };
 
+struct FactorPtrs {  // factor matrices passed by value to kernels
+    const double* U[kMaxModes];
+};
+
 struct Session {
     exafac_als_config cfg;
     int N = 0, R = 0, P = 0;
@@ -55,6 +60,7 @@ struct Session {
     // CP-ARLS-LEV state
     double* scores[kMaxModes] = {nullptr};
     double* cdf[kMaxModes] = {nullptr};
+    uint32_t* guide[kMaxModes] = {nullptr};  // kGuideBuckets + 1: guide[b] = lower_bound(cdf, b / kGuideBuckets)
     double* cdf_total = nullptr;  // [N] sum of the scores (log-weight numerator)
     // STS-CP state
     TreeShape rtree[kMaxModes];
@@ -114,7 +120,9 @@ struct Session {
     uint32_t* hit_key[2] = {nullptr, nullptr};  // nnz each: output rows (sort ping-pong)
     uint32_t* hit_pay[2] = {nullptr, nullptr};  // nnz each: hit indices (sort ping-pong)
     const uint32_t* key_sorted = nullptr;       // the sorted rows of the current step
-    const uint32_t* pay_sorted = nullptr;       // their hit indices
+    const uint32_t* pay_sorted = nullptr;       // their hit indices (FP64 form)
+    uint64_t* pay64[2] = {nullptr, nullptr};    // nnz each, mixed forms: packed (sample, FP32 value) (ping-pong)
+    const uint64_t* pay64_sorted = nullptr;     // the sorted packed hits (mixed forms)
     uint32_t* hs_cnt = nullptr;       // 256 x tile stride: digit counts per tile
     uint32_t* hs_tot = nullptr;       // 256: digit totals
     uint32_t* head_cnt = nullptr;     // chunks: touched-row starts per chunk of sorted hits
@@ -140,21 +148,30 @@ int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
 // ---- step kernels (step_kernels.cu)
 int dedup(Session& s, int n, int64_t J, cudaStream_t st);
 int design_gram(Session& s, int n, int64_t J, cudaStream_t st);
+int design_pinv(Session& s, cudaStream_t st);
 int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist, const int64_t* count_dev,
               double* out_full, cudaStream_t st);
-int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st);
+int lookup_hits(Session& s, int n, int64_t J, bool packed, cudaStream_t st);
 int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st);
 int gram_reduce_to(Session& s, int64_t nblk, double* out, cudaStream_t st);
 int sigma_and_gram(Session& s, cudaStream_t st);
 int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st);
 
 // ---- load-balanced MTTKRP and post-processing, R <= 32 (post_kernels.cu)
-constexpr int kSegChunkHits = 128;
+constexpr int kSegChunkHits = 128;  // hits per chunk of the FP64 segmented reduction
+constexpr int kSegChunkF32 = 32;    // hits per chunk of the FP32 segmented reduction
+// FP32 row stride of the design rows (Df) and MTTKRP rows (Mc): R rounded up
+// to a multiple of 4, so a row is a whole number of float4s.
+__host__ __device__ inline int f32_row_stride(int R) { return (R + 3) & ~3; }
 constexpr int kCarryStride = 32;  // carry rows padded to 32 columns (R <= 32)
 
 // ---- hits grouped by output row (hitsort.cu)
 size_t hitsort_tile_stride(int64_t nnz);
-int hits_by_row(Session& s, int n, cudaStream_t st);
+// packed: carry (sample, FP32 value) through the sort (mixed forms) instead of
+// the hit index.
+int hits_by_row(Session& s, int n, bool packed, cudaStream_t st);
+// All nonzeros sorted by their mode-n index (key_sorted, pay_sorted = position).
+int nonzeros_by_row(Session& s, int n, cudaStream_t st);
 int mttkrp_solve_balanced(Session& s, int n, cudaStream_t st);
 int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st);
 int mttkrp_scatter_out(Session& s, double* out, cudaStream_t st);

@@ -4,10 +4,11 @@
 // share of the hits on a few rows, and atomics on those rows serialise).
 //
 //   expand     hit h (in sample order) -> key[h] = its output row, plus the
-//              sample j and value of the hit (ex_j, ex_val)
+//              sample j and value of the hit (ex_j, ex_val; or, for the
+//              mixed forms, one packed 64-bit payload)
 //   sort       8-bit digits, per pass: per-tile digit counts (upsweep), a
 //              scan of each digit's counts across tiles (spine), a stable
-//              scatter of (key, hit index) (downsweep)
+//              scatter of (key, hit index or packed hit) (downsweep)
 //   heads      runs of equal keys = touched rows: per-tile run counts, their
 //              scan, and the compaction into the touched list and the run
 //              starts (seg_start)
@@ -24,7 +25,9 @@ constexpr int kHsThreads = 256;
 constexpr int kHsItems = 16;
 constexpr int kHsTile = kHsThreads * kHsItems;  // 4096 hits per tile
 constexpr int kHsWarps = kHsThreads / 32;
-constexpr int kHsGrid = 152 * 4;
+constexpr int kHsGrid = 152 * 4;      // upsweep / heads
+constexpr int kHsDownGrid = 152 * 2;        // downsweep: one resident wave (99 registers x 256 threads)
+constexpr int kHsDownGridPacked = 152 * 3;  // 64-bit payloads, 8 items per thread
 constexpr int kExpandChunk = 256;  // hits per warp chunk in the expansion
 constexpr uint32_t kNoItem = 0xffffffffu;
 
@@ -41,11 +44,20 @@ __device__ __forceinline__ int64_t owner_in(const int64_t* __restrict__ f_off, i
 }
 
 // Hits in sample order: the owner sample of each hit by one binary search
-// per warp chunk for its bounds, then a search restricted to them.
+// per warp chunk for its bounds, then a search restricted to them.  kPacked
+// (mixed forms): the sample and the FP32 value go to one 64-bit payload
+// (sample in the low word, value bits in the high word) that travels with
+// the key through the sort; otherwise to ex_j / ex_val.
+__device__ __forceinline__ uint64_t pack_hit(uint32_t j, float v) {
+    return (uint64_t)j | ((uint64_t)__float_as_uint(v) << 32);
+}
+
+template <bool kPacked>
 __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t cap, const int64_t* __restrict__ f_off,
                                   const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
                                   const double* __restrict__ vals_n, uint32_t* __restrict__ key,
-                                  uint32_t* __restrict__ ex_j, double* __restrict__ ex_val, DeviceStatus* status) {
+                                  uint32_t* __restrict__ ex_j, double* __restrict__ ex_val,
+                                  uint64_t* __restrict__ pay64, DeviceStatus* status) {
     const int64_t ju = counters[0];
     int64_t H = counters[1];
     if (H > cap) {
@@ -67,8 +79,12 @@ __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t 
             const int64_t j = owner_in(f_off, jlo, jhi, h);
             const int64_t p = (int64_t)f_start[j] + (h - f_off[j]);
             key[h] = rows_n[p];
-            ex_j[h] = (uint32_t)j;
-            ex_val[h] = vals_n[p];
+            if (kPacked) {
+                pay64[h] = pack_hit((uint32_t)j, (float)vals_n[p]);
+            } else {
+                ex_j[h] = (uint32_t)j;
+                ex_val[h] = vals_n[p];
+            }
         }
     }
 }
@@ -111,24 +127,30 @@ __device__ __forceinline__ uint32_t block256_exclusive(uint32_t v, uint32_t* wsu
     return pre + inc - v;
 }
 
-// cnt[d * stride + t] = number of keys in tile t with digit d.
+// cnt[d * stride + t] = number of keys in tile t (ITEMS per thread) with digit d.
+template <int ITEMS>
 __global__ void __launch_bounds__(kHsThreads) hs_upsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                                 const uint32_t* __restrict__ keys, int shift,
                                                                 uint32_t* __restrict__ cnt, int64_t stride) {
+    constexpr int kTile = kHsThreads * ITEMS;
     __shared__ uint32_t c[256];
     const int64_t H = hit_count(counters, cap);
-    const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
+    const int64_t ntiles = (H + kTile - 1) / kTile;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         c[threadIdx.x] = 0;
         __syncthreads();
-        const int64_t base = t * kHsTile;
-#pragma unroll 4
-        for (int i = threadIdx.x; i < kHsTile; i += kHsThreads) {
-            const int64_t g = base + i;
-            unsigned d = 256;
-            if (g < H) d = (keys[g] >> shift) & 255u;
+        const int64_t base = t * kTile;
+        unsigned dg[ITEMS];  // all of the thread's loads issued before the first use
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            const int64_t g = base + threadIdx.x + r * kHsThreads;
+            dg[r] = g < H ? (keys[g] >> shift) & 255u : 256u;
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            const unsigned d = dg[r];
             const unsigned peers = digit_peers(d);
             if (d < 256 && (peers & lt) == 0) atomicAdd(&c[d], (uint32_t)__popc(peers));
         }
@@ -140,10 +162,12 @@ __global__ void __launch_bounds__(kHsThreads) hs_upsweep_kernel(const int64_t* _
 
 // Warp per digit: exclusive scan of the digit's tile counts in place (four
 // tiles per lane per round), the digit's total to tot[d].  32 blocks x 8 warps.
+template <int ITEMS>
 __global__ void hs_spine_kernel(const int64_t* __restrict__ counters, int64_t cap, uint32_t* __restrict__ cnt,
                                 int64_t stride, uint32_t* __restrict__ tot) {
+    constexpr int kTile = kHsThreads * ITEMS;
     const int64_t H = hit_count(counters, cap);
-    const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
+    const int64_t ntiles = (H + kTile - 1) / kTile;
     const int lane = threadIdx.x & 31;
     const int d = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (d >= 256) return;
@@ -171,23 +195,27 @@ __global__ void hs_spine_kernel(const int64_t* __restrict__ counters, int64_t ca
     if (lane == 0) tot[d] = carry;
 }
 
-// Stable scatter of (key, payload) by digit.  Items of a tile are taken in
-// order warp by warp (warp w owns items [w*512, (w+1)*512) of the tile,
-// round r lane l = item w*512 + r*32 + l); the multi-split gives each item
+// Stable scatter of (key, payload) by digit (payload PT: 32-bit hit index
+// or 64-bit packed hit).  Items of a tile are taken in
+// order warp by warp (warp w owns items [w*32*ITEMS, (w+1)*32*ITEMS) of the
+// tile, round r lane l = item w*32*ITEMS + r*32 + l); the multi-split gives each item
 // its rank among equal digits of its round, per-warp counters carry the rank
 // across rounds, and prefixes over warps and digits give its place in the
 // tile's digit order.  The tile is rearranged in shared memory first, so the
 // global writes run in contiguous pieces, one per digit.  pin == null: the
 // payload is the item's own index (the hit index of the first pass).
+template <typename PT, int ITEMS>
 __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                                   const uint32_t* __restrict__ kin,
-                                                                  const uint32_t* __restrict__ pin, int shift,
+                                                                  const PT* __restrict__ pin, int shift,
                                                                   const uint32_t* __restrict__ cnt, int64_t stride,
                                                                   const uint32_t* __restrict__ tot,
                                                                   uint32_t* __restrict__ kout,
-                                                                  uint32_t* __restrict__ pout) {
-    __shared__ uint32_t skey[kHsTile];
-    __shared__ uint32_t spay[kHsTile];
+                                                                  PT* __restrict__ pout) {
+    extern __shared__ __align__(16) unsigned char hs_dyn[];  // payloads, then keys, of one tile
+    constexpr int kTile = kHsThreads * ITEMS;
+    PT* spay = reinterpret_cast<PT*>(hs_dyn);
+    uint32_t* skey = reinterpret_cast<uint32_t*>(hs_dyn + sizeof(PT) * kTile);
     __shared__ uint32_t whist[kHsWarps][256];
     __shared__ uint32_t dbase[256];  // digit start in the whole output
     __shared__ uint32_t tstart[256];  // digit start within the tile
@@ -197,26 +225,31 @@ __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t*
     const unsigned lt = (1u << lane) - 1u;
     dbase[threadIdx.x] = block256_exclusive(tot[threadIdx.x], wsum);
     const int64_t H = hit_count(counters, cap);
-    const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
+    const int64_t ntiles = (H + kTile - 1) / kTile;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
 #pragma unroll
         for (int ww = 0; ww < kHsWarps; ww++) whist[ww][threadIdx.x] = 0;
         __syncthreads();
-        const int64_t tile0 = t * kHsTile;
-        const int64_t base = tile0 + (int64_t)w * 32 * kHsItems;
-        uint32_t kk[kHsItems], pp[kHsItems];
-        uint32_t rk[kHsItems];  // rank among equal digits of the warp; kNoItem for empty slots
+        const int64_t tile0 = t * kTile;
+        const int64_t base = tile0 + (int64_t)w * 32 * ITEMS;
+        uint32_t kk[ITEMS];
+        PT pp[ITEMS];
+        uint32_t rk[ITEMS];  // rank among equal digits of the warp; kNoItem for empty slots
 #pragma unroll
-        for (int r = 0; r < kHsItems; r++) {
+        for (int r = 0; r < ITEMS; r++) {  // loads first, all in flight together
             const int64_t g = base + r * 32 + lane;
-            unsigned d = 256;
             kk[r] = 0;
             pp[r] = 0;
+            rk[r] = kNoItem;
             if (g < H) {
                 kk[r] = kin[g];
-                pp[r] = pin ? pin[g] : (uint32_t)g;
-                d = (kk[r] >> shift) & 255u;
+                pp[r] = pin ? pin[g] : (PT)g;
+                rk[r] = 0;
             }
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            const unsigned d = rk[r] == kNoItem ? 256u : (kk[r] >> shift) & 255u;
             const unsigned peers = digit_peers(d);
             const uint32_t before = (d < 256) ? whist[w][d] : 0u;
             __syncwarp();
@@ -240,7 +273,7 @@ __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t*
         }
         __syncthreads();
 #pragma unroll
-        for (int r = 0; r < kHsItems; r++) {
+        for (int r = 0; r < ITEMS; r++) {
             if (rk[r] != kNoItem) {
                 const unsigned d = (kk[r] >> shift) & 255u;
                 const uint32_t l = tstart[d] + whist[w][d] + rk[r];
@@ -249,7 +282,7 @@ __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t*
             }
         }
         __syncthreads();
-        const int nvalid = (int)min((int64_t)kHsTile, H - tile0);
+        const int nvalid = (int)min((int64_t)kTile, H - tile0);
         for (int i = threadIdx.x; i < nvalid; i += kHsThreads) {
             const uint32_t k = skey[i];
             const unsigned d = (k >> shift) & 255u;
@@ -353,7 +386,11 @@ __global__ void __launch_bounds__(1024) hs_headscan_kernel(const int64_t* __rest
     }
 }
 
-size_t hitsort_tile_stride(int64_t nnz) { return (size_t)ceil_div(std::max<int64_t>(nnz, 1), kHsTile); }
+constexpr int kHsItemsPacked = 8;  // 64-bit payloads: smaller tiles keep 3 blocks per SM resident
+
+size_t hitsort_tile_stride(int64_t nnz) {
+    return (size_t)ceil_div(std::max<int64_t>(nnz, 1), kHsThreads * kHsItemsPacked);
+}
 
 static int key_bits(int64_t I) {
     int b = 0;
@@ -361,31 +398,63 @@ static int key_bits(int64_t I) {
     return b;
 }
 
-int hits_by_row(Session& s, int n, cudaStream_t st) {
-    const Lookup& L = s.look[n];
+// Sorts (hit_key[0], payload) by key: the identity payload (hit index) or
+// the packed hits in pay64[0].  Leaves key_sorted / pay_sorted / pay64_sorted.
+static int sort_keys(Session& s, int n, bool packed, cudaStream_t st) {
     const int64_t cap = s.nnz;
-    hit_expand_kernel<<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, L.rows, L.vals, s.hit_key[0],
-                                               s.ex_j, s.ex_val, s.status);
-    count_launch();
-    EXAFAC_CHECK_LAUNCH();
     const int passes = std::max(1, (key_bits(s.dims[n]) + 7) / 8);
     const int64_t stride = (int64_t)hitsort_tile_stride(s.nnz);
     int src = 0;
     for (int p = 0; p < passes; p++) {
         const int dst = src ^ 1;
-        hs_upsweep_kernel<<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[src], 8 * p, s.hs_cnt, stride);
-        count_launch();
-        hs_spine_kernel<<<32, 256, 0, st>>>(s.counters, cap, s.hs_cnt, stride, s.hs_tot);
-        count_launch();
-        hs_downsweep_kernel<<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[src],
-                                                           p == 0 ? nullptr : s.hit_pay[src], 8 * p, s.hs_cnt,
-                                                           stride, s.hs_tot, s.hit_key[dst], s.hit_pay[dst]);
+        if (packed) {
+            constexpr int IT = kHsItemsPacked;
+            hs_upsweep_kernel<IT><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[src], 8 * p, s.hs_cnt,
+                                                                 stride);
+            count_launch();
+            hs_spine_kernel<IT><<<32, 256, 0, st>>>(s.counters, cap, s.hs_cnt, stride, s.hs_tot);
+            count_launch();
+            const size_t smem = (sizeof(uint64_t) + sizeof(uint32_t)) * kHsThreads * IT;
+            hs_downsweep_kernel<uint64_t, IT><<<kHsDownGridPacked, kHsThreads, smem, st>>>(
+                s.counters, cap, s.hit_key[src], s.pay64[src], 8 * p, s.hs_cnt, stride, s.hs_tot, s.hit_key[dst],
+                s.pay64[dst]);
+        } else {
+            hs_upsweep_kernel<kHsItems><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[src], 8 * p,
+                                                                       s.hs_cnt, stride);
+            count_launch();
+            hs_spine_kernel<kHsItems><<<32, 256, 0, st>>>(s.counters, cap, s.hs_cnt, stride, s.hs_tot);
+            count_launch();
+            const size_t smem = (sizeof(uint32_t) + sizeof(uint32_t)) * kHsTile;
+            hs_downsweep_kernel<uint32_t, kHsItems><<<kHsDownGrid, kHsThreads, smem, st>>>(
+                s.counters, cap, s.hit_key[src], p == 0 ? nullptr : s.hit_pay[src], 8 * p, s.hs_cnt, stride, s.hs_tot,
+                s.hit_key[dst], s.hit_pay[dst]);
+        }
         count_launch();
         EXAFAC_CHECK_LAUNCH();
         src = dst;
     }
     s.key_sorted = s.hit_key[src];
-    s.pay_sorted = s.hit_pay[src];
+    s.pay_sorted = packed ? nullptr : s.hit_pay[src];
+    s.pay64_sorted = packed ? s.pay64[src] : nullptr;
+    return EXAFAC_OK;
+}
+
+int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
+    const Lookup& L = s.look[n];
+    const int64_t cap = s.nnz;
+    if (packed && !s.pay64[0]) {
+        set_error("packed hits need a session in a mixed precision");
+        return EXAFAC_ERR_ARG;
+    }
+    if (packed)
+        hit_expand_kernel<true><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, L.rows, L.vals,
+                                                         s.hit_key[0], nullptr, nullptr, s.pay64[0], s.status);
+    else
+        hit_expand_kernel<false><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, L.rows, L.vals,
+                                                          s.hit_key[0], s.ex_j, s.ex_val, nullptr, s.status);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    EXAFAC_TRY(sort_keys(s, n, packed, st));
     hs_heads_kernel<false><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, s.head_cnt, nullptr,
                                                           nullptr, nullptr);
     count_launch();
@@ -396,6 +465,22 @@ int hits_by_row(Session& s, int n, cudaStream_t st) {
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
+}
+
+// Every nonzero as a "hit": key = its mode-n index, payload = its position
+// (counters[1] = nnz); used by the exact MTTKRP.
+__global__ void nonzero_keys_kernel(int N, int n, int64_t nnz, const uint32_t* __restrict__ idx,
+                                    uint32_t* __restrict__ key, int64_t* __restrict__ counters) {
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t0 == 0) counters[1] = nnz;
+    for (int64_t i = t0; i < nnz; i += (int64_t)gridDim.x * blockDim.x) key[i] = idx[i * N + n];
+}
+
+int nonzeros_by_row(Session& s, int n, cudaStream_t st) {
+    nonzero_keys_kernel<<<152 * 8, 256, 0, st>>>(s.N, n, s.nnz, s.idx, s.hit_key[0], s.counters);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return sort_keys(s, n, false, st);
 }
 
 }  // namespace exafac

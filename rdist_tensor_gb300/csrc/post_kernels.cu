@@ -113,14 +113,14 @@ __global__ void __launch_bounds__(256) segreduce_kernel(int R, const int64_t* __
 // c0+1+l, c0+1+l+32, ... over all 32 padded columns, then a butterfly
 // reduce-scatter leaves column l's total in lane l (a fixed order, so results
 // are reproducible run to run).
-template <typename TA>
-__global__ void __launch_bounds__(256) segfix_kernel(int R, const int64_t* __restrict__ counters, int64_t cap,
+template <typename TA, int kChunk, int CB = 1>  // CB column blocks of 32 (carry stride 32 CB)
+__global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64_t* __restrict__ counters, int64_t cap,
                                                      const uint32_t* __restrict__ carry_row,
                                                      const uint32_t* __restrict__ keys,
                                                      const TA* __restrict__ carry_first,
                                                      const TA* __restrict__ carry_last, TA* __restrict__ Mc) {
     const int64_t H = min(counters[1], cap);
-    const int64_t nchunks = (H + kSegChunk - 1) / kSegChunk;
+    const int64_t nchunks = (H + kChunk - 1) / kChunk;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -131,30 +131,258 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, const int64_t* __res
         int64_t c1 = c0;
         for (int64_t b = c0 + 1;; b += 32) {
             const int64_t m = b + lane;
-            const bool on = m < nchunks && keys[m * kSegChunk] == row;
+            const bool on = m < nchunks && keys[m * kChunk] == row;
             const unsigned bal = __ballot_sync(full, on);
             c1 = b + __popc(bal) - 1;
             if (bal != full) break;
         }
-        TA acc[32];
+        for (int cb = 0; cb < CB; cb++) {
+            TA acc[32];
 #pragma unroll
-        for (int k = 0; k < 32; k++) acc[k] = 0;
-        for (int64_t m = c0 + 1 + lane; m <= c1; m += 32) {
-            const TA* src = carry_first + m * kCarryStride;
+            for (int k = 0; k < 32; k++) acc[k] = 0;
+            for (int64_t m = c0 + 1 + lane; m <= c1; m += 32) {
+                const TA* src = carry_first + m * (32 * CB) + 32 * cb;
 #pragma unroll
-            for (int k = 0; k < 32; k++) acc[k] += src[k];
+                for (int k = 0; k < 32; k++) acc[k] += src[k];
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) {
+                const bool upper = (lane & off) != 0;
+#pragma unroll
+                for (int k = 0; k < off; k++) {
+                    const TA send = upper ? acc[k] : acc[k + off];
+                    const TA keep = upper ? acc[k + off] : acc[k];
+                    acc[k] = keep + __shfl_xor_sync(full, send, off);
+                }
+            }
+            const int col = 32 * cb + lane;
+            if (col < R) Mc[(int64_t)row * ldm + col] = carry_last[c0 * (32 * CB) + col] + acc[0];
         }
+    }
+}
+
+// Exact MTTKRP (execute_exact_mttkrp, sort_lookup.hpp:440-495) over the
+// nonzeros sorted by their mode-n index: M[i_n] = sum of x * prod_{k != n}
+// U_k[i_k] (mode order from 1.0), in the chunked segmented form of the
+// sampled reduction, so the sums have a fixed order.  Lane l holds columns
+// l + 32 b, b < CB; a lane loads one nonzero's value and coordinates per
+// group of 32, and the factor rows of 8 nonzeros are gathered before their
+// FMAs.  Carries use a stride of 32 CB doubles per chunk.
+template <int CB>
+__global__ void __launch_bounds__(256) exact_segreduce_kernel(int N, int n, int R, const int64_t* __restrict__ counters,
+                                                              int64_t cap, const uint32_t* __restrict__ keys,
+                                                              const uint32_t* __restrict__ pay,
+                                                              const uint32_t* __restrict__ idx,
+                                                              const double* __restrict__ vals, FactorPtrs f,
+                                                              double* __restrict__ M, double* __restrict__ carry_first,
+                                                              double* __restrict__ carry_last,
+                                                              uint32_t* __restrict__ carry_row) {
+    constexpr int ldc = 32 * CB;
+    const int64_t H = min(counters[1], cap);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned full = 0xffffffffu;
+    for (int64_t c = warp; c * kSegChunk < H; c += nwarps) {
+        const int64_t cs = c * kSegChunk;
+        const int64_t ce = min(H, cs + kSegChunk);
+        uint32_t prev_row = kNoRow, next_row = kNoRow, first_row = kNoRow;
+        if (lane == 0 && cs > 0) prev_row = keys[cs - 1];
+        if (lane == 1 && ce < H) next_row = keys[ce];
+        if (lane == 2) first_row = keys[cs];
+        prev_row = __shfl_sync(full, prev_row, 0);
+        next_row = __shfl_sync(full, next_row, 1);
+        uint32_t cur = __shfl_sync(full, first_row, 2);
+        bool first_seg = true;
+        double acc[CB];
 #pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) {
-            const bool upper = (lane & off) != 0;
+        for (int b = 0; b < CB; b++) acc[b] = 0.0;
+        for (int64_t g = cs; g < ce; g += 32) {
+            const int nn = (int)min((int64_t)32, ce - g);
+            uint32_t hr = kNoRow, mi[kMaxModes];
+            double hv = 0.0;
 #pragma unroll
-            for (int k = 0; k < off; k++) {
-                const TA send = upper ? acc[k] : acc[k + off];
-                const TA keep = upper ? acc[k + off] : acc[k];
-                acc[k] = keep + __shfl_xor_sync(full, send, off);
+            for (int k = 0; k < kMaxModes; k++) mi[k] = 0;
+            if (lane < nn) {
+                hr = keys[g + lane];
+                const uint32_t i = pay[g + lane];
+                hv = vals[i];
+#pragma unroll
+                for (int k = 0; k < kMaxModes; k++)
+                    if (k < N) mi[k] = idx[(int64_t)i * N + k];
+            }
+            uint32_t up = __shfl_up_sync(full, hr, 1);
+            if (lane == 0) up = cur;
+            const unsigned brk = __ballot_sync(full, lane < nn && hr != up);
+            for (int t0 = 0; t0 < nn; t0 += 8) {
+                double prod[8][CB];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+#pragma unroll
+                    for (int b = 0; b < CB; b++) prod[u][b] = 1.0;
+#pragma unroll
+                    for (int k = 0; k < kMaxModes; k++) {
+                        if (k < N && k != n) {
+                            const int64_t row = __shfl_sync(full, mi[k], t0 + u);
+#pragma unroll
+                            for (int b = 0; b < CB; b++) {
+                                const int col = lane + 32 * b;
+                                if (col < R && t0 + u < nn) prod[u][b] *= f.U[k][row * R + col];
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int t = t0 + u;
+                    if (t < nn) {
+                        if ((brk >> t) & 1u) {
+#pragma unroll
+                            for (int b = 0; b < CB; b++) {
+                                const int col = lane + 32 * b;
+                                if (col < R) {
+                                    if (first_seg && cur == prev_row) carry_first[c * ldc + col] = acc[b];
+                                    else M[(int64_t)cur * R + col] = acc[b];
+                                }
+                                acc[b] = 0.0;
+                            }
+                            first_seg = false;
+                            cur = __shfl_sync(full, hr, t);
+                        }
+                        const double v = __shfl_sync(full, hv, t);
+#pragma unroll
+                        for (int b = 0; b < CB; b++) acc[b] = fma(prod[u][b], v, acc[b]);
+                    }
+                }
             }
         }
-        if (lane < R) Mc[(int64_t)row * R + lane] = carry_last[c0 * kCarryStride + lane] + acc[0];
+        const bool started_before = first_seg && cur == prev_row;
+        const bool continues = cur == next_row;
+#pragma unroll
+        for (int b = 0; b < CB; b++) {
+            const int col = lane + 32 * b;
+            if (col < R) {
+                if (started_before) carry_first[c * ldc + col] = acc[b];
+                else if (continues) carry_last[c * ldc + col] = acc[b];
+                else M[(int64_t)cur * R + col] = acc[b];
+            }
+        }
+        if (lane == 0) carry_row[c] = (!started_before && continues) ? cur : kNoRow;
+    }
+}
+
+template <int CB>
+static void launch_exact_mttkrp(Session& s, int n, double* M, FactorPtrs f, cudaStream_t st) {
+    const int hb = 152 * 8;
+    exact_segreduce_kernel<CB><<<hb, 256, 0, st>>>(s.N, n, s.R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.idx,
+                                                   s.vals, f, M, s.carry_first, s.carry_last, s.carry_row);
+    count_launch();
+    segfix_kernel<double, kSegChunk, CB><<<hb, 256, 0, st>>>(s.R, s.R, s.counters, s.nnz, s.carry_row, s.key_sorted,
+                                                             s.carry_first, s.carry_last, M);
+    count_launch();
+}
+
+int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st) {
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(M, 0, sizeof(double) * s.dims[n] * s.R, st));
+    EXAFAC_TRY(nonzeros_by_row(s, n, st));
+    FactorPtrs f;
+    for (int k = 0; k < kMaxModes; k++) f.U[k] = k < s.N ? s.F.U[k] : nullptr;
+    const int cb = (s.R + 31) / 32;
+    if (cb == 1) launch_exact_mttkrp<1>(s, n, M, f, st);
+    else if (cb == 2) launch_exact_mttkrp<2>(s, n, M, f, st);
+    else if (cb == 3) launch_exact_mttkrp<3>(s, n, M, f, st);
+    else launch_exact_mttkrp<4>(s, n, M, f, st);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+// FP32 segmented reduction: four 8-lane groups per warp, each owning a chunk
+// of kSegChunkF32 hits; within a group lane `sub` holds column block
+// [4 sub, 4 sub + 4) of a float4 row (Q = f32_row_stride(R) / 4 blocks), so
+// one 16-byte load brings a hit's four columns and the warp advances four
+// hits per instruction.  Each lane loads four of its group's hits (row and
+// the packed (sample, value) that travelled through the sort); hit t of the
+// chunk is broadcast from lane t % 8 of the group.  Design rows are gathered 8 hits at a time before their FMAs.  Rows
+// inside a chunk go straight to Mc (row stride 4Q floats); crossing rows
+// leave the same carries as the FP64 form (kCarryStride floats per chunk).
+template <int Q>
+__global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __restrict__ counters, int64_t cap,
+                                                            const uint32_t* __restrict__ keys,
+                                                            const uint64_t* __restrict__ pay64,
+                                                            const float4* __restrict__ D4, float4* __restrict__ Mc4,
+                                                            float4* __restrict__ carry_first4,
+                                                            float4* __restrict__ carry_last4,
+                                                            uint32_t* __restrict__ carry_row) {
+    constexpr int C = kSegChunkF32;
+    const int64_t H = min(counters[1], cap);
+    const int64_t nchunks = (H + C - 1) / C;
+    const int lane = threadIdx.x & 31, sub = lane & 7, grp = lane >> 3;
+    const unsigned gmask = 0xffu << (8 * grp);
+    const bool col = sub < Q;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t c = warp * 4 + grp; c < nchunks; c += nwarps * 4) {
+        const int64_t cs = c * C;
+        const int n = (int)min((int64_t)C, H - cs);
+        const uint32_t prev_row = cs > 0 ? keys[cs - 1] : kNoRow;
+        const uint32_t next_row = cs + n < H ? keys[cs + n] : kNoRow;
+        uint32_t hr[4], hj[4];
+        float hv[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {  // hit sub + 8 i of the chunk
+            const int t = sub + 8 * i;
+            hr[i] = kNoRow;
+            hj[i] = 0;
+            hv[i] = 0.f;
+            if (t < n) {
+                hr[i] = keys[cs + t];
+                const uint64_t p = pay64[cs + t];
+                hj[i] = (uint32_t)p;
+                hv[i] = __uint_as_float((uint32_t)(p >> 32));
+            }
+        }
+        uint32_t cur = __shfl_sync(gmask, hr[0], 0, 8);
+        bool first_seg = true;
+        float4 acc = zero4;
+#pragma unroll
+        for (int b = 0; b < C; b += 8) {
+            float4 d[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const uint32_t jt = __shfl_sync(gmask, hj[b / 8], u, 8);
+                d[u] = (b + u < n && col) ? D4[(int64_t)jt * Q + sub] : zero4;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int t = b + u;
+                const uint32_t rt = __shfl_sync(gmask, hr[b / 8], u, 8);
+                const float vt = __shfl_sync(gmask, hv[b / 8], u, 8);
+                if (t < n) {
+                    if (rt != cur) {  // the open segment ends inside the chunk
+                        if (col) {
+                            if (first_seg && cur == prev_row) carry_first4[c * 8 + sub] = acc;
+                            else Mc4[(int64_t)cur * Q + sub] = acc;
+                        }
+                        first_seg = false;
+                        cur = rt;
+                        acc = zero4;
+                    }
+                    acc.x = fmaf(d[u].x, vt, acc.x);
+                    acc.y = fmaf(d[u].y, vt, acc.y);
+                    acc.z = fmaf(d[u].z, vt, acc.z);
+                    acc.w = fmaf(d[u].w, vt, acc.w);
+                }
+            }
+        }
+        const bool started_before = first_seg && cur == prev_row;
+        const bool continues = cur == next_row;
+        if (col) {
+            if (started_before) carry_first4[c * 8 + sub] = acc;
+            else if (continues) carry_last4[c * 8 + sub] = acc;
+            else Mc4[(int64_t)cur * Q + sub] = acc;
+        }
+        if (sub == 0) carry_row[c] = (!started_before && continues) ? cur : kNoRow;
     }
 }
 
@@ -304,24 +532,48 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
 // ---------------------------------------------------------------------------
 constexpr int kSolveBlocks = 152 * 2;
 
+// MTTKRP rows of the touched rows into Mc: FP64 rows of R (TA = double) or
+// FP32 rows of f32_row_stride(R) floats (TA = float).
 template <typename TA>
 static int segmented_mttkrp(Session& s, cudaStream_t st) {
     const int R = s.R;
     const int hb = 152 * 8;
-    TA* Mc = reinterpret_cast<TA*>(s.Mc);
-    TA* cf = reinterpret_cast<TA*>(s.carry_first);
-    TA* cl = reinterpret_cast<TA*>(s.carry_last);
-    if (std::is_same<TA, double>::value)
+    if (std::is_same<TA, double>::value) {
+        double* Mc = s.Mc;
+        double* cf = s.carry_first;
+        double* cl = s.carry_last;
         segreduce_kernel<double, double><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.ex_j,
-                                                             s.ex_val, (const double*)s.D, (double*)Mc, (double*)cf,
-                                                             (double*)cl, s.carry_row);
-    else
-        segreduce_kernel<float, float><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.ex_j,
-                                                           s.ex_val, (const float*)s.Df, (float*)Mc, (float*)cf,
-                                                           (float*)cl, s.carry_row);
-    count_launch();
-    segfix_kernel<TA><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.carry_row, s.key_sorted, cf, cl, Mc);
-    count_launch();
+                                                             s.ex_val, (const double*)s.D, Mc, cf, cl, s.carry_row);
+        count_launch();
+        segfix_kernel<double, kSegChunk><<<hb, 256, 0, st>>>(R, R, s.counters, s.nnz, s.carry_row, s.key_sorted, cf,
+                                                             cl, Mc);
+        count_launch();
+    } else {
+        const int RS = f32_row_stride(R), Q = RS / 4;
+        float* Mc = reinterpret_cast<float*>(s.Mc);
+        float* cf = reinterpret_cast<float*>(s.carry_first);
+        float* cl = reinterpret_cast<float*>(s.carry_last);
+        const float4* D4 = reinterpret_cast<const float4*>(s.Df);
+#define EXAFAC_SEG_F32(QQ)                                                                                         \
+    segreduce_f32_kernel<QQ><<<hb, 256, 0, st>>>(s.counters, s.nnz, s.key_sorted, s.pay64_sorted, D4,                  \
+                                                 reinterpret_cast<float4*>(Mc), reinterpret_cast<float4*>(cf),      \
+                                                 reinterpret_cast<float4*>(cl), s.carry_row)
+        switch (Q) {
+            case 1: EXAFAC_SEG_F32(1); break;
+            case 2: EXAFAC_SEG_F32(2); break;
+            case 3: EXAFAC_SEG_F32(3); break;
+            case 4: EXAFAC_SEG_F32(4); break;
+            case 5: EXAFAC_SEG_F32(5); break;
+            case 6: EXAFAC_SEG_F32(6); break;
+            case 7: EXAFAC_SEG_F32(7); break;
+            default: EXAFAC_SEG_F32(8); break;
+        }
+#undef EXAFAC_SEG_F32
+        count_launch();
+        segfix_kernel<float, kSegChunkF32><<<hb, 256, 0, st>>>(R, RS, s.counters, s.nnz, s.carry_row, s.key_sorted, cf,
+                                                               cl, Mc);
+        count_launch();
+    }
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -360,6 +612,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
     __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
     __shared__ double red[32 * 33 / 2];
     const int P = R * (R + 1) / 2;
+    const int ldm = f32_row_stride(R);  // Mc row stride
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
         const int a = e / KC, b = e % KC;
@@ -395,7 +648,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
 #pragma unroll
         for (int r = 0; r < 32; r++) {
             const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
-            v[r] = (r < nrow && lane < R) ? Mc[row * R + lane] : 0.0f;
+            v[r] = (r < nrow && lane < R) ? Mc[row * ldm + lane] : 0.0f;
         }
 #pragma unroll
         for (int r = 0; r < 32; r++)

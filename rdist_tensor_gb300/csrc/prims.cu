@@ -83,22 +83,28 @@ __global__ void scan_partials_kernel(Tacc* partial, int64_t nb, Tacc* total) {
     if (threadIdx.x == 0 && total) *total = carry;
 }
 
-template <typename Tin, typename Tacc, bool kInclusive>
+// kNormalize (inclusive double scans): out_i = S_i / S_{n-1}, out_{n-1} = 1.
+// The tile is held in shared memory with one pad word after every 16
+// elements, so a thread's 16 consecutive elements (stride 17) fall in
+// distinct banks.
+__device__ __forceinline__ int scan_pad(int i) { return i + (i >> 4); }
+
+template <typename Tin, typename Tacc, bool kInclusive, bool kNormalize = false>
 __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, int64_t n,
-                           const Tacc* __restrict__ partial) {
-    __shared__ Tacc tile[kScanTile];
+                           const Tacc* __restrict__ partial, const Tacc* __restrict__ total = nullptr) {
+    __shared__ Tacc tile[kScanTile + kScanTile / 16];
     __shared__ Tacc red[33];
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
         int64_t g = base + i;
-        tile[i] = g < n ? (Tacc)in[g] : Tacc(0);
+        tile[scan_pad(i)] = g < n ? (Tacc)in[g] : Tacc(0);
     }
     __syncthreads();
     Tacc loc[kScanItems];
     Tacc sum = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-        loc[k] = tile[threadIdx.x * kScanItems + k];
+        loc[k] = tile[scan_pad(threadIdx.x * kScanItems + k)];
         sum += loc[k];
     }
     Tacc tot;
@@ -107,16 +113,26 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
     for (int k = 0; k < kScanItems; k++) {
         if (kInclusive) {
             run += loc[k];
-            tile[threadIdx.x * kScanItems + k] = run;
+            tile[scan_pad(threadIdx.x * kScanItems + k)] = run;
         } else {
-            tile[threadIdx.x * kScanItems + k] = run;
+            tile[scan_pad(threadIdx.x * kScanItems + k)] = run;
             run += loc[k];
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
-        int64_t g = base + i;
-        if (g < n) out[g] = tile[i];
+    if (kNormalize) {
+        // One reciprocal per block; the products differ from division by at
+        // most one rounding.
+        const Tacc rt = Tacc(1) / *total;
+        for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
+            int64_t g = base + i;
+            if (g < n) out[g] = (g == n - 1) ? Tacc(1) : tile[scan_pad(i)] * rt;
+        }
+    } else {
+        for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
+            int64_t g = base + i;
+            if (g < n) out[g] = tile[scan_pad(i)];
+        }
     }
 }
 
@@ -144,6 +160,17 @@ int scan_exclusive_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, int64
 }
 int scan_inclusive_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s) {
     return scan_impl<double, double, true>(in, out, n, total, scratch, s);
+}
+int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s) {
+    if (n <= 0) return EXAFAC_OK;
+    int64_t nb = ceil_div(n, kScanTile);
+    double* partial = reinterpret_cast<double*>(scratch);
+    scan_block_sums<double, double><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial); count_launch();
+    scan_partials_kernel<double><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
+    scan_apply<double, double, true, true><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, total);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -18,6 +18,10 @@ int scan_exclusive_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, int64
 // Inclusive scan of doubles.
 int scan_inclusive_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s);
 
+// Discrete CDF of nonnegative weights: out_i = S_i / S_{n-1} with S the
+// blockwise inclusive scan, out_{n-1} = 1; *total (device) = S_{n-1}.
+int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s);
+
 // Stable LSD radix sort of `count` keys (kw = 1: 64-bit keys in lo; kw = 2:
 // 128-bit (lo, hi)) over their low `bits` bits, carrying a uint32 payload.
 // Results land in (lo_out, hi_out, pay_out); the *_tmp arrays are ping-pong

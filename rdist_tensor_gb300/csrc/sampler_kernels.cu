@@ -52,52 +52,77 @@ int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st) {
 // libstdc++ discrete_distribution::param_type::_M_initialize
 // (bits/random.tcc:2657-2678) for short weight vectors, strictly in order:
 // sequential sum, p_i = w_i / sum, sequential partial sums, last = 1.0.
+// The weights are staged in shared memory (n <= kExactCdfMax) so the two
+// serial loops run on shared-memory latency.
 __global__ void cdf_sequential_kernel(const double* __restrict__ w, int64_t n, double* __restrict__ cdf,
                                       double* __restrict__ total) {
+    extern __shared__ double sh[];
     __shared__ double sum_sh;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) sh[i] = w[i];
+    __syncthreads();
     if (threadIdx.x == 0) {
         double sum = 0.0;
-        for (int64_t i = 0; i < n; i++) sum += w[i];
+        for (int64_t i = 0; i < n; i++) sum += sh[i];
         sum_sh = sum;
         *total = sum;
     }
     __syncthreads();
     const double sum = sum_sh;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) cdf[i] = w[i] / sum;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) sh[i] = sh[i] / sum;
     __syncthreads();
     if (threadIdx.x == 0) {
         double run = 0.0;
+        double next = sh[0];
         for (int64_t i = 0; i < n; i++) {
-            run += cdf[i];
-            cdf[i] = run;
+            const double cur = next;
+            if (i + 1 < n) next = sh[i + 1];
+            run += cur;
+            sh[i] = run;
         }
-        cdf[n - 1] = 1.0;
+        sh[n - 1] = 1.0;
     }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) cdf[i] = sh[i];
 }
 
-// Long weight vectors: blockwise inclusive scan S, cdf_i = S_i / S_n, last = 1.
-__global__ void cdf_normalize_kernel(double* __restrict__ cdf, int64_t n, const double* __restrict__ total) {
-    const double t = *total;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        cdf[i] = (i == n - 1) ? 1.0 : cdf[i] / t;
+// Guide table of a CDF (the bucket method of inverse-CDF sampling):
+// guide[b] = lower_bound(cdf, b / B), b = 0..B.  For u in [b/B, (b+1)/B) the
+// first entry >= u lies in [guide[b], guide[b+1]], because lower_bound is
+// monotone in u and cdf[guide[b+1]] >= (b+1)/B > u.  B is a power of two, so
+// b/B and floor(u B) are exact.
+__global__ void cdf_guide_kernel(const double* __restrict__ cdf, int64_t n, uint32_t* __restrict__ guide) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > kGuideBuckets) return;
+    const double x = (double)b / (double)kGuideBuckets;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (cdf[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    guide[b] = (uint32_t)(lo < n ? lo : n - 1);
 }
 
 int arls_build_cdf(Session& s, int k, cudaStream_t st) {
     const int64_t n = s.dims[k];
     if (n < 2) {
         // A one-row distribution always yields row 0 and consumes no draw.
-        cdf_sequential_kernel<<<1, 32, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k); count_launch();
+        cdf_sequential_kernel<<<1, 32, sizeof(double) * n, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k);
+        count_launch();
         EXAFAC_CHECK_LAUNCH();
         return EXAFAC_OK;
     }
     if (n <= kExactCdfMax) {
-        cdf_sequential_kernel<<<1, 256, 0, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k); count_launch();
-        EXAFAC_CHECK_LAUNCH();
-        return EXAFAC_OK;
+        const size_t smem = sizeof(double) * n;
+        if (smem > 48 * 1024)
+            EXAFAC_CUDA_TRY(cudaFuncSetAttribute(cdf_sequential_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem));
+        cdf_sequential_kernel<<<1, 256, smem, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k); count_launch();
+    } else {
+        EXAFAC_TRY(scan_cdf_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st));
     }
-    EXAFAC_TRY(scan_inclusive_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st));
-    int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
-    cdf_normalize_kernel<<<blocks, 256, 0, st>>>(s.cdf[k], n, s.cdf_total + k); count_launch();
+    cdf_guide_kernel<<<(unsigned)ceil_div(kGuideBuckets + 1, 256), 256, 0, st>>>(s.cdf[k], n, s.guide[k]);
+    count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -148,17 +173,22 @@ int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStre
 struct ArlsModes {
     const double* cdf[kMaxModes];
     const double* scores[kMaxModes];
+    const uint32_t* guide[kMaxModes];
     int64_t dims[kMaxModes];
 };
 
 // CP_ARLS_LEV::KRPDrawSamples + draw_leverage_score_samples
 // (cp_arls_lev.hpp:36-163) at one rank, thread per sample: the draw is the
-// first CDF entry >= u (lower_bound), the log weight log(sum) - log(l_idx)
-// is added mode by mode to -log J, then exponentiated.
+// first CDF entry >= u (lower_bound, searched between the guide entries of
+// u's bucket), the log weight log(sum) - log(l_idx) is added mode by mode to
+// -log J, then exponentiated.
 __global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const double* __restrict__ total,
                                  const double* __restrict__ uni, const uint32_t* __restrict__ perms,
                                  uint32_t* __restrict__ samples, double* __restrict__ weights,
                                  DeviceStatus* status) {
+    __shared__ double log_total[kMaxModes];
+    if (threadIdx.x < N) log_total[threadIdx.x] = log(total[threadIdx.x]);
+    __syncthreads();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= J) return;
     double w = 0.0 - log((double)J);
@@ -174,7 +204,8 @@ __global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const dou
         if (I >= 2) {
             const double u = uni[(int64_t)k * J + src];
             const double* cdf = m.cdf[k];
-            int64_t lo = 0, hi = I;
+            const int b = min((int)(u * (double)kGuideBuckets), kGuideBuckets - 1);
+            int64_t lo = m.guide[k][b], hi = (int64_t)m.guide[k][b + 1] + 1;
             while (lo < hi) {
                 int64_t mid = (lo + hi) >> 1;
                 if (cdf[mid] < u) lo = mid + 1;
@@ -182,7 +213,7 @@ __global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const dou
             }
             idx = lo < I ? lo : I - 1;
         }
-        const double lw = 0.0 + (log(total[k]) - log(m.scores[k][idx]));
+        const double lw = 0.0 + (log_total[k] - log(m.scores[k][idx]));
         samples[t * N + k] = (uint32_t)idx;
         w += lw;
     }
@@ -195,6 +226,7 @@ int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* p
     for (int k = 0; k < kMaxModes; k++) {
         m.cdf[k] = k < s.N ? s.cdf[k] : nullptr;
         m.scores[k] = k < s.N ? s.scores[k] : nullptr;
+        m.guide[k] = k < s.N ? s.guide[k] : nullptr;
         m.dims[k] = k < s.N ? s.dims[k] : 0;
     }
     arls_draw_kernel<<<(unsigned)ceil_div(J, 256), 256, 0, st>>>(s.N, n, J, m, s.cdf_total, uni, perms, s.samples,

@@ -45,6 +45,7 @@ static void carve(Session& s) {
         for (int k = 0; k < N; k++) {
             s.scores[k] = a.take<double>(s.dims[k]);
             s.cdf[k] = a.take<double>(s.dims[k]);
+            s.guide[k] = a.take<uint32_t>(kGuideBuckets + 1);
         }
     } else {
         for (int k = 0; k < N; k++) s.treeG[k] = a.take<double>(s.rtree[k].node_count * P);
@@ -96,17 +97,22 @@ static void carve(Session& s) {
     for (int b = 0; b < 2; b++) {
         s.hit_key[b] = a.take<uint32_t>(nnz);
         s.hit_pay[b] = a.take<uint32_t>(nnz);
+        if (s.cfg.precision != EXAFAC_PREC_FP64) s.pay64[b] = a.take<uint64_t>(nnz);
     }
     s.hs_cnt = a.take<uint32_t>(256 * (int64_t)hitsort_tile_stride(nnz));
     s.hs_tot = a.take<uint32_t>(256);
-    s.Mc = a.take<double>(I * R);
-    const int64_t chunks = ceil_div(nnz, kSegChunkHits) + 1;
+    s.Mc = a.take<double>(I * std::max(R, 16));  // FP64 rows of R, or FP32 rows padded to a multiple of 4
+    const int64_t chunks = ceil_div(nnz, kSegChunkF32) + 1;
     s.head_cnt = a.take<uint32_t>(chunks);
     s.head_base = a.take<int64_t>(chunks);
-    s.carry_first = a.take<double>(chunks * kCarryStride);
-    s.carry_last = a.take<double>(chunks * kCarryStride);
+    // carries: FP32 chunks of 32 hits x 32 columns, or FP64 chunks of 128 x
+    // up to 128 columns (the exact MTTKRP at R > 32)
+    const int64_t carry = std::max(chunks * kCarryStride,
+                                   (ceil_div(nnz, kSegChunkHits) + 1) * (int64_t)(32 * ceil_div(R, 32)));
+    s.carry_first = a.take<double>(carry);
+    s.carry_last = a.take<double>(carry);
     s.carry_row = a.take<uint32_t>(chunks);
-    s.Df = a.take<float>(J * R);
+    s.Df = a.take<float>(J * 32);  // rows padded to a multiple of 4 floats
 }
 
 static int plan(const exafac_als_config* cfg, Session& s) {
@@ -212,11 +218,33 @@ struct exafac_als_s {
     bool timing = false;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     double region[7] = {0, 0, 0, 0, 0, 0, 0};
+    // Side stream for the design pseudo-inverse, which runs beside the fiber
+    // lookup and the hit sort (fork / join events on the caller's stream).
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     ~exafac_als_s() {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
     }
 };
+
+// Launches the design pseudo-inverse on the side stream after the work
+// already queued on st; st must wait on h->join before reading Phi.
+static int fork_design_pinv(exafac_als_s* h, cudaStream_t st) {
+    if (!h->side) {
+        EXAFAC_CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+        EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
+    }
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->fork, st));
+    EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork, 0));
+    EXAFAC_TRY(design_pinv(h->s, h->side));
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->join, h->side));
+    return EXAFAC_OK;
+}
 
 static int mark(exafac_als_s* h, int i, cudaStream_t st) {
     if (h->timing) EXAFAC_CUDA_TRY(cudaEventRecord(h->ev[i], st));
@@ -352,12 +380,14 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     // R3: deduplicate, design rows, Gram, pseudo-inverse.
     EXAFAC_TRY(dedup(s, n, J, st));
     EXAFAC_TRY(design_gram(s, n, J, st));
+    EXAFAC_TRY(fork_design_pinv(h, st));
     EXAFAC_TRY(mark(h, 2, st));
     // R4: fiber lookup, hits grouped by output row, MTTKRP rows, then
     // U = MTTKRP * Phi on the touched rows (the other rows are zero).
     const bool arls = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV;
     const bool tiled = s.R <= 32;
-    EXAFAC_TRY(lookup_hits(s, n, J, st));
+    EXAFAC_TRY(lookup_hits(s, n, J, tiled && s.cfg.precision != EXAFAC_PREC_FP64, st));
+    EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join, 0));
     if (tiled) {
         EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
     } else {
@@ -411,7 +441,7 @@ extern "C" int exafac_als_sampled_mttkrp(exafac_als_t h, int32_t n, int64_t Ju, 
         EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.sd, samples, sizeof(uint32_t) * Ju * s.N, cudaMemcpyDeviceToDevice, st));
         EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.D, design, sizeof(double) * Ju * s.R, cudaMemcpyDeviceToDevice, st));
     }
-    EXAFAC_TRY(lookup_hits(s, n, std::max<int64_t>(Ju, 1), st));
+    EXAFAC_TRY(lookup_hits(s, n, std::max<int64_t>(Ju, 1), false, st));
     EXAFAC_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * s.dims[n] * s.R, st));
     if (s.R <= 32) EXAFAC_TRY(mttkrp_scatter_out(s, out, st));
     else EXAFAC_TRY(spmm_solve_into(s, n, nullptr, out, st));

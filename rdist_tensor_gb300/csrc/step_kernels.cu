@@ -12,9 +12,6 @@ namespace exafac {
 
 constexpr int kGramRows = 32;  // rows per block in the Gram partial kernels
 
-struct FactorPtrs {
-    const double* U[kMaxModes];
-};
 
 static FactorPtrs factor_ptrs(const Session& s) {
     FactorPtrs f;
@@ -206,11 +203,11 @@ __global__ void design_kernel(int N, int n, int R, const int64_t* __restrict__ j
     }
 }
 
-// Mixed forms: the same design rows, the MTTKRP operand D' kept in FP32, and
-// the Gram of the sqrt(w)-scaled rows from inputs rounded to TF32 (10-bit
-// mantissa, round to nearest) or BF16 (7-bit), products accumulated in FP32
-// within a block of 32 rows — the arithmetic of a tensor-core MMA with FP32
-// accumulation; blocks are summed in FP64.
+// Mixed forms: the same design rows with FP32 row products, the MTTKRP
+// operand D' kept in FP32, and the Gram of the sqrt(w)-scaled rows from
+// inputs rounded to TF32 (10-bit mantissa, round to nearest) or BF16 (7-bit)
+// on the tensor cores, accumulated in FP32 within a block of 32 rows and in
+// FP64 across blocks.
 __device__ __forceinline__ float round_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -218,43 +215,131 @@ __device__ __forceinline__ float round_tf32(float x) {
 }
 __device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
+// Tensor-core form.  A warp owns 32 design rows at a time:
+//   * factor rows are gathered one per load instruction (lane = column),
+//     32 rows in flight per mode, and multiplied in FP32;
+//   * D'_j = d_j * w_j goes to Df (FP32, rows of f32_row_stride(R) floats,
+//     zero padded), the Gram input round(d_j sqrt(w_j))
+//     to a shared tile T (32 rows x kDStride, zero padded);
+//   * the tile's Gram T^T T comes from mma.sync m16n8k8 TF32 instructions with
+//     FP32 accumulation (only the 16 x 8 blocks on or below the diagonal),
+//     added to FP64 accumulators after every 32-row tile.  BF16-rounded inputs
+//     are exact in TF32, so the same instruction serves both roundings.
+// The block's warps are summed in warp order into part[block] (packed).
+constexpr int kDesignWarps = 8;
+constexpr int kDStride = 40;  // floats per tile row: fragment loads hit 32 distinct banks
+constexpr int kDesignBlocks = 152 * 2;
+
+__device__ __forceinline__ void mma_tf32_16x8x8(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 template <int kRound>  // 1: TF32, 2: BF16
-__global__ void design_mixed_kernel(int N, int n, int R, const int64_t* __restrict__ ju_dev,
-                                    const uint32_t* __restrict__ sd, const double* __restrict__ wd, FactorPtrs f,
-                                    float* __restrict__ Df, double* __restrict__ part) {
-    __shared__ float sm[kGramRows * 32];
-    const int P = packed_size(R);
-    const int64_t ju = *ju_dev;
-    const int64_t base = (int64_t)blockIdx.x * kGramRows;
-    for (int e = threadIdx.x; e < kGramRows * R; e += blockDim.x) {
-        int lr = e / R, c = e % R;
-        int64_t j = base + lr;
-        float v = 0.f;
-        if (j < ju) {
-            double d = 1.0;
-            for (int k = 0; k < N; k++) {
-                if (k == n) continue;
-                d *= f.U[k][(int64_t)sd[j * N + k] * R + c];
-            }
-            const double sw = sqrt(wd[j]);
-            d *= sw;
-            Df[j * R + c] = (float)(d * sw);
-            v = kRound == 1 ? round_tf32((float)d) : round_bf16((float)d);
-        }
-        sm[lr * R + c] = v;
-    }
+__global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, int n, int R,
+                                                                       const int64_t* __restrict__ ju_dev,
+                                                                       const uint32_t* __restrict__ sd,
+                                                                       const double* __restrict__ wd, FactorPtrs f,
+                                                                       float* __restrict__ Df,
+                                                                       double* __restrict__ part) {
+    __shared__ __align__(16) float tile[kDesignWarps][32][kDStride];
+    __shared__ double red[32 * 33 / 2];
+    // lower-triangle (m-tile, n-tile) pairs of the 32 x 32 Gram: 16-row m-tiles, 8-column n-tiles
+    constexpr int kPairs = 6;
+    constexpr int kMt[kPairs] = {0, 0, 1, 1, 1, 1};
+    constexpr int kNt[kPairs] = {0, 1, 0, 1, 2, 3};
+    const int P = R * (R + 1) / 2;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gid = lane >> 2, tig = lane & 3;
+    for (int e = threadIdx.x; e < P; e += blockDim.x) red[e] = 0.0;
     __syncthreads();
-    for (int e = threadIdx.x; e < P; e += blockDim.x) {
-        int a = 0, rem = e;
-        while (rem >= R - a) {
-            rem -= R - a;
-            a++;
+    double gacc[kPairs][4];
+#pragma unroll
+    for (int p = 0; p < kPairs; p++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) gacc[p][i] = 0.0;
+    float (*t)[kDStride] = tile[w];
+    const int RS = (R + 3) & ~3;  // Df row stride (zero padded)
+    const int64_t ju = *ju_dev;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < ju; base += nwarps * 32) {
+        const int nrow = (int)min((int64_t)32, ju - base);
+        float prod[32];
+#pragma unroll
+        for (int r = 0; r < 32; r++) prod[r] = 1.0f;
+        for (int k = 0; k < N; k++) {
+            if (k == n) continue;
+            const uint32_t myidx = lane < nrow ? sd[(base + lane) * N + k] : 0u;
+            const double* Uk = f.U[k];
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                const int64_t i = __shfl_sync(0xffffffffu, myidx, r);
+                if (r < nrow && lane < R) prod[r] *= (float)Uk[i * R + lane];
+            }
         }
-        int b = a + rem;
-        float acc = 0.f;
-        for (int lr = 0; lr < kGramRows; lr++) acc = fmaf(sm[lr * R + a], sm[lr * R + b], acc);
-        part[(int64_t)blockIdx.x * P + e] = (double)acc;
+        double wj = 0.0;
+        if (lane < nrow) wj = wd[base + lane];
+        const float myw = (float)wj, mysw = (float)sqrt(wj);
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            const float wr = __shfl_sync(0xffffffffu, myw, r), swr = __shfl_sync(0xffffffffu, mysw, r);
+            float v = 0.0f;
+            if (r < nrow && lane < R) {
+                const float x = prod[r] * swr;
+                v = kRound == 1 ? round_tf32(x) : round_bf16(x);
+            }
+            if (r < nrow && lane < RS) Df[(base + r) * RS + lane] = lane < R ? prod[r] * wr : 0.0f;
+            t[r][lane] = v;  // lanes >= R and rows >= nrow: zero
+        }
+        __syncwarp();
+        float c[kPairs][4];
+#pragma unroll
+        for (int p = 0; p < kPairs; p++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) c[p][i] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+            const int k0 = ks * 8 + tig;
+            uint32_t af[2][4], bf[4][2];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {  // A = T^T: A[m][k] = T[k][m]
+                af[mt][0] = __float_as_uint(t[k0][16 * mt + gid]);
+                af[mt][1] = __float_as_uint(t[k0][16 * mt + gid + 8]);
+                af[mt][2] = __float_as_uint(t[k0 + 4][16 * mt + gid]);
+                af[mt][3] = __float_as_uint(t[k0 + 4][16 * mt + gid + 8]);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {  // B = T: B[k][n] = T[k][n]
+                bf[nt][0] = __float_as_uint(t[k0][8 * nt + gid]);
+                bf[nt][1] = __float_as_uint(t[k0 + 4][8 * nt + gid]);
+            }
+#pragma unroll
+            for (int p = 0; p < kPairs; p++) mma_tf32_16x8x8(c[p], af[kMt[p]], bf[kNt[p]]);
+        }
+#pragma unroll
+        for (int p = 0; p < kPairs; p++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) gacc[p][i] += (double)c[p][i];
+        __syncwarp();
     }
+    for (int ww = 0; ww < kDesignWarps; ww++) {  // block sum in warp order
+        if (w == ww) {
+#pragma unroll
+            for (int p = 0; p < kPairs; p++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int row = 16 * kMt[p] + gid + 8 * (i >> 1);
+                    const int col = 8 * kNt[p] + 2 * tig + (i & 1);
+                    if (row < R && col <= row) red[packed_index(R, col, row)] += gacc[p][i];
+                }
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
 }
 
 int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
@@ -266,24 +351,29 @@ int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
             return EXAFAC_ERR_UNSUPPORTED;
         }
         if (s.cfg.precision == EXAFAC_PREC_TF32)
-            design_mixed_kernel<1><<<(unsigned)nblk, 128, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
-                                                                    factor_ptrs(s), s.Df, s.part);
+            design_mma_kernel<1><<<kDesignBlocks, kDesignWarps * 32, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
+                                                                               factor_ptrs(s), s.Df, s.part);
         else
-            design_mixed_kernel<2><<<(unsigned)nblk, 128, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
-                                                                    factor_ptrs(s), s.Df, s.part);
+            design_mma_kernel<2><<<kDesignBlocks, kDesignWarps * 32, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
+                                                                               factor_ptrs(s), s.Df, s.part);
         count_launch();
-        gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram); count_launch();
+        gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, kDesignBlocks, R, s.dgram); count_launch();
         EXAFAC_CHECK_LAUNCH();
-        // FP64 Cholesky / pseudo-inverse of the FP32-accumulated Gram, plus
-        // one Newton step X <- X (2I - G X) on the solve.
-        return launch_pinv_refined(R, s.dgram, s.dpinv, 1e-11, s.vt, st);
+        return EXAFAC_OK;
     }
     design_kernel<<<(unsigned)nblk, 128, sizeof(double) * kGramRows * R, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
                                                                                factor_ptrs(s), s.D, s.part); count_launch();
     gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, nblk, R, s.dgram); count_launch();
     EXAFAC_CHECK_LAUNCH();
-    // compute_pinv_square (common.h:405-443), eigenvalue cut 1e-11.
-    return launch_pinv(R, s.dgram, s.dpinv, 1e-11, s.vt, st);
+    return EXAFAC_OK;
+}
+
+// Phi = pseudo-inverse of the design Gram: compute_pinv_square
+// (common.h:405-443, eigenvalue cut 1e-11); the mixed forms add one Newton
+// step X <- X (2I - G X) on the FP32-accumulated Gram.
+int design_pinv(Session& s, cudaStream_t st) {
+    if (s.cfg.precision != EXAFAC_PREC_FP64) return launch_pinv_refined(s.R, s.dgram, s.dpinv, 1e-11, s.vt, st);
+    return launch_pinv(s.R, s.dgram, s.dpinv, 1e-11, s.vt, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -346,9 +436,9 @@ int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st) {
     return EXAFAC_OK;
 }
 
-int lookup_hits(Session& s, int n, int64_t J, cudaStream_t st) {
+int lookup_hits(Session& s, int n, int64_t J, bool packed, cudaStream_t st) {
     EXAFAC_TRY(lookup_fibers(s, n, J, st));
-    return hits_by_row(s, n, st);
+    return hits_by_row(s, n, packed, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -560,32 +650,6 @@ int fit_residual(Session& s, double* out_dev, cudaStream_t st) {
     const int blocks = 152 * 8;
     fit_kernel<<<blocks, 256, 0, st>>>(s.N, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), s.F.sigma, s.fitpart); count_launch();
     sum_kernel<<<1, 256, 0, st>>>(s.fitpart, blocks, out_dev); count_launch();
-    EXAFAC_CHECK_LAUNCH();
-    return EXAFAC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Exact MTTKRP (execute_exact_mttkrp, sort_lookup.hpp:440-495): for every
-// nonzero, M[i_n] += (prod_{k != n} U_k[i_k]) * x.  Atomic accumulation.
-// ---------------------------------------------------------------------------
-__global__ void exact_mttkrp_kernel(int N, int n, int R, int64_t nnz, const uint32_t* __restrict__ idx,
-                                    const double* __restrict__ vals, FactorPtrs f, double* __restrict__ M) {
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz * R; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = e / R;
-        const int u = (int)(e % R);
-        const uint32_t* c = idx + i * N;
-        double p = 1.0;
-        for (int k = 0; k < N; k++) {
-            if (k == n) continue;
-            p *= f.U[k][(int64_t)c[k] * R + u];
-        }
-        atomicAdd(&M[(int64_t)c[n] * R + u], p * vals[i]);
-    }
-}
-
-int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st) {
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(M, 0, sizeof(double) * s.dims[n] * s.R, st));
-    exact_mttkrp_kernel<<<152 * 16, 256, 0, st>>>(s.N, n, s.R, s.nnz, s.idx, s.vals, factor_ptrs(s), M); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
