@@ -131,6 +131,10 @@ struct Session {
     double* carry_first = nullptr;  // chunks x kCarryStride
     double* carry_last = nullptr;   // chunks x kCarryStride
     uint32_t* carry_row = nullptr;  // chunks: row continuing past the chunk, or 0xffffffff
+    uint32_t* carry_seg = nullptr;  // chunks: that row's touched-row index (compact Mc)
+    uint32_t* chunk_seg = nullptr;  // chunks of kSegChunkF32 sorted hits: run index of the first hit
+    float* Uc = nullptr;            // Imax x 32, mixed forms: solved rows by touched-row index
+    uint32_t* rowbits = nullptr;    // ceil(Imax / 32): rows touched by the current step
     float* Df = nullptr;          // Jmax x R design rows (mixed forms)
 
     uint64_t seed = 0x5eed;

@@ -296,14 +296,16 @@ __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t*
 
 // Run heads (first hit of a row) of the sorted keys, per tile: the tile's
 // count, or (compact) the heads themselves written to touched / seg_start at
-// the tile's base.  Same item order as the downsweep.
+// the tile's base, and for every chunk of kSegChunkF32 hits the index of the
+// run holding its first hit (chunk_seg).  Same item order as the downsweep.
 template <bool kCompact>
 __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                               const uint32_t* __restrict__ keys,
                                                               uint32_t* __restrict__ tile_heads,
                                                               const int64_t* __restrict__ tile_base,
                                                               uint32_t* __restrict__ touched,
-                                                              int64_t* __restrict__ seg_start) {
+                                                              int64_t* __restrict__ seg_start,
+                                                              uint32_t* __restrict__ chunk_seg) {
     __shared__ uint32_t wsum[kHsWarps];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -344,6 +346,10 @@ __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __r
                     touched[q] = kk[r];
                     seg_start[q] = base + r * 32 + lane;
                 }
+                // each round is one chunk of kSegChunkF32 hits: the index of
+                // the run holding its first hit
+                if (lane == 0 && base + r * 32 < H)
+                    chunk_seg[(base + r * 32) / kSegChunkF32] = (uint32_t)(at + (heads[r] & 1u) - 1);
                 at += __popc(heads[r]);
             }
         }
@@ -456,12 +462,12 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(sort_keys(s, n, packed, st));
     hs_heads_kernel<false><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, s.head_cnt, nullptr,
-                                                          nullptr, nullptr);
+                                                          nullptr, nullptr, nullptr);
     count_launch();
     hs_headscan_kernel<<<1, 1024, 0, st>>>(s.counters, cap, s.head_cnt, s.head_base, s.counters + 2, s.seg_start);
     count_launch();
     hs_heads_kernel<true><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, nullptr, s.head_base,
-                                                         s.touched, s.seg_start);
+                                                         s.touched, s.seg_start, s.chunk_seg);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

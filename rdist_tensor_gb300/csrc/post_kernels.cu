@@ -113,9 +113,11 @@ __global__ void __launch_bounds__(256) segreduce_kernel(int R, const int64_t* __
 // c0+1+l, c0+1+l+32, ... over all 32 padded columns, then a butterfly
 // reduce-scatter leaves column l's total in lane l (a fixed order, so results
 // are reproducible run to run).
+// carry_seg != null: Mc is compact and the row's output index is carry_seg[c0].
 template <typename TA, int kChunk, int CB = 1>  // CB column blocks of 32 (carry stride 32 CB)
 __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64_t* __restrict__ counters, int64_t cap,
                                                      const uint32_t* __restrict__ carry_row,
+                                                     const uint32_t* __restrict__ carry_seg,
                                                      const uint32_t* __restrict__ keys,
                                                      const TA* __restrict__ carry_first,
                                                      const TA* __restrict__ carry_last, TA* __restrict__ Mc) {
@@ -156,7 +158,8 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
                 }
             }
             const int col = 32 * cb + lane;
-            if (col < R) Mc[(int64_t)row * ldm + col] = carry_last[c0 * (32 * CB) + col] + acc[0];
+            const int64_t out = carry_seg ? (int64_t)carry_seg[c0] : (int64_t)row;
+            if (col < R) Mc[out * ldm + col] = carry_last[c0 * (32 * CB) + col] + acc[0];
         }
     }
 }
@@ -277,8 +280,8 @@ static void launch_exact_mttkrp(Session& s, int n, double* M, FactorPtrs f, cuda
     exact_segreduce_kernel<CB><<<hb, 256, 0, st>>>(s.N, n, s.R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.idx,
                                                    s.vals, f, M, s.carry_first, s.carry_last, s.carry_row);
     count_launch();
-    segfix_kernel<double, kSegChunk, CB><<<hb, 256, 0, st>>>(s.R, s.R, s.counters, s.nnz, s.carry_row, s.key_sorted,
-                                                             s.carry_first, s.carry_last, M);
+    segfix_kernel<double, kSegChunk, CB><<<hb, 256, 0, st>>>(s.R, s.R, s.counters, s.nnz, s.carry_row, nullptr,
+                                                             s.key_sorted, s.carry_first, s.carry_last, M);
     count_launch();
 }
 
@@ -309,10 +312,12 @@ template <int Q>
 __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                             const uint32_t* __restrict__ keys,
                                                             const uint64_t* __restrict__ pay64,
+                                                            const uint32_t* __restrict__ chunk_seg,
                                                             const float4* __restrict__ D4, float4* __restrict__ Mc4,
                                                             float4* __restrict__ carry_first4,
                                                             float4* __restrict__ carry_last4,
-                                                            uint32_t* __restrict__ carry_row) {
+                                                            uint32_t* __restrict__ carry_row,
+                                                            uint32_t* __restrict__ carry_seg) {
     constexpr int C = kSegChunkF32;
     const int64_t H = min(counters[1], cap);
     const int64_t nchunks = (H + C - 1) / C;
@@ -343,6 +348,7 @@ __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __res
             }
         }
         uint32_t cur = __shfl_sync(gmask, hr[0], 0, 8);
+        int64_t seg = chunk_seg[c];  // compact index of the run holding hit cs
         bool first_seg = true;
         float4 acc = zero4;
 #pragma unroll
@@ -362,10 +368,11 @@ __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __res
                     if (rt != cur) {  // the open segment ends inside the chunk
                         if (col) {
                             if (first_seg && cur == prev_row) carry_first4[c * 8 + sub] = acc;
-                            else Mc4[(int64_t)cur * Q + sub] = acc;
+                            else Mc4[seg * Q + sub] = acc;
                         }
                         first_seg = false;
                         cur = rt;
+                        seg++;
                         acc = zero4;
                     }
                     acc.x = fmaf(d[u].x, vt, acc.x);
@@ -380,9 +387,12 @@ __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __res
         if (col) {
             if (started_before) carry_first4[c * 8 + sub] = acc;
             else if (continues) carry_last4[c * 8 + sub] = acc;
-            else Mc4[(int64_t)cur * Q + sub] = acc;
+            else Mc4[seg * Q + sub] = acc;
         }
-        if (sub == 0) carry_row[c] = (!started_before && continues) ? cur : kNoRow;
+        if (sub == 0) {
+            carry_row[c] = (!started_before && continues) ? cur : kNoRow;
+            carry_seg[c] = (uint32_t)seg;
+        }
     }
 }
 
@@ -532,8 +542,9 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
 // ---------------------------------------------------------------------------
 constexpr int kSolveBlocks = 152 * 2;
 
-// MTTKRP rows of the touched rows into Mc: FP64 rows of R (TA = double) or
-// FP32 rows of f32_row_stride(R) floats (TA = float).
+// MTTKRP rows of the touched rows into Mc: FP64 rows of R indexed by row
+// (TA = double), or compact FP32 rows of f32_row_stride(R) floats indexed by
+// touched-row position (TA = float).
 template <typename TA>
 static int segmented_mttkrp(Session& s, cudaStream_t st) {
     const int R = s.R;
@@ -545,8 +556,8 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
         segreduce_kernel<double, double><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.ex_j,
                                                              s.ex_val, (const double*)s.D, Mc, cf, cl, s.carry_row);
         count_launch();
-        segfix_kernel<double, kSegChunk><<<hb, 256, 0, st>>>(R, R, s.counters, s.nnz, s.carry_row, s.key_sorted, cf,
-                                                             cl, Mc);
+        segfix_kernel<double, kSegChunk><<<hb, 256, 0, st>>>(R, R, s.counters, s.nnz, s.carry_row, nullptr,
+                                                             s.key_sorted, cf, cl, Mc);
         count_launch();
     } else {
         const int RS = f32_row_stride(R), Q = RS / 4;
@@ -555,9 +566,9 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
         float* cl = reinterpret_cast<float*>(s.carry_last);
         const float4* D4 = reinterpret_cast<const float4*>(s.Df);
 #define EXAFAC_SEG_F32(QQ)                                                                                         \
-    segreduce_f32_kernel<QQ><<<hb, 256, 0, st>>>(s.counters, s.nnz, s.key_sorted, s.pay64_sorted, D4,                  \
+    segreduce_f32_kernel<QQ><<<hb, 256, 0, st>>>(s.counters, s.nnz, s.key_sorted, s.pay64_sorted, s.chunk_seg, D4,     \
                                                  reinterpret_cast<float4*>(Mc), reinterpret_cast<float4*>(cf),      \
-                                                 reinterpret_cast<float4*>(cl), s.carry_row)
+                                                 reinterpret_cast<float4*>(cl), s.carry_row, s.carry_seg)
         switch (Q) {
             case 1: EXAFAC_SEG_F32(1); break;
             case 2: EXAFAC_SEG_F32(2); break;
@@ -570,8 +581,8 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
         }
 #undef EXAFAC_SEG_F32
         count_launch();
-        segfix_kernel<float, kSegChunkF32><<<hb, 256, 0, st>>>(R, RS, s.counters, s.nnz, s.carry_row, s.key_sorted, cf,
-                                                               cl, Mc);
+        segfix_kernel<float, kSegChunkF32><<<hb, 256, 0, st>>>(R, RS, s.counters, s.nnz, s.carry_row, s.carry_seg,
+                                                               s.key_sorted, cf, cl, Mc);
         count_launch();
     }
     EXAFAC_CHECK_LAUNCH();
@@ -583,7 +594,8 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
 // A warp owns 32 touched rows at a time, staged in shared memory with rows
 // padded to KC floats (KC a multiple of 4, >= R):
 //   * rows move between HBM and the tile one row per instruction (lane =
-//     column), so each global access is one contiguous row;
+//     column), so each global access is one contiguous row; the solve reads
+//     and writes compact rows (Mc, Uc), the normalisation writes the factor;
 //   * row products run thread per row, the R x R operand read as float4
 //     broadcasts from shared memory;
 //   * the Gram of the solved rows is accumulated in 4 x 4 register blocks of
@@ -602,10 +614,9 @@ struct TileShape {
 
 template <int KC>
 __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R, const int64_t* __restrict__ counters,
-                                                                         const uint32_t* __restrict__ touched,
                                                                          const float* __restrict__ Mc,
                                                                          const double* __restrict__ Phi,
-                                                                         double* __restrict__ U,
+                                                                         float* __restrict__ Uc,
                                                                          double* __restrict__ part) {
     using S = TileShape<KC>;
     __shared__ __align__(16) float phi[KC][KC];
@@ -643,13 +654,9 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < nt; base += nwarps * 32) {
         const int nrow = (int)min((int64_t)32, nt - base);
-        const uint32_t myrow = lane < nrow ? touched[base + lane] : 0u;
-        float v[32];  // stage M rows (all 32 loads in flight), zero padding
+        float v[32];  // stage M rows (compact: the tile is one contiguous block), zero padding
 #pragma unroll
-        for (int r = 0; r < 32; r++) {
-            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
-            v[r] = (r < nrow && lane < R) ? Mc[row * ldm + lane] : 0.0f;
-        }
+        for (int r = 0; r < 32; r++) v[r] = (r < nrow && lane < R) ? Mc[(base + r) * ldm + lane] : 0.0f;
 #pragma unroll
         for (int r = 0; r < 32; r++)
             if (lane < KC) t[r][lane] = v[r];
@@ -681,10 +688,8 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
         for (int c = 0; c < KC; c += 4)
             *reinterpret_cast<float4*>(&t[lane][c]) = make_float4(u[c], u[c + 1], u[c + 2], u[c + 3]);
         __syncwarp();
-        for (int r = 0; r < nrow; r++) {  // store U rows (FP64 factor)
-            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
-            if (lane < R) U[row * R + lane] = (double)t[r][lane];
-        }
+        for (int r = 0; r < nrow; r++)  // store the solved rows, compact
+            if (lane < ldm) Uc[(base + r) * ldm + lane] = t[r][lane];
 #pragma unroll
         for (int q = 0; q < S::kNB; q++) {
             if (bi[q] >= 0) {
@@ -725,11 +730,14 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
     for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
 }
 
-// u_r = U_r / sigma and, when P != null, l_r = u_r^T P u_r, FP32 row
-// products; rows staged as in solve_gram_f32_kernel.
+// u_r = Uc_r / sigma (Uc: the compact rows of solve_gram_f32_kernel) written
+// to U at the touched row, and, when P != null, l_r = u_r^T P u_r in FP32;
+// rows staged as in solve_gram_f32_kernel.  This is the one scattered pass
+// over the factor.
 template <int KC>
 __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, const int64_t* __restrict__ counters,
                                                                       const uint32_t* __restrict__ touched,
+                                                                      const float* __restrict__ Uc,
                                                                       const double* __restrict__ sigma,
                                                                       const double* __restrict__ Pm,
                                                                       const int* __restrict__ degenerate,
@@ -738,7 +746,9 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
     __shared__ __align__(16) float psm[KC][KC];
     __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
     __shared__ double sg[32];
-    if (*degenerate) return;  // handled over all rows by scale_rows
+    // A zero column norm: write the unscaled rows and leave the division of
+    // every row (as the reference does) to scale_rows_if_degenerate.
+    const bool deg = *degenerate != 0;
     for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
         const int a = e / KC, b = e % KC;
         psm[a][b] = (Pm && a < R && b < R) ? (float)Pm[a * R + b] : 0.0f;
@@ -748,32 +758,34 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
     for (int c = threadIdx.x; c < 32; c += blockDim.x) sg[c] = c < R ? 1.0 / sigma[c] : 0.0;
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ldm = f32_row_stride(R);  // Uc row stride
     float (*t)[kTileStride] = tile[w];
-    const double sgl = sg[lane];
+    const double sgl = deg ? 1.0 : sg[lane];
     const int64_t nt = counters[2];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < nt; base += nwarps * 32) {
         const int nrow = (int)min((int64_t)32, nt - base);
         const uint32_t myrow = lane < nrow ? touched[base + lane] : 0u;
+        {
+            float v[32];  // the tile's compact rows (one contiguous block), all loads in flight
 #pragma unroll
-        for (int h = 0; h < 32; h += 16) {  // 16 row loads in flight at a time
-            double x[16];
+            for (int r = 0; r < 32; r++) v[r] = (r < nrow && lane < R) ? Uc[(base + r) * ldm + lane] : 0.0f;
 #pragma unroll
-            for (int r = 0; r < 16; r++) {
-                const int64_t row = __shfl_sync(0xffffffffu, myrow, h + r);
-                x[r] = (h + r < nrow && lane < R) ? U[row * R + lane] : 0.0;
-            }
-#pragma unroll
-            for (int r = 0; r < 16; r++) {
-                const int64_t row = __shfl_sync(0xffffffffu, myrow, h + r);
-                const double y = x[r] * sgl;
-                if (h + r < nrow && lane < R) U[row * R + lane] = y;
-                if (lane < KC) t[h + r][lane] = (float)y;
+            for (int r = 0; r < 32; r++)
+                if (lane < KC) t[r][lane] = v[r];
+        }
+#pragma unroll 4
+        for (int r = 0; r < nrow; r++) {  // normalised FP64 rows to the factor, one row per store
+            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
+            if (lane < KC) {
+                const double y = (double)t[r][lane] * sgl;
+                if (lane < R) U[row * R + lane] = y;
+                t[r][lane] = (float)y;
             }
         }
         __syncwarp();
-        if (Pm && lane < nrow) {
+        if (Pm && !deg && lane < nrow) {
             float u[KC];
 #pragma unroll
             for (int c = 0; c < KC; c += 4) {
@@ -808,13 +820,13 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
 template <int KC>
 static void launch_solve_f32(Session& s, int n, cudaStream_t st) {
     solve_gram_f32_kernel<KC><<<kSolveBlocks, kSolveWarps * 32, 0, st>>>(
-        s.R, s.counters, s.touched, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.F.U[n], s.part);
+        s.R, s.counters, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.Uc, s.part);
 }
 
 template <int KC>
 static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
     normlev_f32_kernel<KC><<<kSolveBlocks, kSolveWarps * 32, 0, st>>>(
-        s.R, s.counters, s.touched, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
+        s.R, s.counters, s.touched, s.Uc, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
         s.F.U[n], arls ? s.scores[n] : nullptr);
 }
 

@@ -112,6 +112,10 @@ static void carve(Session& s) {
     s.carry_first = a.take<double>(carry);
     s.carry_last = a.take<double>(carry);
     s.carry_row = a.take<uint32_t>(chunks);
+    s.carry_seg = a.take<uint32_t>(chunks);
+    s.chunk_seg = a.take<uint32_t>(chunks);
+    if (s.cfg.precision != EXAFAC_PREC_FP64) s.Uc = a.take<float>(I * 32);
+    s.rowbits = a.take<uint32_t>(ceil_div(I, 32));
     s.Df = a.take<float>(J * 32);  // rows padded to a multiple of 4 floats
 }
 

@@ -572,25 +572,42 @@ int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st) {
 
 // Warp per 32 listed rows: indices loaded together, then one row per store
 // instruction (lane = column).
+// Rows listed in `keep` (a bitmap over the rows) are skipped: they are
+// rewritten by the current update.
 __global__ void zero_rows_kernel(int R, const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
-                                 double* __restrict__ U, double* __restrict__ scores) {
+                                 const uint32_t* __restrict__ keep, double* __restrict__ U,
+                                 double* __restrict__ scores) {
     const int64_t cnt = *cnt_dev;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < cnt; base += nwarps * 32) {
         const int n = (int)min((int64_t)32, cnt - base);
-        const uint32_t myrow = lane < n ? list[base + lane] : 0u;
-        if (scores && lane < n) scores[myrow] = 0.0;
-        for (int r = 0; r < n; r++) {
+        uint32_t myrow = lane < n ? list[base + lane] : 0u;
+        bool clear = lane < n && !(keep && ((keep[myrow >> 5] >> (myrow & 31)) & 1u));
+        if (scores && clear) scores[myrow] = 0.0;
+        unsigned todo = __ballot_sync(0xffffffffu, clear);
+        while (todo) {
+            const int r = __ffs(todo) - 1;
+            todo &= todo - 1;
             const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
             for (int c = lane; c < R; c += 32) U[row * R + c] = 0.0;
         }
     }
 }
 
+__global__ void mark_rows_kernel(const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
+                                 uint32_t* __restrict__ bits) {
+    const int64_t cnt = *cnt_dev;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = list[i];
+        atomicOr(&bits[r >> 5], 1u << (r & 31));
+    }
+}
+
 // Clears the rows of U_n (and their leverage scores) that the previous update
-// left nonzero; a factor that was never updated is cleared entirely.
+// left nonzero and the current one (s.touched, counters[2]) does not write;
+// a factor that was never updated is cleared entirely.
 int zero_factor_rows(Session& s, int n, cudaStream_t st) {
     const int R = s.R;
     double* sc = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV ? s.scores[n] : nullptr;
@@ -598,7 +615,10 @@ int zero_factor_rows(Session& s, int n, cudaStream_t st) {
         EXAFAC_CUDA_TRY(cudaMemsetAsync(s.F.U[n], 0, sizeof(double) * s.dims[n] * R, st));
         if (sc) EXAFAC_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * s.dims[n], st));
     } else {
-        zero_rows_kernel<<<152 * 8, 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.F.U[n], sc); count_launch();
+        EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowbits, 0, sizeof(uint32_t) * ceil_div(s.dims[n], 32), st));
+        mark_rows_kernel<<<152 * 8, 256, 0, st>>>(s.touched, s.counters + 2, s.rowbits); count_launch();
+        zero_rows_kernel<<<152 * 8, 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.rowbits, s.F.U[n], sc);
+        count_launch();
         EXAFAC_CHECK_LAUNCH();
     }
     return EXAFAC_OK;
