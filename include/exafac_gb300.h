@@ -210,6 +210,41 @@ int exafac_als_step_info(exafac_als_t s, exafac_step_info* out, void* stream);
 int exafac_als_last_dedup(exafac_als_t s, const uint32_t** samples_dev, const double** weights_dev,
                           const double** design_gram_dev, const double** design_pinv_dev);
 
+/* ---------------------------------------------------------------------------
+ * Generalized CP on sampled entries.  No counterpart in the reference: these
+ * are the forward and adjoint of a sampled-MTTKRP torch.autograd.Function
+ * (rdist_tensor_gb300/gcp.py) for gradient-based CP with Poisson or
+ * Bernoulli losses.  Nearest reference relatives: execute_exact_mttkrp
+ * (sort_lookup.hpp:440-495) and the zero-sampling fit estimate
+ * (exafac/low_rank_tensor.py:110-184).
+ *
+ * Factors are device row-major dims[k] x R matrices of `dtype`; idx is a
+ * device int32 [J x N] coordinate array.  Entries with a coordinate outside
+ * dims are skipped (model value 0, no gradient) and set *status_dev to 1
+ * when status_dev is not null.
+ * ------------------------------------------------------------------------- */
+enum { EXAFAC_DTYPE_F32 = 0, EXAFAC_DTYPE_F64 = 1 };
+
+/* m[j] = sum_r prod_k U_k[idx[j,k], r]. */
+int exafac_cp_sampled_model(int32_t N, int32_t R, const int64_t* dims_host, int64_t J, const int32_t* idx_dev,
+                            const void* const* factors_dev, void* m_dev, int32_t dtype, int32_t* status_dev,
+                            void* stream);
+
+/* Adjoint of the model: grads[n][idx[j,n], :] += grad_m[j] * prod_{k != n}
+ * U_k[idx[j,k], :] for every n with grads[n] != null (accumulates; the
+ * Khatri-Rao rows are recomputed, not stored; atomic accumulation). */
+int exafac_cp_sampled_adjoint(int32_t N, int32_t R, const int64_t* dims_host, int64_t J, const int32_t* idx_dev,
+                              const void* grad_m_dev, const void* const* factors_dev, void* const* grads_dev,
+                              int32_t dtype, int32_t* status_dev, void* stream);
+
+/* Stratified entry sample: J_nz nonzeros drawn uniformly with replacement
+ * (value x, weight nnz / J_nz) followed by J_z uniform coordinates taken as
+ * zeros (value 0, weight (prod dims - nnz) / J_z); Philox4x32-10 keyed by
+ * seed at counter `counter`.  Outputs idx [J x N], x [J], w [J]. */
+int exafac_gcp_sample_entries(int32_t N, const int64_t* dims_host, int64_t nnz, const int32_t* nz_idx_dev,
+                              const void* nz_vals_dev, int64_t J_nz, int64_t J_z, uint64_t seed, uint64_t counter,
+                              int32_t* idx_dev, void* x_dev, void* w_dev, int32_t dtype, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

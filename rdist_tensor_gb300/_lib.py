@@ -17,6 +17,7 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "device-side check failed",
 SAMPLER = {"cp_arls_lev": 0, "sts_cp": 1}
 PRECISION = {"fp64": 0, "tf32": 1, "bf16": 2}
 PREPROCESSING = {"none": 0, "None": 0, "log_count": 1, "ones": 2}
+DTYPE = {"float32": 0, "float64": 1}
 
 
 class ExafacError(RuntimeError):
@@ -72,6 +73,10 @@ SIGNATURES = {
     "exafac_als_step_info": (ctypes.c_int, [_P, ctypes.POINTER(StepInfo), _P]),
     "exafac_als_last_dedup": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                                              ctypes.POINTER(_P)]),
+    "exafac_cp_sampled_model": (ctypes.c_int, [_I32, _I32, _P, _I64, _P, _P, _P, _I32, _P, _P]),
+    "exafac_cp_sampled_adjoint": (ctypes.c_int, [_I32, _I32, _P, _I64, _P, _P, _P, _P, _I32, _P, _P]),
+    "exafac_gcp_sample_entries": (ctypes.c_int, [_I32, _P, _I64, _P, _P, _I64, _I64, ctypes.c_uint64,
+                                                 ctypes.c_uint64, _P, _P, _P, _I32, _P]),
 }
 
 _lib = None

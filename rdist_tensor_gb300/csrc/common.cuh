@@ -53,6 +53,27 @@ void count_launch();
         if (_s != EXAFAC_OK) return _s;                                                           \
     } while (0)
 
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter-based uniforms.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        unsigned lo0 = c.x * 0xD2511F53u, hi0 = __umulhi(c.x, 0xD2511F53u);
+        unsigned lo1 = c.z * 0xCD9E8D57u, hi1 = __umulhi(c.z, 0xCD9E8D57u);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Uniform double in [0, 1) from 53 bits of two words.
+__device__ __forceinline__ double u53(unsigned a, unsigned b) {
+    unsigned long long x = ((unsigned long long)a << 32) | b;
+    return (double)(x >> 11) * 0x1.0p-53;
+}
+
 // Device error word: kernels that find an out-of-range index record it here
 // (first writer wins) and skip the access instead of trapping.
 struct DeviceStatus {

@@ -1,0 +1,169 @@
+"""Generalized CP: the sampled-model autograd Function and its hand-written
+adjoint, against finite differences and a dense FP64 reference gradient;
+the stratified entry sampler; a short Poisson fit."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from rdist_tensor_gb300 import gcp
+
+    return gcp
+
+
+def _all_entries(dims):
+    grids = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    return np.stack([g.reshape(-1) for g in grids], axis=1).astype(np.int32)
+
+
+def _dense_model(factors):
+    N = len(factors)
+    letters = "abcdefgh"[:N]
+    expr = ",".join(f"{c}r" for c in letters) + "->" + letters
+    return torch.einsum(expr, *factors)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_model_matches_dense(dtype):
+    gcp = _cuda()
+    dt = getattr(torch, dtype)
+    dims = (7, 6, 5)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    U = [torch.randn((d, 4), generator=g, device="cuda", dtype=dt) for d in dims]
+    idx = torch.as_tensor(_all_entries(dims), device="cuda")
+    m = gcp.sampled_model(idx, U)
+    ref = _dense_model([u.double() for u in U]).reshape(-1)
+    tol = 1e-5 if dtype == "float32" else 1e-13
+    assert torch.max(torch.abs(m.double() - ref)).item() <= tol * torch.max(torch.abs(ref)).item()
+
+
+def test_adjoint_matches_finite_differences():
+    """FP64 kernels: autograd gradient of a weighted Poisson objective on 60
+    sampled entries (with repeats) against central differences."""
+    gcp = _cuda()
+    dims, R = (6, 5, 4), 3
+    rng = np.random.default_rng(3)
+    idx = torch.as_tensor(np.stack([rng.integers(0, d, 60) for d in dims], axis=1).astype(np.int32), device="cuda")
+    x = torch.as_tensor(rng.poisson(2.0, 60).astype(np.float64), device="cuda")
+    w = torch.as_tensor(rng.uniform(0.5, 2.0, 60), device="cuda")
+    U = [torch.as_tensor(rng.uniform(0.2, 1.0, (d, R)), device="cuda").requires_grad_() for d in dims]
+
+    def objective(fs):
+        m = gcp.sampled_model(idx, fs)
+        return (w * gcp.loss_values("poisson", x, m)).sum()
+
+    objective(U).backward()
+    h = 1e-6
+    for k, Uk in enumerate(U):
+        fd = torch.zeros_like(Uk)
+        for i in range(dims[k]):
+            for r in range(R):
+                with torch.no_grad():
+                    base = [u.detach().clone() for u in U]
+                    plus = [u.clone() for u in base]
+                    minus = [u.clone() for u in base]
+                    plus[k][i, r] += h
+                    minus[k][i, r] -= h
+                    fd[i, r] = (objective(plus) - objective(minus)) / (2 * h)
+        err = torch.max(torch.abs(Uk.grad - fd)).item() / torch.max(torch.abs(fd)).item()
+        assert err < 1e-7, (k, err)
+
+
+@pytest.mark.parametrize("dtype,tol", [("float32", 2e-4), ("float64", 1e-11)])
+def test_adjoint_matches_dense_fp64_gradient(dtype, tol):
+    """All 200^3 entries of a Poisson count tensor as the sample (weight 1):
+    the kernels' gradient of the Poisson objective against the dense FP64
+    gradient einsum(Y, U_j, U_k), Y = df/dm over the dense tensor."""
+    gcp = _cuda()
+    from rdist_tensor_gb300 import synthetic
+
+    dims, R = (200, 200, 200), 32
+    d, nz_idx, nz_vals, _ = synthetic.poisson_counts(dims, 400_000, rank=16, seed=5)
+    X = torch.zeros(dims, dtype=torch.float64, device="cuda")
+    X[tuple(torch.as_tensor(nz_idx.astype(np.int64), device="cuda").T)] = torch.as_tensor(
+        nz_vals.astype(np.float64), device="cuda")
+    dt = getattr(torch, dtype)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    U64 = [torch.rand((n, R), generator=g, device="cuda", dtype=torch.float64) * 0.3 + 0.05 for n in dims]
+    U = [u.to(dt).requires_grad_() for u in U64]
+    idx = torch.as_tensor(_all_entries(dims), device="cuda")
+    x = X.reshape(-1).to(dt)
+    m = gcp.sampled_model(idx, U)
+    gcp.loss_values("poisson", x, m).sum().backward()
+    Ud = [u.detach().double() for u in U]
+    M = _dense_model(Ud)
+    Y = 1.0 - X / (M + gcp.EPS)
+    ref = [torch.einsum("ijk,jr,kr->ir", Y, Ud[1], Ud[2]), torch.einsum("ijk,ir,kr->jr", Y, Ud[0], Ud[2]),
+           torch.einsum("ijk,ir,jr->kr", Y, Ud[0], Ud[1])]
+    for k in range(3):
+        err = torch.max(torch.abs(U[k].grad.double() - ref[k])).item() / torch.max(torch.abs(ref[k])).item()
+        print(f"{dtype} mode {k}: max rel err {err:.2e}")
+        assert err < tol, (k, err)
+
+
+def test_sampler_strata():
+    gcp = _cuda()
+    from rdist_tensor_gb300 import synthetic
+
+    dims = (300, 200, 100)
+    _, nz_idx, nz_vals = synthetic.random_sparse(dims, 5000, seed=2)
+    idx = torch.as_tensor(nz_idx.astype(np.int32), device="cuda")
+    vals = torch.as_tensor(nz_vals, device="cuda")
+    J_nz, J_z = 4000, 6000
+    s_idx, s_x, s_w = gcp.sample_entries(idx, vals, dims, J_nz, J_z, seed=11, counter=0)
+    s_idx, s_x, s_w = s_idx.cpu().numpy(), s_x.cpu().numpy(), s_w.cpu().numpy()
+    lookup = {tuple(c): v for c, v in zip(nz_idx.tolist(), nz_vals.tolist())}
+    for c, v in zip(s_idx[:J_nz].tolist(), s_x[:J_nz].tolist()):
+        assert lookup[tuple(c)] == v
+    assert np.all(s_x[J_nz:] == 0.0)
+    for k, dk in enumerate(dims):
+        assert s_idx[:, k].min() >= 0 and s_idx[:, k].max() < dk
+    assert np.allclose(s_w[:J_nz], 5000 / J_nz)
+    assert np.allclose(s_w[J_nz:], (np.prod(dims) - 5000) / J_z)
+    # a different counter gives a different sample
+    s2, _, _ = gcp.sample_entries(idx, vals, dims, J_nz, J_z, seed=11, counter=1)
+    assert not np.array_equal(s2.cpu().numpy(), s_idx)
+
+
+def test_out_of_range_entry_is_skipped_and_flagged():
+    gcp = _cuda()
+    dims, R = (5, 4, 3), 2
+    U = [torch.rand((d, R), device="cuda", dtype=torch.float64).requires_grad_() for d in dims]
+    idx = torch.tensor([[0, 0, 0], [5, 1, 1], [4, 3, 2]], dtype=torch.int32, device="cuda")
+    m = gcp.SampledCPModel.apply(idx, *U)
+    assert m[1].item() == 0.0
+    m.sum().backward()
+    # the skipped entry adds nothing: compare with the two valid entries alone
+    V = [u.detach().clone().requires_grad_() for u in U]
+    gcp.sampled_model(idx[[0, 2]].contiguous(), V).sum().backward()
+    for a, b in zip(U, V):
+        assert torch.equal(a.grad, b.grad)
+
+
+def test_poisson_fit_decreases_objective():
+    gcp = _cuda()
+    from rdist_tensor_gb300 import synthetic
+
+    dims = (60, 50, 40)
+    _, nz_idx, nz_vals, _ = synthetic.poisson_counts(dims, 20_000, rank=4, seed=9)
+    model = gcp.GCP(nz_idx, nz_vals, dims, rank=4, loss="poisson", seed=0)
+    idx_all = torch.as_tensor(_all_entries(dims), device="cuda")
+    X = torch.zeros(dims, dtype=torch.float32, device="cuda")
+    X[tuple(torch.as_tensor(nz_idx.astype(np.int64), device="cuda").T)] = torch.as_tensor(nz_vals, device="cuda")
+    x_all = X.reshape(-1)
+    ones = torch.ones_like(x_all)
+
+    def full():
+        with torch.no_grad():
+            return model.objective(idx_all, x_all, ones).item()
+
+    f0 = full()
+    model.fit(200, J_nz=4096, J_z=4096, lr=2e-2)
+    f1 = full()
+    assert np.isfinite(f1) and f1 < 0.9 * f0, (f0, f1)
