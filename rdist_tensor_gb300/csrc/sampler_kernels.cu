@@ -337,7 +337,10 @@ int sts_compute_M(Session& s, int n, cudaStream_t st) {
     EXAFAC_CHECK_LAUNCH();
     const int first = (n == 0) ? 1 : 0;
     EXAFAC_TRY(launch_syev(R, s.chain + (int64_t)first * R2, 0, 1, s.eigV, s.eigL, 0, nullptr, 0.0, s.vt, st));
-    sts_phi_kernel<<<1, 256, sizeof(double) * R2, st>>>(N, n, R, s.eigV, s.eigL, s.chain, s.Emat, s.Phi, s.PhiP); count_launch();
+    const size_t phi_smem = sizeof(double) * R2;
+    if (phi_smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(sts_phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)phi_smem));
+    sts_phi_kernel<<<1, 256, phi_smem, st>>>(N, n, R, s.eigV, s.eigL, s.chain, s.Emat, s.Phi, s.PhiP); count_launch();
     EXAFAC_CHECK_LAUNCH();
     if (N > 1) {
         // matrices 1..N-1 (chain[n] was cleared, its decomposition is trivial)

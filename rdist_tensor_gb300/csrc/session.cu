@@ -129,7 +129,6 @@ static int plan(const exafac_als_config* cfg, Session& s) {
     EXAFAC_ARG(cfg->precision == EXAFAC_PREC_FP64 || cfg->precision == EXAFAC_PREC_TF32 ||
                    cfg->precision == EXAFAC_PREC_BF16,
                "precision must be FP64, TF32 or BF16");
-    EXAFAC_ARG(cfg->precision == EXAFAC_PREC_FP64 || cfg->R <= 32, "the mixed forms support R <= 32 in this build");
     EXAFAC_ARG(cfg->preprocessing >= 0 && cfg->preprocessing <= 2, "bad preprocessing");
     s.cfg = *cfg;
     s.N = cfg->N;

@@ -1,7 +1,7 @@
 // Kernels of one sampled-ALS step after the draw (accumulator_stationary.hpp:
 // 173-294 at one rank): deduplication, design rows + Gram, fiber lookup,
-// counting sort of the hits by output row, sampled MTTKRP fused with the
-// R x R solve, column renormalisation; plus the exact fit and exact MTTKRP.
+// sampled MTTKRP + R x R solve for R > 32, column renormalisation; plus the
+// exact fit.
 #include <cuda_bf16.h>
 
 #include "dense.cuh"
@@ -342,15 +342,149 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
     for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
 }
 
+// R > 32 (padded to RP = 64 or 128): the block's 8 warps share one 32-row
+// tile (warp w builds rows 4w..4w+3, FP64 row products, D' = d w in FP64 for
+// the FP64 MTTKRP), and split the lower-triangle 16 x 8 MMA blocks of the
+// RP x RP Gram between them; each Gram entry has one owner, so the block sum
+// needs no ordering.
+template <int kRound, int RP>
+__global__ void __launch_bounds__(kDesignWarps * 32) design_mma_wide_kernel(int N, int n, int R,
+                                                                            const int64_t* __restrict__ ju_dev,
+                                                                            const uint32_t* __restrict__ sd,
+                                                                            const double* __restrict__ wd,
+                                                                            FactorPtrs f, double* __restrict__ D,
+                                                                            double* __restrict__ part) {
+    constexpr int kStride = RP + 8;  // row stride mod 32 == 8: conflict-free fragment loads
+    constexpr int kMT = RP / 16;
+    constexpr int kPairs = kMT * (kMT + 1);  // m-tile mt pairs with n-tiles 0 .. 2 mt + 1
+    constexpr int kPerWarp = (kPairs + kDesignWarps - 1) / kDesignWarps;
+    constexpr int kCB = RP / 32;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    float (*t)[kStride] = reinterpret_cast<float (*)[kStride]>(dyn);
+    double* red = reinterpret_cast<double*>(dyn + sizeof(float) * 32 * kStride);
+    const int P = R * (R + 1) / 2;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gid = lane >> 2, tig = lane & 3;
+    for (int e = threadIdx.x; e < P; e += blockDim.x) red[e] = 0.0;
+    int pm[kPerWarp], pn[kPerWarp];
+#pragma unroll
+    for (int q = 0; q < kPerWarp; q++) {
+        const int p = w + kDesignWarps * q;
+        int mt = 0, rem = p;
+        while (mt < kMT && rem >= 2 * (mt + 1)) {
+            rem -= 2 * (mt + 1);
+            mt++;
+        }
+        pm[q] = p < kPairs ? mt : -1;
+        pn[q] = rem;
+    }
+    double gacc[kPerWarp][4];
+#pragma unroll
+    for (int q = 0; q < kPerWarp; q++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) gacc[q][i] = 0.0;
+    __syncthreads();
+    const int64_t ju = *ju_dev;
+    for (int64_t base = (int64_t)blockIdx.x * 32; base < ju; base += (int64_t)gridDim.x * 32) {
+        const int nrow = (int)min((int64_t)32, ju - base);
+        for (int rr = 0; rr < 4; rr++) {
+            const int r = 4 * w + rr;
+            const int64_t j = base + r;
+            double d[kCB];
+#pragma unroll
+            for (int cb = 0; cb < kCB; cb++) d[cb] = 1.0;
+            double wj = 0.0;
+            if (r < nrow) {
+                wj = wd[j];
+                for (int k = 0; k < N; k++) {
+                    if (k == n) continue;
+                    const int64_t i = sd[j * N + k];
+#pragma unroll
+                    for (int cb = 0; cb < kCB; cb++) {
+                        const int c = lane + 32 * cb;
+                        if (c < R) d[cb] *= f.U[k][i * R + c];
+                    }
+                }
+            }
+            const double sw = sqrt(wj);
+#pragma unroll
+            for (int cb = 0; cb < kCB; cb++) {
+                const int c = lane + 32 * cb;
+                float v = 0.0f;
+                if (r < nrow && c < R) {
+                    const double x = d[cb] * sw;
+                    D[j * R + c] = x * sw;
+                    v = kRound == 1 ? round_tf32((float)x) : round_bf16((float)x);
+                }
+                t[r][c] = v;
+            }
+        }
+        __syncthreads();
+        float c[kPerWarp][4];
+#pragma unroll
+        for (int q = 0; q < kPerWarp; q++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) c[q][i] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+            const int k0 = ks * 8 + tig;
+#pragma unroll
+            for (int q = 0; q < kPerWarp; q++) {
+                if (pm[q] < 0) continue;
+                const int m0 = 16 * pm[q], n0 = 8 * pn[q];
+                const uint32_t a[4] = {__float_as_uint(t[k0][m0 + gid]), __float_as_uint(t[k0][m0 + gid + 8]),
+                                       __float_as_uint(t[k0 + 4][m0 + gid]), __float_as_uint(t[k0 + 4][m0 + gid + 8])};
+                const uint32_t b[2] = {__float_as_uint(t[k0][n0 + gid]), __float_as_uint(t[k0 + 4][n0 + gid])};
+                mma_tf32_16x8x8(c[q], a, b);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kPerWarp; q++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) gacc[q][i] += (double)c[q][i];
+        __syncthreads();  // the next tile overwrites t
+    }
+#pragma unroll
+    for (int q = 0; q < kPerWarp; q++) {
+        if (pm[q] < 0) continue;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int row = 16 * pm[q] + gid + 8 * (i >> 1);
+            const int col = 8 * pn[q] + 2 * tig + (i & 1);
+            if (row < R && col <= row) red[packed_index(R, col, row)] = gacc[q][i];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
+}
+
+template <int kRound, int RP>
+static int launch_design_wide(Session& s, int n, cudaStream_t st) {
+    const size_t smem = sizeof(float) * 32 * (RP + 8) + sizeof(double) * packed_size(RP);
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(design_mma_wide_kernel<kRound, RP>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    design_mma_wide_kernel<kRound, RP><<<kDesignBlocks, kDesignWarps * 32, smem, st>>>(
+        s.N, n, s.R, s.counters + 0, s.sd, s.wd, factor_ptrs(s), s.D, s.part);
+    count_launch();
+    return EXAFAC_OK;
+}
+
 int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
     const int R = s.R;
     int64_t nblk = std::max<int64_t>(1, ceil_div(J, kGramRows));
     if (s.cfg.precision != EXAFAC_PREC_FP64) {
-        if (R > 32) {
-            set_error("mixed precision supports R <= 32 in this build");
-            return EXAFAC_ERR_UNSUPPORTED;
+        const bool tf32 = s.cfg.precision == EXAFAC_PREC_TF32;
+        if (R > 32) {  // FP64 design rows for the FP64 MTTKRP, tensor-core Gram
+            int rc;
+            if (R <= 64) rc = tf32 ? launch_design_wide<1, 64>(s, n, st) : launch_design_wide<2, 64>(s, n, st);
+            else rc = tf32 ? launch_design_wide<1, 128>(s, n, st) : launch_design_wide<2, 128>(s, n, st);
+            EXAFAC_TRY(rc);
+            gram_reduce_kernel<<<packed_size(R), 256, 0, st>>>(s.part, kDesignBlocks, R, s.dgram); count_launch();
+            EXAFAC_CHECK_LAUNCH();
+            return EXAFAC_OK;
         }
-        if (s.cfg.precision == EXAFAC_PREC_TF32)
+        if (tf32)
             design_mma_kernel<1><<<kDesignBlocks, kDesignWarps * 32, 0, st>>>(s.N, n, R, s.counters + 0, s.sd, s.wd,
                                                                                factor_ptrs(s), s.Df, s.part);
         else

@@ -256,18 +256,20 @@ def make_optimizer_prec(dims, idx, vals, factors, sampler, J_max, precision):
     return opt, lr
 
 
+@pytest.mark.parametrize("R", [16, 48, 100])
 @pytest.mark.parametrize("precision", ["tf32", "bf16"])
 @pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
-def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler):
+def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler, R):
     """First step of the mixed forms (same samples as FP64: the initial
-    sampler state is FP64) against the oracle.  The MTTKRP is accumulated in
-    FP32 from FP32 design rows (relative error ~1e-6); the factor also passes
-    through Phi, the pseudo-inverse of a Gram formed from TF32 (10-bit) or
-    BF16 (7-bit mantissa) products: factor within 1e-3 (TF32) / 2e-2 (BF16)."""
+    sampler state is FP64) against the oracle.  R <= 32: the MTTKRP is
+    accumulated in FP32 from FP32 design rows (relative error ~1e-6); R > 32:
+    FP64 design rows and MTTKRP.  The factor also passes through Phi, the
+    pseudo-inverse of a Gram formed on the tensor cores from TF32 (10-bit) or
+    BF16 (7-bit mantissa) inputs: factor within 1e-3 (TF32) / 2e-2 (BF16)."""
     from rdist_tensor_gb300 import synthetic
 
     dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
-    R, J = 16, 8192
+    J = 8192
     factors = synthetic.gaussian_factors(dims, R, seed=5)
     opt, lr = make_optimizer_prec(dims, idx, vals, factors, sampler, J, precision)
     ora = oracle_mod.OracleALS(dims, idx, vals, factors, sampler)
@@ -280,7 +282,7 @@ def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler):
     tol = 1e-3 if precision == "tf32" else 2e-2
     err_u = rel_err(lr.factors[0].data.cpu().numpy(), out["factor"])
     err_s = rel_err(lr.sigma.cpu().numpy(), out["sigma"])
-    print(f"{precision} {sampler}: factor {err_u:.2e} sigma {err_s:.2e}")
+    print(f"{precision} {sampler} R={R}: factor {err_u:.2e} sigma {err_s:.2e}")
     assert err_u < tol and err_s < tol
     opt.deinitialize()
 
