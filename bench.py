@@ -107,6 +107,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes (read + write) of the sampled-MTTKRP region per sweep, summed over its
+# kernels from one ncu capture of this bench on the same workload and form (the
+# capture and its command: profiles/sweep_launches_zipf4_1e8_{tf32,fp64}.md).  The
+# bench cannot run ncu itself; other workloads and forms report null.
+REGION_TRAFFIC = {("zipf4", "tf32"): 2.0695e9, ("zipf4", "fp64"): 3.0576e9}
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -313,7 +320,8 @@ def run_gpu(args, w):
     peak, peak_kind = measured_peaks()
     achieved = tot_bytes / spmm_s / 1e9 if spmm_s > 0 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": REGION_TRAFFIC.get((args.workload, args.precision)),
                 "kernel": "sampled MTTKRP region (lookup, hit sort, scatter + solve), per sweep",
                 "algorithmic_bytes": tot_bytes, "duration_s": spmm_s, "peak_source": peak_kind,
                 "regions_s": {k: v for k, v in zip(["leverage_sampling", "row_gather", "design_matrix_prep",
