@@ -201,6 +201,16 @@ int exafac_als_set_seed(exafac_als_t s, uint64_t seed);
 int exafac_als_enable_timing(exafac_als_t s, int32_t enable);
 int exafac_als_region_times(exafac_als_t s, double* out7);
 
+/* `count` sweeps (steps 0..N-1 each; round loop of als_optimizer.hpp:40-124
+ * without its timers) at J samples per step.  uniforms_dev: null for the
+ * session's Philox stream, or N per-step blocks laid out as for
+ * exafac_als_step, read again on every sweep.  After any factor has had a
+ * sampled update, one sweep is captured into a CUDA graph on an internal
+ * stream and replayed (the capture is kept for the same J and uniforms
+ * pointer, and dropped by exafac_als_init / exafac_als_set_seed); results are
+ * those of calling exafac_als_step N x count times.  Region timing must be off. */
+int exafac_als_sweeps(exafac_als_t s, int64_t J, int32_t count, const double* uniforms_dev, void* stream);
+
 /* Copies the last step's counters to the host (synchronises). */
 int exafac_als_step_info(exafac_als_t s, exafac_step_info* out, void* stream);
 

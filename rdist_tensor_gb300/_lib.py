@@ -65,6 +65,7 @@ SIGNATURES = {
     "exafac_als_draw": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P]),
     "exafac_als_step": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P]),
     "exafac_als_exact_step": (ctypes.c_int, [_P, _I32, _P]),
+    "exafac_als_sweeps": (ctypes.c_int, [_P, _I64, _I32, _P, _P]),
     "exafac_als_sampled_mttkrp": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P]),
     "exafac_als_fit": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
     "exafac_als_set_seed": (ctypes.c_int, [_P, ctypes.c_uint64]),

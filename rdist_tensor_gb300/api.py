@@ -321,6 +321,22 @@ class ALS_Optimizer:
         _lib.call("exafac_als_step", self._h, int(mode), int(J), _ptr(uniforms) if uniforms is not None else None,
                   _ptr(perms) if perms is not None else None, _stream())
 
+    def execute_sweeps(self, num_sweeps: int, J: int, uniforms: torch.Tensor | None = None):
+        """num_sweeps sweeps (modes 0..N-1) without per-region timers, replayed
+        from one captured CUDA graph once every factor has had a sampled
+        update.  uniforms: None for the session's Philox stream, or a device
+        tensor of N per-step blocks (as execute_ALS_step takes), read on every
+        sweep (refill it in place between calls)."""
+        self._require()
+        if J > self.max_samples:
+            self.max_samples = int(J)
+            self._create(self.max_samples)
+        if self.timing:
+            _lib.call("exafac_als_enable_timing", self._h, 0)
+            self.timing = False
+        _lib.call("exafac_als_sweeps", self._h, int(J), int(num_sweeps),
+                  _ptr(uniforms) if uniforms is not None else None, _stream())
+
     def execute_ALS_rounds(self, num_rounds: int, J: int, epoch_interval: int):
         """als_optimizer.hpp:40-124; timers are CUDA events on the GPU."""
         self._require()

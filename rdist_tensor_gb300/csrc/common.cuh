@@ -18,8 +18,10 @@ constexpr int kMaxRank = 128;
 // Last-error text for the C-ABI (thread-local).
 void set_error(const std::string& msg);
 
-// Kernel launches issued by the library since load (exafac_kernel_launches).
+// Kernel launches issued by the library since load (exafac_kernel_launches);
+// a replayed graph adds the launches it holds.
 void count_launch();
+void add_launches(long long n);
 
 #define EXAFAC_CUDA_TRY(expr)                                                                     \
     do {                                                                                          \

@@ -19,6 +19,7 @@ namespace exafac {
 constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr int64_t kExactCdfMax = 16384;  // CDFs up to this length are summed strictly in order
 constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a power of two)
+constexpr int kRngSlot = 15;              // counters[] slot of the session's Philox counter
 
 struct Slot1 {
     unsigned long long key;
@@ -94,7 +95,7 @@ struct Session {
     int64_t* pos = nullptr;
     uint32_t* sd = nullptr;
     double* wd = nullptr;
-    int64_t* counters = nullptr;  // [0] J_u, [1] H, [2] touched, [3..] scratch
+    int64_t* counters = nullptr;  // [0] J_u, [1] H, [2] touched, [3..] scratch, [kRngSlot] Philox counter
     double* D = nullptr;          // Jmax x R design rows (scaled twice)
     double* part = nullptr;       // Gram partials
     int64_t part_rows = 0;
@@ -137,8 +138,7 @@ struct Session {
     uint32_t* rowbits = nullptr;    // ceil(Imax / 32): rows touched by the current step
     float* Df = nullptr;          // Jmax x R design rows (mixed forms)
 
-    uint64_t seed = 0x5eed;
-    uint64_t counter = 0;
+    uint64_t seed = 0x5eed;  // Philox key; the stream counter is counters[kRngSlot] on the device
 };
 
 // ---- sampler kernels (sampler_kernels.cu)

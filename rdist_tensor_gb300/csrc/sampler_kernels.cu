@@ -7,20 +7,28 @@
 
 namespace exafac {
 
-__global__ void philox_uniform_kernel(double* out, int64_t count, uint64_t seed, uint64_t ctr) {
+// The stream counter lives in device memory (counters[kRngSlot]) and advances
+// by one per call in a one-thread kernel, so a captured and replayed sweep
+// draws fresh uniforms on every replay.
+__global__ void philox_uniform_kernel(double* out, int64_t count, uint64_t seed, const int64_t* __restrict__ ctr_dev) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t i = 2 * t;
     if (i >= count) return;
+    const uint64_t ctr = (uint64_t)*ctr_dev;
     uint4 c = make_uint4((unsigned)t, (unsigned)(t >> 32), (unsigned)ctr, (unsigned)(ctr >> 32));
     uint4 r = philox4x32_10(c, make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
     out[i] = u53(r.x, r.y);
     if (i + 1 < count) out[i + 1] = u53(r.z, r.w);
 }
 
+__global__ void philox_advance_kernel(int64_t* ctr_dev) { *ctr_dev += 1; }
+
 int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st) {
     if (count <= 0) return EXAFAC_OK;
     int64_t threads = (count + 1) / 2;
-    philox_uniform_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(out, count, s.seed, s.counter++); count_launch();
+    int64_t* ctr = s.counters + kRngSlot;
+    philox_uniform_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(out, count, s.seed, ctr); count_launch();
+    philox_advance_kernel<<<1, 1, 0, st>>>(ctr); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

@@ -21,6 +21,7 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 static int64_t next_pow2(int64_t x) {
     int64_t p = 1;
@@ -225,12 +226,23 @@ struct exafac_als_s {
     // lookup and the hit sort (fork / join events on the caller's stream).
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // One captured sweep (exafac_als_sweeps), keyed by J and the uniforms
+    // pointer it was captured with, and the kernels it launches.
+    cudaStream_t cap = nullptr;
+    cudaEvent_t cap_ev = nullptr;
+    cudaGraphExec_t sweep_exec = nullptr;
+    int64_t sweep_J = -1;
+    const double* sweep_uni = nullptr;
+    long long sweep_launches = 0;
     ~exafac_als_s() {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         if (side) cudaStreamDestroy(side);
+        if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
+        if (cap_ev) cudaEventDestroy(cap_ev);
+        if (cap) cudaStreamDestroy(cap);
     }
 };
 
@@ -317,7 +329,12 @@ extern "C" int exafac_als_destroy(exafac_als_t h) {
 extern "C" int exafac_als_set_seed(exafac_als_t h, uint64_t seed) {
     EXAFAC_ARG(h != nullptr, "null session");
     h->s.seed = seed;
-    h->s.counter = 0;
+    if (h->sweep_exec) {  // the captured sweep holds the old key
+        cudaGraphExecDestroy(h->sweep_exec);
+        h->sweep_exec = nullptr;
+    }
+    if (h->s.counters)  // restart the stream (synchronous; a set-up call)
+        EXAFAC_CUDA_TRY(cudaMemset(h->s.counters + kRngSlot, 0, sizeof(int64_t)));
     return EXAFAC_OK;
 }
 
@@ -325,6 +342,10 @@ extern "C" int exafac_als_init(exafac_als_t h, const uint32_t* idx, const double
                                void* setup, size_t setup_sz, double* tensor_norm, void* stream) {
     EXAFAC_ARG(h && idx && vals && F && setup, "null argument");
     Session& s = h->s;
+    if (h->sweep_exec) {  // the captured sweep holds the previous factor pointers
+        cudaGraphExecDestroy(h->sweep_exec);
+        h->sweep_exec = nullptr;
+    }
     cudaStream_t st = (cudaStream_t)stream;
     for (int k = 0; k < s.N; k++) EXAFAC_ARG(F->U[k] != nullptr, "null factor matrix");
     EXAFAC_ARG(F->sigma != nullptr, "null sigma");
@@ -427,6 +448,76 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
             EXAFAC_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]));
             h->region[map[i]] += ms * 1e-3;
         }
+    }
+    return EXAFAC_OK;
+}
+
+// One sweep: steps 0..N-1; explicit uniforms are N per-step blocks.
+static int run_sweep(exafac_als_s* h, int64_t J, const double* uni, cudaStream_t st) {
+    const Session& s = h->s;
+    const int64_t per_step = (int64_t)s.N * (s.cfg.sampler == EXAFAC_SAMPLER_STS_CP ? 2 : 1) * J;
+    for (int n = 0; n < s.N; n++) EXAFAC_TRY(exafac_als_step(h, n, J, uni ? uni + n * per_step : nullptr, nullptr, st));
+    return EXAFAC_OK;
+}
+
+static bool any_dense(const Session& s) {
+    for (int k = 0; k < s.N; k++)
+        if (s.dense[k]) return true;
+    return false;
+}
+
+// Captures one steady-state sweep into s->sweep_exec on the internal stream
+// (ordered after the work already queued on st).
+static int capture_sweep(exafac_als_s* h, int64_t J, const double* uni, cudaStream_t st) {
+    if (h->sweep_exec) {
+        cudaGraphExecDestroy(h->sweep_exec);
+        h->sweep_exec = nullptr;
+    }
+    if (!h->cap) {
+        EXAFAC_CUDA_TRY(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+        EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->cap_ev, cudaEventDisableTiming));
+    }
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->cap_ev, st));
+    EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->cap, h->cap_ev, 0));
+    const long long l0 = exafac_kernel_launches();
+    EXAFAC_CUDA_TRY(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeRelaxed));
+    const int rc = run_sweep(h, J, uni, h->cap);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->cap, &graph);
+    h->sweep_launches = exafac_kernel_launches() - l0;
+    add_launches(-h->sweep_launches);  // recorded, not launched
+    if (rc != EXAFAC_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    EXAFAC_CUDA_TRY(e);
+    const cudaError_t ei = cudaGraphInstantiate(&h->sweep_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    EXAFAC_CUDA_TRY(ei);
+    h->sweep_J = J;
+    h->sweep_uni = uni;
+    return EXAFAC_OK;
+}
+
+extern "C" int exafac_als_sweeps(exafac_als_t h, int64_t J, int32_t count, const double* uni, void* stream) {
+    EXAFAC_ARG(h && h->s.initialized, "session not initialised");
+    Session& s = h->s;
+    EXAFAC_ARG(J >= 1 && J <= s.Jmax, "J out of range");
+    EXAFAC_ARG(count >= 0, "count must be >= 0");
+    EXAFAC_ARG(!h->timing, "exafac_als_sweeps: region timing is on (it reads events after every step)");
+    cudaStream_t st = (cudaStream_t)stream;
+    int done = 0;
+    // A factor that no sampled step has updated yet is cleared whole by its
+    // next update, a different launch sequence: run plain sweeps until none is.
+    while (done < count && any_dense(s)) {
+        EXAFAC_TRY(run_sweep(h, J, uni, st));
+        done++;
+    }
+    if (done == count) return EXAFAC_OK;
+    if (!h->sweep_exec || h->sweep_J != J || h->sweep_uni != uni) EXAFAC_TRY(capture_sweep(h, J, uni, st));
+    for (; done < count; done++) {
+        EXAFAC_CUDA_TRY(cudaGraphLaunch(h->sweep_exec, st));
+        add_launches(h->sweep_launches);
     }
     return EXAFAC_OK;
 }

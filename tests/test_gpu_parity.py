@@ -308,3 +308,61 @@ def test_mixed_equal_fit(lib, precision, sampler):
         opt.deinitialize()
     assert fits["fp64"] > 0.5, fits
     assert abs(fits[precision] - fits["fp64"]) < 1e-3, fits
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32"])
+@pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
+def test_sessions_repeat_bitwise(lib, precision, sampler):
+    """Two sessions on the same input, stepped alike, stay bitwise equal:
+    every reduction on the path has a fixed order."""
+    from rdist_tensor_gb300 import synthetic
+
+    dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
+    factors = synthetic.gaussian_factors(dims, 16, seed=5)
+    a, la = make_optimizer_prec(dims, idx, vals, factors, sampler, 4096, precision)
+    b, lb = make_optimizer_prec(dims, idx, vals, factors, sampler, 4096, precision)
+    for _ in range(3):
+        for n in range(3):
+            a.execute_ALS_step(n, 4096)
+            b.execute_ALS_step(n, 4096)
+    for k in range(3):
+        assert torch.equal(la.factors[k].data, lb.factors[k].data), k
+    assert torch.equal(la.sigma, lb.sigma)
+    a.deinitialize()
+    b.deinitialize()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32"])
+@pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
+def test_graph_sweeps_match_steps(lib, precision, sampler):
+    """execute_sweeps (a captured sweep replayed as a CUDA graph) gives the
+    same factors, bit for bit, as the same sweeps run step by step: with the
+    session's Philox stream, and with explicit uniforms refilled in place."""
+    from rdist_tensor_gb300 import synthetic
+
+    dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
+    factors = synthetic.gaussian_factors(dims, 16, seed=5)
+    J = 4096
+    a, la = make_optimizer_prec(dims, idx, vals, factors, sampler, J, precision)
+    b, lb = make_optimizer_prec(dims, idx, vals, factors, sampler, J, precision)
+    a.execute_sweeps(4, J)
+    for _ in range(4):
+        for n in range(3):
+            b.execute_ALS_step(n, J)
+    for k in range(3):
+        assert torch.equal(la.factors[k].data, lb.factors[k].data), k
+    per_step = 3 * (2 if sampler == "sts_cp" else 1) * J
+    buf = torch.empty(3 * per_step, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(8)
+    for _ in range(3):
+        u = dev(rng.random(3 * per_step), torch.float64)
+        buf.copy_(u)
+        a.execute_sweeps(1, J, buf)
+        for n in range(3):
+            b.execute_ALS_step(n, J, u[n * per_step:(n + 1) * per_step])
+    for k in range(3):
+        assert torch.equal(la.factors[k].data, lb.factors[k].data), k
+    assert torch.equal(la.sigma, lb.sigma)
+    assert a.compute_exact_fit() == b.compute_exact_fit()
+    a.deinitialize()
+    b.deinitialize()
