@@ -61,7 +61,8 @@ struct Session {
     // CP-ARLS-LEV state
     double* scores[kMaxModes] = {nullptr};
     double* cdf[kMaxModes] = {nullptr};
-    uint32_t* guide[kMaxModes] = {nullptr};  // kGuideBuckets + 1: guide[b] = lower_bound(cdf, b / kGuideBuckets)
+    uint32_t* guide[kMaxModes] = {nullptr};
+    bool cdf_compact[kMaxModes] = {false};  // CDF over nzrows[k] (a sampled update) rather than all rows  // kGuideBuckets + 1: guide[b] = lower_bound(cdf, b / kGuideBuckets)
     double* cdf_total = nullptr;  // [N] sum of the scores (log-weight numerator)
     // STS-CP state
     TreeShape rtree[kMaxModes];
@@ -143,7 +144,7 @@ struct Session {
 
 // ---- sampler kernels (sampler_kernels.cu)
 int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st);
-int arls_build_cdf(Session& s, int k, cudaStream_t st);
+int arls_build_cdf(Session& s, int k, const uint32_t* list, const int64_t* count_dev, cudaStream_t st);
 int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStream_t st);
 int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* perms, cudaStream_t st);
 int sts_compute_M(Session& s, int n, cudaStream_t st);

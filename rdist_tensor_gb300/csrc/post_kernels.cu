@@ -109,10 +109,11 @@ __global__ void __launch_bounds__(256) segreduce_kernel(int R, const int64_t* __
 // Crossing rows, one warp per chunk c0 whose last row continues: the row's
 // carries carry_last[c0] + sum over c in (c0, c1] of carry_first[c], c1 the
 // last chunk that starts inside the row (the chunks that do form a prefix of
-// c0+1, c0+2, ..., found 32 at a time by ballot).  Lane l sums chunks
-// c0+1+l, c0+1+l+32, ... over all 32 padded columns, then a butterfly
-// reduce-scatter leaves column l's total in lane l (a fixed order, so results
-// are reproducible run to run).
+// c0+1, c0+2, ..., found 32 at a time by ballot).  Spans of up to 32 chunks
+// (almost every row): lane = column, chunks summed in order.  Longer spans
+// (the hot rows): lane l sums chunks c0+1+l, c0+1+l+32, ... over all 32 padded
+// columns, then a butterfly reduce-scatter leaves column l's total in lane l.
+// Both orders are fixed, so results are reproducible run to run.
 // carry_seg != null: Mc is compact and the row's output index is carry_seg[c0].
 template <typename TA, int kChunk, int CB = 1>  // CB column blocks of 32 (carry stride 32 CB)
 __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64_t* __restrict__ counters, int64_t cap,
@@ -138,6 +139,17 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
             c1 = b + __popc(bal) - 1;
             if (bal != full) break;
         }
+        const int64_t out = carry_seg ? (int64_t)carry_seg[c0] : (int64_t)row;
+        if (c1 - c0 <= 32) {  // short span: column per lane, chunks in order
+            for (int cb = 0; cb < CB; cb++) {
+                const int col = 32 * cb + lane;
+                if (col >= R) continue;
+                TA v = carry_last[c0 * (32 * CB) + col];
+                for (int64_t m = c0 + 1; m <= c1; m++) v += carry_first[m * (32 * CB) + col];
+                Mc[out * ldm + col] = v;
+            }
+            continue;
+        }
         for (int cb = 0; cb < CB; cb++) {
             TA acc[32];
 #pragma unroll
@@ -158,7 +170,6 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
                 }
             }
             const int col = 32 * cb + lane;
-            const int64_t out = carry_seg ? (int64_t)carry_seg[c0] : (int64_t)row;
             if (col < R) Mc[out * ldm + col] = carry_last[c0 * (32 * CB) + col] + acc[0];
         }
     }
@@ -775,13 +786,33 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
             for (int r = 0; r < 32; r++)
                 if (lane < KC) t[r][lane] = v[r];
         }
+        __syncwarp();
+        const uint32_t row0 = __shfl_sync(0xffffffffu, myrow, 0);
+        const uint32_t row31 = __shfl_sync(0xffffffffu, myrow, 31);
+        if (nrow == 32 && row31 - row0 == 31) {
+            // 32 consecutive rows: one contiguous block of 32 R doubles, written
+            // with full-width stores (lane l: elements l, l + 32, ...)
+            double* blk = U + (int64_t)row0 * R;
+            int r = lane / R, c = lane % R;
+            for (int e = lane; e < 32 * R; e += 32) {
+                const double y = (double)t[r][c] * (deg ? 1.0 : sg[c]);
+                blk[e] = y;
+                t[r][c] = (float)y;
+                c += 32;
+                while (c >= R) {
+                    c -= R;
+                    r++;
+                }
+            }
+        } else {
 #pragma unroll 4
-        for (int r = 0; r < nrow; r++) {  // normalised FP64 rows to the factor, one row per store
-            const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
-            if (lane < KC) {
-                const double y = (double)t[r][lane] * sgl;
-                if (lane < R) U[row * R + lane] = y;
-                t[r][lane] = (float)y;
+            for (int r = 0; r < nrow; r++) {  // normalised FP64 rows to the factor, one row per store
+                const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
+                if (lane < KC) {
+                    const double y = (double)t[r][lane] * sgl;
+                    if (lane < R) U[row * R + lane] = y;
+                    t[r][lane] = (float)y;
+                }
             }
         }
         __syncwarp();

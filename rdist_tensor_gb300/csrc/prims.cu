@@ -55,14 +55,18 @@ __device__ T block_exclusive_scan(T v, T* red, T* total) {
     return out;
 }
 
+// Optional forms: element g is in[gather[g]] when gather is given, and the
+// length is min(n, *n_dev) when n_dev is given (n sizes the grid).
 template <typename Tin, typename Tacc>
-__global__ void scan_block_sums(const Tin* __restrict__ in, int64_t n, Tacc* __restrict__ partial) {
+__global__ void scan_block_sums(const Tin* __restrict__ in, int64_t n, Tacc* __restrict__ partial,
+                                const uint32_t* __restrict__ gather = nullptr, const int64_t* n_dev = nullptr) {
     __shared__ Tacc red[33];
+    if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     Tacc acc = 0;
     for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
         int64_t g = base + i;
-        if (g < n) acc += (Tacc)in[g];
+        if (g < n) acc += (Tacc)in[gather ? (int64_t)gather[g] : g];
     }
     Tacc s = block_reduce_sum(acc, red);
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
@@ -91,13 +95,16 @@ __device__ __forceinline__ int scan_pad(int i) { return i + (i >> 4); }
 
 template <typename Tin, typename Tacc, bool kInclusive, bool kNormalize = false>
 __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, int64_t n,
-                           const Tacc* __restrict__ partial, const Tacc* __restrict__ total = nullptr) {
+                           const Tacc* __restrict__ partial, const Tacc* __restrict__ total = nullptr,
+                           const uint32_t* __restrict__ gather = nullptr, const int64_t* n_dev = nullptr) {
     __shared__ Tacc tile[kScanTile + kScanTile / 16];
     __shared__ Tacc red[33];
+    if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    if (base >= n) return;  // uniform per block
     for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
         int64_t g = base + i;
-        tile[scan_pad(i)] = g < n ? (Tacc)in[g] : Tacc(0);
+        tile[scan_pad(i)] = g < n ? (Tacc)in[gather ? (int64_t)gather[g] : g] : Tacc(0);
     }
     __syncthreads();
     Tacc loc[kScanItems];
@@ -161,13 +168,16 @@ int scan_exclusive_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, int64
 int scan_inclusive_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s) {
     return scan_impl<double, double, true>(in, out, n, total, scratch, s);
 }
-int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s) {
+int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s,
+                 const uint32_t* gather, const int64_t* n_dev) {
     if (n <= 0) return EXAFAC_OK;
     int64_t nb = ceil_div(n, kScanTile);
     double* partial = reinterpret_cast<double*>(scratch);
-    scan_block_sums<double, double><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial); count_launch();
+    scan_block_sums<double, double><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial, gather, n_dev);
+    count_launch();
     scan_partials_kernel<double><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
-    scan_apply<double, double, true, true><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, total);
+    scan_apply<double, double, true, true><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, total, gather,
+                                                                                   n_dev);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

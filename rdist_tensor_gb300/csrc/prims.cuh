@@ -20,7 +20,10 @@ int scan_inclusive_f64(const double* in, double* out, int64_t n, double* total, 
 
 // Discrete CDF of nonnegative weights: out_i = S_i / S_{n-1} with S the
 // blockwise inclusive scan, out_{n-1} = 1; *total (device) = S_{n-1}.
-int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s);
+// gather (optional): weight i is in[gather[i]]; n_dev (optional): the length
+// is min(n, *n_dev), n only sizes the launch.
+int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s,
+                 const uint32_t* gather = nullptr, const int64_t* n_dev = nullptr);
 
 // Stable LSD radix sort of `count` keys (kw = 1: 64-bit keys in lo; kw = 2:
 // 128-bit (lo, hi)) over their low `bits` bits, carrying a uint32 payload.

@@ -43,10 +43,16 @@ int gen_uniforms(Session& s, double* out, int64_t count, cudaStream_t st) {
 // The weights are staged in shared memory (n <= kExactCdfMax) so the two
 // serial loops run on shared-memory latency.
 __global__ void cdf_sequential_kernel(const double* __restrict__ w, int64_t n, double* __restrict__ cdf,
-                                      double* __restrict__ total) {
+                                      double* __restrict__ total, const uint32_t* __restrict__ gather,
+                                      const int64_t* __restrict__ n_dev) {
     extern __shared__ double sh[];
     __shared__ double sum_sh;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) sh[i] = w[i];
+    if (n_dev) n = min(n, *n_dev);
+    if (n < 1) {
+        if (threadIdx.x == 0) *total = 0.0;
+        return;
+    }
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) sh[i] = w[gather ? (int64_t)gather[i] : i];
     __syncthreads();
     if (threadIdx.x == 0) {
         double sum = 0.0;
@@ -78,9 +84,15 @@ __global__ void cdf_sequential_kernel(const double* __restrict__ w, int64_t n, d
 // first entry >= u lies in [guide[b], guide[b+1]], because lower_bound is
 // monotone in u and cdf[guide[b+1]] >= (b+1)/B > u.  B is a power of two, so
 // b/B and floor(u B) are exact.
-__global__ void cdf_guide_kernel(const double* __restrict__ cdf, int64_t n, uint32_t* __restrict__ guide) {
+__global__ void cdf_guide_kernel(const double* __restrict__ cdf, int64_t n, uint32_t* __restrict__ guide,
+                                 const int64_t* __restrict__ n_dev) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > kGuideBuckets) return;
+    if (n_dev) n = min(n, *n_dev);
+    if (n < 1) {
+        guide[b] = 0;
+        return;
+    }
     const double x = (double)b / (double)kGuideBuckets;
     int64_t lo = 0, hi = n;
     while (lo < hi) {
@@ -91,11 +103,19 @@ __global__ void cdf_guide_kernel(const double* __restrict__ cdf, int64_t n, uint
     guide[b] = (uint32_t)(lo < n ? lo : n - 1);
 }
 
-int arls_build_cdf(Session& s, int k, cudaStream_t st) {
+// CDF of mode k's leverage scores.  list == null: over all rows.  Otherwise
+// over the rows in list[0 .. *count_dev) (ascending; the rows whose scores can
+// be nonzero after a sampled update): the partial sums at those rows are the
+// ones the full CDF takes there (the other rows add exactly zero), so a draw
+// lands on the same row; only the final 1.0 sits at the last listed row.
+int arls_build_cdf(Session& s, int k, const uint32_t* list, const int64_t* count_dev, cudaStream_t st) {
     const int64_t n = s.dims[k];
+    s.cdf_compact[k] = list != nullptr;
     if (n < 2) {
         // A one-row distribution always yields row 0 and consumes no draw.
-        cdf_sequential_kernel<<<1, 32, sizeof(double) * n, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k);
+        s.cdf_compact[k] = false;
+        cdf_sequential_kernel<<<1, 32, sizeof(double) * n, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k, nullptr,
+                                                                  nullptr);
         count_launch();
         EXAFAC_CHECK_LAUNCH();
         return EXAFAC_OK;
@@ -105,11 +125,12 @@ int arls_build_cdf(Session& s, int k, cudaStream_t st) {
         if (smem > 48 * 1024)
             EXAFAC_CUDA_TRY(cudaFuncSetAttribute(cdf_sequential_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)smem));
-        cdf_sequential_kernel<<<1, 256, smem, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k); count_launch();
+        cdf_sequential_kernel<<<1, 256, smem, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k, list, count_dev);
+        count_launch();
     } else {
-        EXAFAC_TRY(scan_cdf_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st));
+        EXAFAC_TRY(scan_cdf_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st, list, count_dev));
     }
-    cdf_guide_kernel<<<(unsigned)ceil_div(kGuideBuckets + 1, 256), 256, 0, st>>>(s.cdf[k], n, s.guide[k]);
+    cdf_guide_kernel<<<(unsigned)ceil_div(kGuideBuckets + 1, 256), 256, 0, st>>>(s.cdf[k], n, s.guide[k], count_dev);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
@@ -162,6 +183,8 @@ struct ArlsModes {
     const double* cdf[kMaxModes];
     const double* scores[kMaxModes];
     const uint32_t* guide[kMaxModes];
+    const uint32_t* rowmap[kMaxModes];  // compact CDF: entry -> row (null: entry = row)
+    const int64_t* len[kMaxModes];      // compact CDF: its length on the device
     int64_t dims[kMaxModes];
 };
 
@@ -190,16 +213,24 @@ __global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const dou
         }
         int64_t idx = 0;
         if (I >= 2) {
+            const int64_t L = m.len[k] ? min(I, *m.len[k]) : I;  // CDF entries
             const double u = uni[(int64_t)k * J + src];
-            const double* cdf = m.cdf[k];
-            const int b = min((int)(u * (double)kGuideBuckets), kGuideBuckets - 1);
-            int64_t lo = m.guide[k][b], hi = (int64_t)m.guide[k][b + 1] + 1;
-            while (lo < hi) {
-                int64_t mid = (lo + hi) >> 1;
-                if (cdf[mid] < u) lo = mid + 1;
-                else hi = mid;
+            if (L >= 1) {
+                const double* cdf = m.cdf[k];
+                const int b = min((int)(u * (double)kGuideBuckets), kGuideBuckets - 1);
+                int64_t lo = m.guide[k][b], hi = min((int64_t)m.guide[k][b + 1] + 1, L);
+                while (lo < hi) {
+                    int64_t mid = (lo + hi) >> 1;
+                    if (cdf[mid] < u) lo = mid + 1;
+                    else hi = mid;
+                }
+                idx = lo < L ? lo : L - 1;
+                if (m.rowmap[k]) idx = m.rowmap[k][idx];
+                if (idx >= I) {  // a row list entry out of range: report, take row 0
+                    report(status, EXAFAC_ERR_DEVICE, 7, idx, I);
+                    idx = 0;
+                }
             }
-            idx = lo < I ? lo : I - 1;
         }
         const double lw = 0.0 + (log_total[k] - log(m.scores[k][idx]));
         samples[t * N + k] = (uint32_t)idx;
@@ -215,6 +246,9 @@ int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* p
         m.cdf[k] = k < s.N ? s.cdf[k] : nullptr;
         m.scores[k] = k < s.N ? s.scores[k] : nullptr;
         m.guide[k] = k < s.N ? s.guide[k] : nullptr;
+        const bool compact = k < s.N && s.cdf_compact[k];
+        m.rowmap[k] = compact ? s.nzrows[k] : nullptr;
+        m.len[k] = compact ? s.nzcount + k : nullptr;
         m.dims[k] = k < s.N ? s.dims[k] : 0;
     }
     arls_draw_kernel<<<(unsigned)ceil_div(J, 256), 256, 0, st>>>(s.N, n, J, m, s.cdf_total, uni, perms, s.samples,

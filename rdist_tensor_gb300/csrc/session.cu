@@ -182,7 +182,7 @@ static int refresh_sampler(Session& s, int k, bool all_rows, cudaStream_t st) {
         EXAFAC_TRY(launch_pinv(R, s.ngram, s.upinv, 1e-11, s.vt, st));
         if (all_rows) EXAFAC_CUDA_TRY(cudaMemsetAsync(s.scores[k], 0, sizeof(double) * s.dims[k], st));
         EXAFAC_TRY(arls_leverage(s, k, all_rows, s.upinv, st));
-        EXAFAC_TRY(arls_build_cdf(s, k, st));
+        EXAFAC_TRY(arls_build_cdf(s, k, nullptr, nullptr, st));
     } else {
         EXAFAC_TRY(launch_tree_build(s.rtree[k], R, s.F.U[k], s.treeG[k], st));
     }
@@ -434,7 +434,7 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     // R7: sampler update (CDF of the new scores, or the row tree).
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.gram + (int64_t)n * s.R * s.R, s.ngram, sizeof(double) * s.R * s.R,
                                     cudaMemcpyDeviceToDevice, st));
-    if (arls) EXAFAC_TRY(arls_build_cdf(s, n, st));
+    if (arls) EXAFAC_TRY(arls_build_cdf(s, n, s.touched, s.counters + 2, st));
     else EXAFAC_TRY(launch_tree_build(s.rtree[n], s.R, s.F.U[n], s.treeG[n], st));
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.nzrows[n], s.touched, sizeof(uint32_t) * s.dims[n], cudaMemcpyDeviceToDevice, st));
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.nzcount + n, s.counters + 2, sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
