@@ -128,6 +128,72 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// Conversions between binary32 and binary64 in integer arithmetic.  GB300
+// retires about two FP64 operations (conversions included) per clock per SM
+// against ~116 FP32 ones, so a hardware conversion per element costs more than
+// all the FP32 arithmetic around it.  Both follow IEEE 754 directly: the two
+// formats differ in exponent bias (127 / 1023) and mantissa width (23 / 52).
+//
+// widen_f32: exact.  A normal value keeps sign and mantissa and moves its
+// exponent by 1023 - 127 = 896; a subnormal one (mag x 2^-149) is normalised
+// by its leading bit; infinities and NaNs keep their mantissa bits.
+__device__ __forceinline__ double widen_f32(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t mag = b & 0x7fffffffu;
+    const uint32_t sign = b & 0x80000000u;
+    uint32_t hi = sign | ((mag >> 3) + (896u << 20)), lo = mag << 29;
+    if (__builtin_expect(mag - 0x00800000u >= 0x7f000000u, 0)) {
+        if (mag == 0) {
+            hi = sign;
+        } else if (mag >= 0x7f800000u) {
+            hi = sign | 0x7ff00000u | ((mag >> 3) & 0x000fffffu);
+        } else {  // subnormal: leading bit k in [0, 22], value 1.f x 2^(k - 149)
+            const int k = 31 - __clz(mag);
+            const uint64_t m = ((uint64_t)mag << (52 - k)) & 0x000fffffffffffffull;
+            hi = sign | ((uint32_t)(k + 874) << 20) | (uint32_t)(m >> 32);
+            lo = (uint32_t)m;
+        }
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// narrow_f64: round to nearest, ties to even, as the ordinary conversion.
+// The 53-bit significand is cut to 24 bits (normal results) or to the
+// subnormal grid of 2^-149; a carry out of the mantissa moves the exponent
+// up (to infinity past the largest float).
+__device__ __forceinline__ float narrow_f64(double d) {
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const uint32_t sign = hi & 0x80000000u;
+    const uint32_t mhi = hi & 0x7fffffffu;
+    const uint32_t e = mhi >> 20;
+    if (__builtin_expect(e - 897u < 254u, 1)) {  // normal float range before rounding
+        const uint32_t keep = ((mhi - (896u << 20)) << 3) | (lo >> 29);
+        const uint32_t rem = lo & 0x1fffffffu;
+        const uint32_t up = (rem > 0x10000000u) | ((rem == 0x10000000u) & keep);
+        return __uint_as_float(sign | (keep + up));
+    }
+    if (e == 2047u) return __uint_as_float(((mhi & 0x000fffffu) | lo) == 0 ? (sign | 0x7f800000u) : (sign | 0x7fffffffu));
+    if (e >= 1151u) return __uint_as_float(sign | 0x7f800000u);  // beyond the float range
+    if (e < 873u) return __uint_as_float(sign);                    // below half the least subnormal
+    // subnormal result: significand M (53 bits) x 2^(e - 1075) on the grid 2^-149
+    const uint64_t M = ((uint64_t)((mhi & 0x000fffffu) | 0x00100000u) << 32) | lo;
+    const uint32_t s = 926u - e;  // 30 .. 53
+    const uint64_t q = M >> s, rem = M & ((1ull << s) - 1), half = 1ull << (s - 1);
+    const uint64_t up = (rem > half) | ((rem == half) & q);
+    return __uint_as_float(sign | (uint32_t)(q + up));
+}
+
+// Compensated FP32 accumulation (Knuth's TwoSum: hi + lo carries the running
+// sum to about twice FP32 precision), for sums over many tiles kept off the
+// FP64 pipe.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float xp = s - hi;
+    const float hp = s - xp;
+    lo += (hi - hp) + (x - xp);
+    hi = s;
+}
+
 // Number of bits needed to hold coordinates in [0, dim).
 inline int bits_for(int64_t dim) {
     int b = 0;

@@ -290,27 +290,109 @@ __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __r
 
 // R <= 32: the symmetric sweep operator (Gauss-Jordan with diagonal pivots,
 // stable without pivoting on a positive-definite matrix) with the upper
-// triangle held in registers, kSmallPinvEpt elements per thread, and one
-// barrier per pivot.  Sweeping every pivot leaves -A^{-1}.  A non-positive
-// pivot means A is not positive definite.  The same acceptance test as the
-// Cholesky path (lambda_min >= 1/||A^{-1}||_F > 10 tol) guards the result;
-// otherwise the CTA computes the Jacobi pseudo-inverse.
+// triangle held in registers, kSmallPinvEpt elements per thread.  Sweeping
+// every pivot leaves -A^{-1}.  A non-positive pivot means A is not positive
+// definite.  The same acceptance test as the Cholesky path (lambda_min >=
+// 1/||A^{-1}||_F > 10 tol) guards the result; otherwise the CTA computes the
+// Jacobi pseudo-inverse.
 //
-// The refinement (refine != 0) is the Newton step written as
-// X + X (I - A X): the residual I - A X is formed in FP64 and the small
-// correction X (I - A X) in FP32, which keeps the FP64 pipe (the scarce one
-// on this part) to a single R^3 product.
+// Per pivot, warp 0 forms 1/pivot and the scaled pivot row once (one FP64
+// division per pivot, not one per thread: GB300 retires about two FP64
+// operations per clock per SM), then every element takes one FMA.
+//
+// refine == 2 tries pinv_sweep_f32 first (below).  The refinement (refine
+// == 1) is the Newton step written as
+// X + X (I - A X): the residual I - A X is formed in FP64 (A staged in shared
+// memory) and the small correction X (I - A X) in FP32 from FP32 copies of X
+// and the residual, which keeps the FP64 pipe to a single R^3 product.
 constexpr int kSmallPinvThreads = 128;
 constexpr int kSmallPinvMaxR = 32;
 constexpr int kSmallPinvEpt = (kSmallPinvMaxR * (kSmallPinvMaxR + 1) / 2 + kSmallPinvThreads - 1) / kSmallPinvThreads;
 
+// The same sweep in FP32 (mode 2: the leverage-score pseudo-inverse of the
+// mixed forms, whose scores are formed in FP32 anyway).  Accepted when every
+// pivot is positive and the FP32 error bound R ||A^{-1}||_F 2^-24 (A has a
+// unit diagonal here, so R bounds ||A||) stays below 2^-10; otherwise the
+// caller falls back to the FP64 sweep.  A dependent FP64 operation costs ~64
+// cycles on GB300 against ~4 for FP32, and this inverse sits on the step's
+// critical path.  Returns the uniform accept flag; on acceptance out holds
+// the inverse.
+__device__ bool pinv_sweep_f32(int R, const int (&ii)[kSmallPinvEpt], const int (&jj)[kSmallPinvEpt],
+                               const double (&a64)[kSmallPinvEpt], const double* __restrict__ A,
+                               double* __restrict__ out) {
+    __shared__ float rowf[2][kSmallPinvMaxR];
+    __shared__ float rpf[kSmallPinvMaxR];
+    __shared__ float pf;
+    __shared__ int badf;
+    __shared__ float frof;
+    const int tid = threadIdx.x;
+    float a[kSmallPinvEpt];
+#pragma unroll
+    for (int m = 0; m < kSmallPinvEpt; m++) a[m] = narrow_f64(a64[m]);
+    if (tid < R) rowf[0][tid] = narrow_f64(A[tid]);
+    if (tid == 0) {
+        badf = 0;
+        frof = 0.0f;
+    }
+    __syncthreads();
+    for (int k = 0; k < R; k++) {
+        const float* r = rowf[k & 1];
+        float* nr = rowf[(k + 1) & 1];
+        if (tid < 32) {
+            const float piv = r[k];
+            if (!(piv > 0.0f) || !isfinite(piv)) {
+                if (tid == 0) badf = 1;
+            } else {
+                const float p = 1.0f / piv;
+                if (tid < R) rpf[tid] = r[tid] * p;
+                if (tid == 0) pf = p;
+            }
+        }
+        __syncthreads();
+        if (badf) return false;  // uniform
+        const float p = pf;
+#pragma unroll
+        for (int m = 0; m < kSmallPinvEpt; m++) {
+            const int i = ii[m], j = jj[m];
+            if (i < 0) continue;
+            float v;
+            if (i != k && j != k) v = fmaf(-rpf[i], r[j], a[m]);
+            else if (i == k && j == k) v = -p;
+            else v = rpf[i == k ? j : i];
+            a[m] = v;
+            if (i == k + 1) nr[j] = v;
+            else if (j == k + 1) nr[i] = v;
+        }
+        __syncthreads();
+    }
+    float part = 0.0f;
+#pragma unroll
+    for (int m = 0; m < kSmallPinvEpt; m++)
+        if (ii[m] >= 0) part += (ii[m] == jj[m] ? 1.0f : 2.0f) * a[m] * a[m];
+    part = warp_sum(part);
+    if ((tid & 31) == 0) atomicAdd(&frof, part);
+    __syncthreads();
+    const float fro = frof;
+    if (!(isfinite(fro) && (float)R * sqrtf(fro) <= 0x1.0p14f)) return false;  // R ||X||_F 2^-24 <= 2^-10
+#pragma unroll
+    for (int m = 0; m < kSmallPinvEpt; m++) {
+        if (ii[m] < 0) continue;
+        const double x = widen_f32(-a[m]);
+        out[ii[m] * R + jj[m]] = x;
+        out[jj[m] * R + ii[m]] = x;
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(kSmallPinvThreads)
     spd_pinv_small_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
                           double* vt_scratch, int refine) {
-    extern __shared__ double smem[];  // Jacobi fallback / FP64 Newton step
-    __shared__ double rowbuf[2][kSmallPinvMaxR];
+    extern __shared__ double smem[];  // Jacobi fallback; in the accepted path A, X and E staged for refinement
+    __shared__ double rowbuf[2][kSmallPinvMaxR];  // pivot row k (unscaled), ping-pong
+    __shared__ double rp[kSmallPinvMaxR];         // pivot row k times 1/pivot
+    __shared__ double pinv_k;                     // 1/pivot
+    __shared__ int bad;
     __shared__ double Xs[kSmallPinvMaxR][kSmallPinvMaxR + 1];
-    __shared__ double Es[kSmallPinvMaxR][kSmallPinvMaxR + 1];
     __shared__ double fro;
     const int tid = threadIdx.x;
     const int P = R * (R + 1) / 2;
@@ -328,27 +410,41 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
         jj[m] = (e < P) ? i + (e - base) : -1;
         a[m] = (e < P) ? A[i * R + jj[m]] : 0.0;
     }
+    if (refine == 2 && pinv_sweep_f32(R, ii, jj, a, A, out)) return;
     if (tid < R) rowbuf[0][tid] = A[tid];
-    if (tid == 0) fro = 0.0;
+    if (tid == 0) {
+        fro = 0.0;
+        bad = 0;
+    }
     __syncthreads();
     bool ok = true;
     for (int k = 0; k < R; k++) {
         const double* r = rowbuf[k & 1];
         double* nr = rowbuf[(k + 1) & 1];
-        const double piv = r[k];  // same value in every thread: the exit is uniform
-        if (!(piv > 0.0) || !isfinite(piv)) {
+        if (tid < 32) {
+            const double piv = r[k];
+            if (!(piv > 0.0) || !isfinite(piv)) {
+                if (tid == 0) bad = 1;
+            } else {
+                const double p = 1.0 / piv;
+                if (tid < R) rp[tid] = r[tid] * p;
+                if (tid == 0) pinv_k = p;
+            }
+        }
+        __syncthreads();
+        if (bad) {  // uniform
             ok = false;
             break;
         }
-        const double p = 1.0 / piv;
+        const double p = pinv_k;
 #pragma unroll
         for (int m = 0; m < kSmallPinvEpt; m++) {
             const int i = ii[m], j = jj[m];
             if (i < 0) continue;
             double v;
-            if (i != k && j != k) v = fma(-r[i] * p, r[j], a[m]);
+            if (i != k && j != k) v = fma(-rp[i], r[j], a[m]);
             else if (i == k && j == k) v = -p;
-            else v = r[i == k ? j : i] * p;
+            else v = rp[i == k ? j : i];
             a[m] = v;
             if (i == k + 1) nr[j] = v;
             else if (j == k + 1) nr[i] = v;
@@ -372,28 +468,37 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
         ok = isfinite(fro) && 1.0 / sqrt(fro) > 10.0 * tol;
     }
     if (ok) {
-        if (!refine) {
+        if (refine != 1) {
             for (int e = tid; e < R * R; e += kSmallPinvThreads) out[e] = Xs[e / R][e % R];
             return;
         }
+        double* As = smem;                                        // R x R
+        float* Xf = reinterpret_cast<float*>(smem + R * R);       // R x (R + 1)
+        float* Ef = Xf + R * (R + 1);                             // R x (R + 1)
+        for (int e = tid; e < R * R; e += kSmallPinvThreads) {
+            const int i = e / R, j = e % R;
+            As[e] = A[(i <= j) ? i * R + j : j * R + i];
+            Xf[i * (R + 1) + j] = narrow_f64(Xs[i][j]);
+        }
+        __syncthreads();
         for (int e = tid; e < R * R; e += kSmallPinvThreads) {  // E = I - A X
             const int i = e / R, j = e % R;
             double acc = (i == j) ? 1.0 : 0.0;
-            for (int t = 0; t < R; t++) acc = fma(-A[(i <= t) ? i * R + t : t * R + i], Xs[t][j], acc);
-            Es[i][j] = acc;
+            for (int t = 0; t < R; t++) acc = fma(-As[i * R + t], Xs[t][j], acc);
+            Ef[i * (R + 1) + j] = narrow_f64(acc);
         }
         __syncthreads();
         for (int e = tid; e < R * R; e += kSmallPinvThreads) {  // out = X + X E
             const int i = e / R, j = e % R;
             float c = 0.0f;
-            for (int t = 0; t < R; t++) c = fmaf((float)Xs[i][t], (float)Es[t][j], c);
-            out[e] = Xs[i][j] + (double)c;
+            for (int t = 0; t < R; t++) c = fmaf(Xf[i * (R + 1) + t], Ef[t * (R + 1) + j], c);
+            out[e] = Xs[i][j] + widen_f32(c);
         }
         return;
     }
     __syncthreads();
     syev_block(R, A, nullptr, nullptr, out, tol, vt_scratch, smem);
-    if (refine) newton_refine(R, A, out, smem);
+    if (refine == 1) newton_refine(R, A, out, smem);
 }
 
 // Shared memory of the Cholesky path (L, L^{-1}, and the Newton step's
@@ -434,6 +539,12 @@ int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scra
 
 int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream) {
     return launch_pinv_impl(R, A, out, tol, vt_scratch, 1, stream);
+}
+
+int launch_pinv_leverage_f32(int R, const double* A, double* out, double tol, double* vt_scratch,
+                             cudaStream_t stream) {
+    if (R > kSmallPinvMaxR) return launch_pinv_impl(R, A, out, tol, vt_scratch, 0, stream);
+    return launch_pinv_impl(R, A, out, tol, vt_scratch, 2, stream);
 }
 
 size_t syev_smem_bytes(int R) {

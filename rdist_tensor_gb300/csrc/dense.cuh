@@ -20,5 +20,9 @@ int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scra
 // The same followed by one Newton step X <- 2X - X A X (the refinement the
 // mixed forms apply to the solve).
 int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
+// The leverage-score pseudo-inverse of the mixed forms (unit-diagonal Gram):
+// the sweep in FP32 when its error bound allows, else the FP64 path.
+int launch_pinv_leverage_f32(int R, const double* A, double* out, double tol, double* vt_scratch,
+                             cudaStream_t stream);
 
 }  // namespace exafac

@@ -17,7 +17,10 @@
 namespace exafac {
 
 constexpr uint32_t kEmpty = 0xffffffffu;
-constexpr int64_t kExactCdfMax = 16384;  // CDFs up to this length are summed strictly in order
+// CDFs up to this length are summed strictly in order (bit compatible with
+// libstdc++).  The two serial FP64 chains cost ~64 cycles per element on GB300
+// (a dependent FP64 add), so longer CDFs take the blockwise scan.
+constexpr int64_t kExactCdfMax = 512;
 constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a power of two)
 constexpr int kRngSlot = 15;              // counters[] slot of the session's Philox counter
 

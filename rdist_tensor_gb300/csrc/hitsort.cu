@@ -80,7 +80,7 @@ __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t 
             const int64_t p = (int64_t)f_start[j] + (h - f_off[j]);
             key[h] = rows_n[p];
             if (kPacked) {
-                pay64[h] = pack_hit((uint32_t)j, (float)vals_n[p]);
+                pay64[h] = pack_hit((uint32_t)j, narrow_f64(vals_n[p]));
             } else {
                 ex_j[h] = (uint32_t)j;
                 ex_val[h] = vals_n[p];

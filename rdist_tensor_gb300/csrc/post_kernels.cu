@@ -611,7 +611,8 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
 //     broadcasts from shared memory;
 //   * the Gram of the solved rows is accumulated in 4 x 4 register blocks of
 //     the lower triangle (NB blocks per lane), in FP32 within a 32-row tile
-//     and in FP64 across tiles, then summed over the block's warps in warp
+//     and in compensated FP32 (hi + lo) across tiles, then in FP64 over the
+//     block's warps in warp
 //     order (reproducible).
 // ---------------------------------------------------------------------------
 constexpr int kTileStride = 36;  // floats per staged row (16-byte aligned rows)
@@ -631,8 +632,8 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
                                                                          double* __restrict__ part) {
     using S = TileShape<KC>;
     __shared__ __align__(16) float phi[KC][KC];
-    __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
-    __shared__ double red[32 * 33 / 2];
+    __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];  // at the end: the per-warp Gram slab
+    static_assert(sizeof(tile) >= sizeof(double) * kSolveWarps * (32 * 33 / 2), "slab does not fit");
     const int P = R * (R + 1) / 2;
     const int ldm = f32_row_stride(R);  // Mc row stride
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -640,7 +641,6 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
         const int a = e / KC, b = e % KC;
         phi[a][b] = (a < R && b < R) ? (float)Phi[a * R + b] : 0.0f;
     }
-    for (int e = threadIdx.x; e < P; e += blockDim.x) red[e] = 0.0;
     // this lane's lower-triangle 4x4 blocks
     int bi[S::kNB], bj[S::kNB];
 #pragma unroll
@@ -653,11 +653,11 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
         bi[q] = (lane + 32 * q < S::kTri) ? i : -1;
         bj[q] = blk;
     }
-    double gd[S::kNB][16];
+    float ghi[S::kNB][16], glo[S::kNB][16];  // compensated sums over the warp's tiles
 #pragma unroll
     for (int q = 0; q < S::kNB; q++)
 #pragma unroll
-        for (int x = 0; x < 16; x++) gd[q][x] = 0.0;
+        for (int x = 0; x < 16; x++) ghi[q][x] = glo[q][x] = 0.0f;
     __syncthreads();
     float (*t)[kTileStride] = tile[w];
     const int64_t nt = counters[2];
@@ -717,34 +717,43 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
                         for (int y = 0; y < 4; y++) g[x * 4 + y] = fmaf(av[x], bv[y], g[x * 4 + y]);
                 }
 #pragma unroll
-                for (int x = 0; x < 16; x++) gd[q][x] += (double)g[x];
+                for (int x = 0; x < 16; x++) two_sum_acc(ghi[q][x], glo[q][x], g[x]);
             }
         }
         __syncwarp();
     }
-    for (int ww = 0; ww < kSolveWarps; ww++) {  // block sum in warp order
-        if (w == ww) {
+    // Block sum in warp order: every warp leaves its sums in its row of a slab
+    // over the (now free) tiles, each packed entry with one owner lane per
+    // warp; a thread per entry then adds the rows in order.
+    __syncthreads();
+    double* slab = reinterpret_cast<double*>(&tile[0][0][0]);
 #pragma unroll
-            for (int q = 0; q < S::kNB; q++) {
-                if (bi[q] < 0) continue;
+    for (int q = 0; q < S::kNB; q++) {
+        if (bi[q] < 0) continue;
 #pragma unroll
-                for (int x = 0; x < 4; x++)
+        for (int x = 0; x < 4; x++)
 #pragma unroll
-                    for (int y = 0; y < 4; y++) {
-                        const int a = 4 * bi[q] + x, b = 4 * bj[q] + y;  // b's block <= a's block
-                        if (a < R && b < R && b <= a) red[packed_index(R, b, a)] += gd[q][x * 4 + y];
-                    }
+            for (int y = 0; y < 4; y++) {
+                const int a = 4 * bi[q] + x, b = 4 * bj[q] + y;  // b's block <= a's block
+                if (a < R && b < R && b <= a)
+                    slab[w * P + packed_index(R, b, a)] = (double)ghi[q][x * 4 + y] + (double)glo[q][x * 4 + y];
             }
-        }
-        __syncthreads();
     }
-    for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        double acc = 0.0;
+#pragma unroll
+        for (int ww = 0; ww < kSolveWarps; ww++) acc += slab[ww * P + e];
+        part[(int64_t)blockIdx.x * P + e] = acc;
+    }
 }
 
 // u_r = Uc_r / sigma (Uc: the compact rows of solve_gram_f32_kernel) written
 // to U at the touched row, and, when P != null, l_r = u_r^T P u_r in FP32;
 // rows staged as in solve_gram_f32_kernel.  This is the one scattered pass
-// over the factor.
+// over the factor.  The scaling runs in FP32 (u = Uc * fl32(1 / sigma)) and
+// the result is widened to FP64 exactly, so no element goes through the FP64
+// pipe.
 template <int KC>
 __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, const int64_t* __restrict__ counters,
                                                                       const uint32_t* __restrict__ touched,
@@ -756,7 +765,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
                                                                       double* __restrict__ scores) {
     __shared__ __align__(16) float psm[KC][KC];
     __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
-    __shared__ double sg[32];
+    __shared__ float sg[32];
     // A zero column norm: write the unscaled rows and leave the division of
     // every row (as the reference does) to scale_rows_if_degenerate.
     const bool deg = *degenerate != 0;
@@ -764,14 +773,14 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
         const int a = e / KC, b = e % KC;
         psm[a][b] = (Pm && a < R && b < R) ? (float)Pm[a * R + b] : 0.0f;
     }
-    // Multiplying by 1/sigma differs from the reference's division by at
-    // most one rounding.
-    for (int c = threadIdx.x; c < 32; c += blockDim.x) sg[c] = c < R ? 1.0 / sigma[c] : 0.0;
+    // Multiplying by fl32(1/sigma) differs from the reference's division by
+    // at most two FP32 roundings.
+    for (int c = threadIdx.x; c < 32; c += blockDim.x) sg[c] = deg ? 1.0f : (c < R ? (float)(1.0 / sigma[c]) : 0.0f);
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ldm = f32_row_stride(R);  // Uc row stride
     float (*t)[kTileStride] = tile[w];
-    const double sgl = deg ? 1.0 : sg[lane];
+    const float sgl = sg[lane];
     const int64_t nt = counters[2];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -795,9 +804,9 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
             double* blk = U + (int64_t)row0 * R;
             int r = lane / R, c = lane % R;
             for (int e = lane; e < 32 * R; e += 32) {
-                const double y = (double)t[r][c] * (deg ? 1.0 : sg[c]);
-                blk[e] = y;
-                t[r][c] = (float)y;
+                const float y = t[r][c] * sg[c];
+                blk[e] = widen_f32(y);
+                t[r][c] = y;
                 c += 32;
                 while (c >= R) {
                     c -= R;
@@ -809,9 +818,9 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
             for (int r = 0; r < nrow; r++) {  // normalised FP64 rows to the factor, one row per store
                 const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
                 if (lane < KC) {
-                    const double y = (double)t[r][lane] * sgl;
-                    if (lane < R) U[row * R + lane] = y;
-                    t[r][lane] = (float)y;
+                    const float y = t[r][lane] * sgl;
+                    if (lane < R) U[row * R + lane] = widen_f32(y);
+                    t[r][lane] = y;
                 }
             }
         }
@@ -842,7 +851,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
                     acc = fmaf(u[a], y, acc);
                 }
             }
-            scores[myrow] = (double)acc;
+            scores[myrow] = widen_f32(acc);
         }
         __syncwarp();
     }
@@ -922,7 +931,7 @@ int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st) {
     const int R = s.R;
     EXAFAC_TRY(gram_reduce_to(s, kSolveBlocks, s.ugram, st));
     EXAFAC_TRY(sigma_and_gram(s, st));
-    if (arls) EXAFAC_TRY(launch_pinv(R, s.ngram, s.upinv, 1e-11, s.vt, st));
+    if (arls) EXAFAC_TRY(launch_pinv_leverage_f32(R, s.ngram, s.upinv, 1e-11, s.vt, st));
     if (R <= 16) launch_normlev_f32<16>(s, n, arls, st);
     else if (R <= 28) launch_normlev_f32<28>(s, n, arls, st);
     else launch_normlev_f32<32>(s, n, arls, st);

@@ -191,9 +191,14 @@ struct ArlsModes {
 // CP_ARLS_LEV::KRPDrawSamples + draw_leverage_score_samples
 // (cp_arls_lev.hpp:36-163) at one rank, thread per sample: the draw is the
 // first CDF entry >= u (lower_bound, searched between the guide entries of
-// u's bucket), the log weight log(sum) - log(l_idx) is added mode by mode to
-// -log J, then exponentiated.
-__global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const double* __restrict__ total,
+// u's bucket).  The weight is the reference's exp(sum_k (log sum_k - log l_k)
+// - log J) in the FP64 form (log_form != 0).  The mixed forms take the
+// product (prod_k sum_k) / (J prod_k l_k) instead: the same number to ~1e-14
+// relative (the rounding of the log-exp form itself), with one division in
+// place of N logs and an exp, which on GB300's narrow FP64 pipe dominated the
+// draw; a product that leaves the normal range (or a zero score) falls back
+// to the log form.
+__global__ void arls_draw_kernel(int N, int n, int64_t J, int log_form, ArlsModes m, const double* __restrict__ total,
                                  const double* __restrict__ uni, const uint32_t* __restrict__ perms,
                                  uint32_t* __restrict__ samples, double* __restrict__ weights,
                                  DeviceStatus* status) {
@@ -202,7 +207,7 @@ __global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const dou
     __syncthreads();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= J) return;
-    double w = 0.0 - log((double)J);
+    double num = 1.0, den = (double)J;
     for (int k = 0; k < N; k++) {
         if (k == n) continue;
         const int64_t I = m.dims[k];
@@ -232,12 +237,20 @@ __global__ void arls_draw_kernel(int N, int n, int64_t J, ArlsModes m, const dou
                 }
             }
         }
-        const double lw = 0.0 + (log_total[k] - log(m.scores[k][idx]));
+        num *= total[k];
+        den *= m.scores[k][idx];
         samples[t * N + k] = (uint32_t)idx;
-        w += lw;
     }
     samples[t * N + n] = 0;
-    weights[t] = exp(w);
+    double w = log_form ? 0.0 : num / den;
+    const uint32_t ew = (uint32_t)(__double_as_longlong(w) >> 52) & 0x7ffu;
+    if (log_form || ew == 0 || ew == 0x7ffu) {  // the FP64 form, or zero, subnormal, inf or nan
+        double lw = 0.0 - log((double)J);
+        for (int k = 0; k < N; k++)
+            if (k != n) lw += 0.0 + (log_total[k] - log(m.scores[k][samples[t * N + k]]));
+        w = exp(lw);
+    }
+    weights[t] = w;
 }
 
 int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* perms, cudaStream_t st) {
@@ -251,7 +264,8 @@ int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* p
         m.len[k] = compact ? s.nzcount + k : nullptr;
         m.dims[k] = k < s.N ? s.dims[k] : 0;
     }
-    arls_draw_kernel<<<(unsigned)ceil_div(J, 256), 256, 0, st>>>(s.N, n, J, m, s.cdf_total, uni, perms, s.samples,
+    const int log_form = s.cfg.precision == EXAFAC_PREC_FP64;
+    arls_draw_kernel<<<(unsigned)ceil_div(J, 256), 256, 0, st>>>(s.N, n, J, log_form, m, s.cdf_total, uni, perms, s.samples,
                                                                   s.weights, s.status); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

@@ -217,13 +217,15 @@ __device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(_
 
 // Tensor-core form.  A warp owns 32 design rows at a time:
 //   * factor rows are gathered one per load instruction (lane = column),
-//     32 rows in flight per mode, and multiplied in FP32;
+//     32 rows in flight per mode, rounded to FP32 in integer arithmetic
+//     (narrow_f64, off the FP64 pipe) and multiplied in FP32;
 //   * D'_j = d_j * w_j goes to Df (FP32, rows of f32_row_stride(R) floats,
 //     zero padded), the Gram input round(d_j sqrt(w_j))
 //     to a shared tile T (32 rows x kDStride, zero padded);
 //   * the tile's Gram T^T T comes from mma.sync m16n8k8 TF32 instructions with
 //     FP32 accumulation (only the 16 x 8 blocks on or below the diagonal),
-//     added to FP64 accumulators after every 32-row tile.  BF16-rounded inputs
+//     added to compensated FP32 sums (hi + lo) after every 32-row tile, and
+//     to FP64 once per warp at the end.  BF16-rounded inputs
 //     are exact in TF32, so the same instruction serves both roundings.
 // The block's warps are summed in warp order into part[block] (packed).
 constexpr int kDesignWarps = 8;
@@ -245,8 +247,10 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
                                                                        const double* __restrict__ wd, FactorPtrs f,
                                                                        float* __restrict__ Df,
                                                                        double* __restrict__ part) {
+    // the warps' tiles; at the end the per-warp Gram sums (kDesignWarps x P doubles)
     __shared__ __align__(16) float tile[kDesignWarps][32][kDStride];
-    __shared__ double red[32 * 33 / 2];
+    __shared__ uint32_t sidx[kDesignWarps][kMaxModes][32];  // the tile's sample indices, all modes
+    static_assert(sizeof(tile) >= sizeof(double) * kDesignWarps * (32 * 33 / 2), "slab does not fit");
     // lower-triangle (m-tile, n-tile) pairs of the 32 x 32 Gram: 16-row m-tiles, 8-column n-tiles
     constexpr int kPairs = 6;
     constexpr int kMt[kPairs] = {0, 0, 1, 1, 1, 1};
@@ -254,13 +258,11 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
     const int P = R * (R + 1) / 2;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gid = lane >> 2, tig = lane & 3;
-    for (int e = threadIdx.x; e < P; e += blockDim.x) red[e] = 0.0;
-    __syncthreads();
-    double gacc[kPairs][4];
+    float ghi[kPairs][4], glo[kPairs][4];  // compensated sums over the warp's tiles
 #pragma unroll
     for (int p = 0; p < kPairs; p++)
 #pragma unroll
-        for (int i = 0; i < 4; i++) gacc[p][i] = 0.0;
+        for (int i = 0; i < 4; i++) ghi[p][i] = glo[p][i] = 0.0f;
     float (*t)[kDStride] = tile[w];
     const int RS = (R + 3) & ~3;  // Df row stride (zero padded)
     const int64_t ju = *ju_dev;
@@ -271,19 +273,20 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
         float prod[32];
 #pragma unroll
         for (int r = 0; r < 32; r++) prod[r] = 1.0f;
+        // every mode's indices in one round of loads, before the first gather
+        for (int k = 0; k < N; k++) sidx[w][k][lane] = lane < nrow ? sd[(base + lane) * N + k] : 0u;
+        __syncwarp();
         for (int k = 0; k < N; k++) {
             if (k == n) continue;
-            const uint32_t myidx = lane < nrow ? sd[(base + lane) * N + k] : 0u;
+            const uint32_t myidx = sidx[w][k][lane];
             const double* Uk = f.U[k];
 #pragma unroll
             for (int r = 0; r < 32; r++) {
                 const int64_t i = __shfl_sync(0xffffffffu, myidx, r);
-                if (r < nrow && lane < R) prod[r] *= (float)Uk[i * R + lane];
+                if (r < nrow && lane < R) prod[r] *= narrow_f64(Uk[i * R + lane]);
             }
         }
-        double wj = 0.0;
-        if (lane < nrow) wj = wd[base + lane];
-        const float myw = (float)wj, mysw = (float)sqrt(wj);
+        const float myw = lane < nrow ? narrow_f64(wd[base + lane]) : 0.0f, mysw = sqrtf(myw);
 #pragma unroll
         for (int r = 0; r < 32; r++) {
             const float wr = __shfl_sync(0xffffffffu, myw, r), swr = __shfl_sync(0xffffffffu, mysw, r);
@@ -323,23 +326,29 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
 #pragma unroll
         for (int p = 0; p < kPairs; p++)
 #pragma unroll
-            for (int i = 0; i < 4; i++) gacc[p][i] += (double)c[p][i];
+            for (int i = 0; i < 4; i++) two_sum_acc(ghi[p][i], glo[p][i], c[p][i]);
         __syncwarp();
     }
-    for (int ww = 0; ww < kDesignWarps; ww++) {  // block sum in warp order
-        if (w == ww) {
+    // Block sum in warp order: every warp leaves its sums in its row of the
+    // slab (each packed entry has exactly one owner lane per warp), then a
+    // thread per entry adds the rows in order.
+    __syncthreads();
+    double* slab = reinterpret_cast<double*>(&tile[0][0][0]);
 #pragma unroll
-            for (int p = 0; p < kPairs; p++)
+    for (int p = 0; p < kPairs; p++)
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int row = 16 * kMt[p] + gid + 8 * (i >> 1);
-                    const int col = 8 * kNt[p] + 2 * tig + (i & 1);
-                    if (row < R && col <= row) red[packed_index(R, col, row)] += gacc[p][i];
-                }
+        for (int i = 0; i < 4; i++) {
+            const int row = 16 * kMt[p] + gid + 8 * (i >> 1);
+            const int col = 8 * kNt[p] + 2 * tig + (i & 1);
+            if (row < R && col <= row) slab[w * P + packed_index(R, col, row)] = (double)ghi[p][i] + (double)glo[p][i];
         }
-        __syncthreads();
+    __syncthreads();
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        double acc = 0.0;
+#pragma unroll
+        for (int ww = 0; ww < kDesignWarps; ww++) acc += slab[ww * P + e];
+        part[(int64_t)blockIdx.x * P + e] = acc;
     }
-    for (int e = threadIdx.x; e < P; e += blockDim.x) part[(int64_t)blockIdx.x * P + e] = red[e];
 }
 
 // R > 32 (padded to RP = 64 or 128): the block's 8 warps share one 32-row
