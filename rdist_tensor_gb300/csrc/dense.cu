@@ -310,77 +310,71 @@ constexpr int kSmallPinvMaxR = 32;
 constexpr int kSmallPinvEpt = (kSmallPinvMaxR * (kSmallPinvMaxR + 1) / 2 + kSmallPinvThreads - 1) / kSmallPinvThreads;
 
 // The same sweep in FP32 (mode 2: the leverage-score pseudo-inverse of the
-// mixed forms, whose scores are formed in FP32 anyway).  Accepted when every
-// pivot is positive and the FP32 error bound R ||A^{-1}||_F 2^-24 (A has a
-// unit diagonal here, so R bounds ||A||) stays below 2^-10; otherwise the
-// caller falls back to the FP64 sweep.  A dependent FP64 operation costs ~64
-// cycles on GB300 against ~4 for FP32, and this inverse sits on the step's
-// critical path.  Returns the uniform accept flag; on acceptance out holds
-// the inverse.
-__device__ bool pinv_sweep_f32(int R, const int (&ii)[kSmallPinvEpt], const int (&jj)[kSmallPinvEpt],
-                               const double (&a64)[kSmallPinvEpt], const double* __restrict__ A,
-                               double* __restrict__ out) {
-    __shared__ float rowf[2][kSmallPinvMaxR];
-    __shared__ float rpf[kSmallPinvMaxR];
-    __shared__ float pf;
-    __shared__ int badf;
-    __shared__ float frof;
+// mixed forms, whose scores are formed in FP32 anyway), run by warp 0 with
+// the whole matrix in registers.  Lane j holds column j; the rows rotate
+// through the registers so that the pivot row is always slot 0 (before pivot
+// k, slot s holds row (k + s) mod 32), which keeps every register index
+// static in a rolled pivot loop.  The swept matrix stays symmetric, so the
+// pivot column's entry for row (k + s) is lane (k + s)'s row-k value, one
+// shuffle each; no barrier per pivot.  Rows and lanes >= R hold zeros and
+// stay zero.  Accepted when every pivot is positive and the FP32 error bound
+// R ||A^{-1}||_F 2^-24 (A has a unit diagonal here, so R bounds ||A||) stays
+// below 2^-10; otherwise the caller falls back to the FP64 sweep.  A
+// dependent FP64 operation costs ~64 cycles on GB300 against ~4 for FP32, and
+// this inverse sits on the step's critical path.  Returns the block-uniform
+// accept flag; on acceptance out holds the inverse.
+__device__ bool pinv_sweep_f32(int R, const double* __restrict__ A, double* __restrict__ out) {
+    // Loads, conversions and stores run as rolled loops over the whole block:
+    // a single warp's straight-line code is fetched once and pays the
+    // instruction-fetch latency per line.
+    __shared__ float Af[32][33];
+    __shared__ int accepted;
     const int tid = threadIdx.x;
-    float a[kSmallPinvEpt];
-#pragma unroll
-    for (int m = 0; m < kSmallPinvEpt; m++) a[m] = narrow_f64(a64[m]);
-    if (tid < R) rowf[0][tid] = narrow_f64(A[tid]);
-    if (tid == 0) {
-        badf = 0;
-        frof = 0.0f;
+    for (int e = tid; e < 32 * 32; e += blockDim.x) {
+        const int i = e >> 5, c = e & 31;
+        Af[i][c] = (i < R && c < R) ? narrow_f64(A[i * R + c]) : 0.0f;
     }
     __syncthreads();
-    for (int k = 0; k < R; k++) {
-        const float* r = rowf[k & 1];
-        float* nr = rowf[(k + 1) & 1];
-        if (tid < 32) {
-            const float piv = r[k];
+    if (tid < 32) {
+        const int j = tid;
+        const unsigned full = 0xffffffffu;
+        float col[32];
+#pragma unroll
+        for (int s = 0; s < 32; s++) col[s] = Af[s][j];
+        bool ok = true;
+#pragma unroll 1
+        for (int k = 0; k < R; k++) {
+            const float akj = col[0];                     // A[k][j]
+            const float piv = __shfl_sync(full, akj, k);  // A[k][k], the same in every lane
             if (!(piv > 0.0f) || !isfinite(piv)) {
-                if (tid == 0) badf = 1;
-            } else {
-                const float p = 1.0f / piv;
-                if (tid < R) rpf[tid] = r[tid] * p;
-                if (tid == 0) pf = p;
+                ok = false;
+                break;
             }
-        }
-        __syncthreads();
-        if (badf) return false;  // uniform
-        const float p = pf;
+            const float p = 1.0f / piv;
+            const float akjp = akj * p;
+            float nxt[32];
 #pragma unroll
-        for (int m = 0; m < kSmallPinvEpt; m++) {
-            const int i = ii[m], j = jj[m];
-            if (i < 0) continue;
-            float v;
-            if (i != k && j != k) v = fmaf(-rpf[i], r[j], a[m]);
-            else if (i == k && j == k) v = -p;
-            else v = rpf[i == k ? j : i];
-            a[m] = v;
-            if (i == k + 1) nr[j] = v;
-            else if (j == k + 1) nr[i] = v;
+            for (int s = 1; s < 32; s++) {
+                const float aik = __shfl_sync(full, akj, (k + s) & 31);  // A[k + s][k]
+                nxt[s - 1] = (j == k) ? aik * p : fmaf(-aik, akjp, col[s]);
+            }
+            nxt[31] = (j == k) ? -p : akjp;  // row k moves to the last slot
+#pragma unroll
+            for (int s = 0; s < 32; s++) col[s] = nxt[s];
         }
-        __syncthreads();
+        float fro = 0.0f;
+#pragma unroll
+        for (int s = 0; s < 32; s++) fro = fmaf(col[s], col[s], fro);
+        fro = warp_sum(fro);
+        ok = ok && isfinite(fro) && (float)R * sqrtf(fro) <= 0x1.0p14f;  // R ||X||_F 2^-24 <= 2^-10
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < 32; s++) Af[(R + s) & 31][j] = -col[s];  // after R pivots slot s holds row (R + s) mod 32
+        if (j == 0) accepted = ok;
     }
-    float part = 0.0f;
-#pragma unroll
-    for (int m = 0; m < kSmallPinvEpt; m++)
-        if (ii[m] >= 0) part += (ii[m] == jj[m] ? 1.0f : 2.0f) * a[m] * a[m];
-    part = warp_sum(part);
-    if ((tid & 31) == 0) atomicAdd(&frof, part);
     __syncthreads();
-    const float fro = frof;
-    if (!(isfinite(fro) && (float)R * sqrtf(fro) <= 0x1.0p14f)) return false;  // R ||X||_F 2^-24 <= 2^-10
-#pragma unroll
-    for (int m = 0; m < kSmallPinvEpt; m++) {
-        if (ii[m] < 0) continue;
-        const double x = widen_f32(-a[m]);
-        out[ii[m] * R + jj[m]] = x;
-        out[jj[m] * R + ii[m]] = x;
-    }
+    if (!accepted) return false;
+    for (int e = tid; e < R * R; e += blockDim.x) out[e] = widen_f32(Af[e / R][e % R]);
     return true;
 }
 
@@ -394,6 +388,7 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
     __shared__ int bad;
     __shared__ double Xs[kSmallPinvMaxR][kSmallPinvMaxR + 1];
     __shared__ double fro;
+    if (refine == 2 && pinv_sweep_f32(R, A, out)) return;
     const int tid = threadIdx.x;
     const int P = R * (R + 1) / 2;
     int ii[kSmallPinvEpt], jj[kSmallPinvEpt];
@@ -410,7 +405,6 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
         jj[m] = (e < P) ? i + (e - base) : -1;
         a[m] = (e < P) ? A[i * R + jj[m]] : 0.0;
     }
-    if (refine == 2 && pinv_sweep_f32(R, ii, jj, a, A, out)) return;
     if (tid < R) rowbuf[0][tid] = A[tid];
     if (tid == 0) {
         fro = 0.0;

@@ -22,6 +22,7 @@ constexpr uint32_t kEmpty = 0xffffffffu;
 // (a dependent FP64 add), so longer CDFs take the blockwise scan.
 constexpr int64_t kExactCdfMax = 512;
 constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a power of two)
+constexpr int kExpandChunk = 256;  // hits per warp chunk in the hit expansion
 constexpr int kRngSlot = 15;              // counters[] slot of the session's Philox counter
 
 struct Slot1 {
@@ -95,6 +96,7 @@ struct Session {
     int32_t* d_minj = nullptr;
     int32_t* d_count = nullptr;
     int32_t* slot_of = nullptr;
+    Key128* dkey = nullptr;         // J: packed dedup key of each sample
     uint32_t* flags = nullptr;
     int64_t* pos = nullptr;
     uint32_t* sd = nullptr;
@@ -138,6 +140,7 @@ struct Session {
     uint32_t* carry_row = nullptr;  // chunks: row continuing past the chunk, or 0xffffffff
     uint32_t* carry_seg = nullptr;  // chunks: that row's touched-row index (compact Mc)
     uint32_t* chunk_seg = nullptr;  // chunks of kSegChunkF32 sorted hits: run index of the first hit
+    uint32_t* expand_first = nullptr;  // ceil(nnz / kExpandChunk) + 1: sample owning each expansion chunk's first hit
     float* Uc = nullptr;            // Imax x 32, mixed forms: solved rows by touched-row index
     uint32_t* rowbits = nullptr;    // ceil(Imax / 32): rows touched by the current step
     float* Df = nullptr;          // Jmax x R design rows (mixed forms)

@@ -28,7 +28,6 @@ constexpr int kHsWarps = kHsThreads / 32;
 constexpr int kHsGrid = 152 * 4;      // upsweep / heads
 constexpr int kHsDownGrid = 152 * 2;        // downsweep: one resident wave (99 registers x 256 threads)
 constexpr int kHsDownGridPacked = 152 * 3;  // 64-bit payloads, 8 items per thread
-constexpr int kExpandChunk = 256;  // hits per warp chunk in the expansion
 constexpr uint32_t kNoItem = 0xffffffffu;
 
 __device__ __forceinline__ int64_t hit_count(const int64_t* counters, int64_t cap) { return min(counters[1], cap); }
@@ -43,8 +42,26 @@ __device__ __forceinline__ int64_t owner_in(const int64_t* __restrict__ f_off, i
     return lo;
 }
 
-// Hits in sample order: the owner sample of each hit by one binary search
-// per warp chunk for its bounds, then a search restricted to them.  kPacked
+// The sample owning the first hit of every expansion chunk (a load-balanced
+// search, thread per sample): sample j owns hits [f_off[j], f_off[j] +
+// f_len[j]), and the chunk starts c * kExpandChunk in that range are its.
+// The samples with hits partition [0, H), so every chunk start has one owner.
+__global__ void expand_owner_kernel(const int64_t* __restrict__ counters, int64_t cap,
+                                    const int64_t* __restrict__ f_off, const uint32_t* __restrict__ f_len,
+                                    uint32_t* __restrict__ first) {
+    const int64_t ju = counters[0];
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ju; j += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t len = f_len[j];
+        if (len == 0) continue;
+        const int64_t a = f_off[j];
+        const int64_t b = min(a + (int64_t)len, cap);
+        for (int64_t c = (a + kExpandChunk - 1) / kExpandChunk; c * kExpandChunk < b; c++) first[c] = (uint32_t)j;
+    }
+}
+
+// Hits in sample order: each warp chunk's samples lie between the owners of
+// its first hit and of the next chunk's first hit (expand_owner_kernel), and
+// each hit's owner is found by a binary search restricted to them.  kPacked
 // (mixed forms): the sample and the FP32 value go to one 64-bit payload
 // (sample in the low word, value bits in the high word) that travels with
 // the key through the sort; otherwise to ex_j / ex_val.
@@ -54,7 +71,8 @@ __device__ __forceinline__ uint64_t pack_hit(uint32_t j, float v) {
 
 template <bool kPacked>
 __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t cap, const int64_t* __restrict__ f_off,
-                                  const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ rows_n,
+                                  const uint32_t* __restrict__ f_start, const uint32_t* __restrict__ first,
+                                  const uint32_t* __restrict__ rows_n,
                                   const double* __restrict__ vals_n, uint32_t* __restrict__ key,
                                   uint32_t* __restrict__ ex_j, double* __restrict__ ex_val,
                                   uint64_t* __restrict__ pay64, DeviceStatus* status) {
@@ -70,11 +88,8 @@ __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t 
     for (int64_t c = warp; c * kExpandChunk < H; c += nwarps) {
         const int64_t h0 = c * kExpandChunk;
         const int64_t h1 = min(H, h0 + kExpandChunk);
-        int64_t jlo = 0, jhi = 0;
-        if (lane == 0) jlo = owner_in(f_off, 0, ju, h0);
-        if (lane == 1) jhi = owner_in(f_off, 0, ju, h1 - 1) + 1;
-        jlo = __shfl_sync(0xffffffffu, jlo, 0);
-        jhi = __shfl_sync(0xffffffffu, jhi, 1);
+        const int64_t jlo = first[c];
+        const int64_t jhi = h1 < H ? min((int64_t)first[c + 1] + 1, ju) : ju;
         for (int64_t h = h0 + lane; h < h1; h += 32) {
             const int64_t j = owner_in(f_off, jlo, jhi, h);
             const int64_t p = (int64_t)f_start[j] + (h - f_off[j]);
@@ -452,12 +467,15 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
         set_error("packed hits need a session in a mixed precision");
         return EXAFAC_ERR_ARG;
     }
+    expand_owner_kernel<<<152 * 4, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_len, s.expand_first);
+    count_launch();
     if (packed)
-        hit_expand_kernel<true><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, L.rows, L.vals,
-                                                         s.hit_key[0], nullptr, nullptr, s.pay64[0], s.status);
+        hit_expand_kernel<true><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, s.expand_first, L.rows,
+                                                         L.vals, s.hit_key[0], nullptr, nullptr, s.pay64[0], s.status);
     else
-        hit_expand_kernel<false><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, L.rows, L.vals,
-                                                          s.hit_key[0], s.ex_j, s.ex_val, nullptr, s.status);
+        hit_expand_kernel<false><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, s.expand_first,
+                                                          L.rows, L.vals, s.hit_key[0], s.ex_j, s.ex_val, nullptr,
+                                                          s.status);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(sort_keys(s, n, packed, st));

@@ -108,8 +108,10 @@ __global__ void __launch_bounds__(256) segreduce_kernel(int R, const int64_t* __
 
 // Crossing rows, one warp per chunk c0 whose last row continues: the row's
 // carries carry_last[c0] + sum over c in (c0, c1] of carry_first[c], c1 the
-// last chunk that starts inside the row (the chunks that do form a prefix of
-// c0+1, c0+2, ..., found 32 at a time by ballot).  Spans of up to 32 chunks
+// last chunk that starts inside the row: the chunk of the row's last hit,
+// seg_start[carry_seg[c0] + 1] - 1, when the run starts are given (one load
+// however long the row); otherwise the chunks that do form a prefix of c0+1,
+// c0+2, ..., found 32 at a time by ballot.  Spans of up to 32 chunks
 // (almost every row): lane = column, chunks summed in order.  Longer spans
 // (the hot rows): lane l sums chunks c0+1+l, c0+1+l+32, ... over all 32 padded
 // columns, then a butterfly reduce-scatter leaves column l's total in lane l.
@@ -119,6 +121,7 @@ template <typename TA, int kChunk, int CB = 1>  // CB column blocks of 32 (carry
 __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64_t* __restrict__ counters, int64_t cap,
                                                      const uint32_t* __restrict__ carry_row,
                                                      const uint32_t* __restrict__ carry_seg,
+                                                     const int64_t* __restrict__ seg_start,
                                                      const uint32_t* __restrict__ keys,
                                                      const TA* __restrict__ carry_first,
                                                      const TA* __restrict__ carry_last, TA* __restrict__ Mc) {
@@ -131,20 +134,25 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
     for (int64_t c0 = warp; c0 < nchunks; c0 += nwarps) {
         const uint32_t row = carry_row[c0];
         if (row == kNoRow) continue;
-        int64_t c1 = c0;
-        for (int64_t b = c0 + 1;; b += 32) {
-            const int64_t m = b + lane;
-            const bool on = m < nchunks && keys[m * kChunk] == row;
-            const unsigned bal = __ballot_sync(full, on);
-            c1 = b + __popc(bal) - 1;
-            if (bal != full) break;
-        }
         const int64_t out = carry_seg ? (int64_t)carry_seg[c0] : (int64_t)row;
+        int64_t c1 = c0;
+        if (seg_start) {
+            c1 = (min(seg_start[out + 1], H) - 1) / kChunk;
+        } else {
+            for (int64_t b = c0 + 1;; b += 32) {
+                const int64_t m = b + lane;
+                const bool on = m < nchunks && keys[m * kChunk] == row;
+                const unsigned bal = __ballot_sync(full, on);
+                c1 = b + __popc(bal) - 1;
+                if (bal != full) break;
+            }
+        }
         if (c1 - c0 <= 32) {  // short span: column per lane, chunks in order
             for (int cb = 0; cb < CB; cb++) {
                 const int col = 32 * cb + lane;
                 if (col >= R) continue;
                 TA v = carry_last[c0 * (32 * CB) + col];
+#pragma unroll 4
                 for (int64_t m = c0 + 1; m <= c1; m++) v += carry_first[m * (32 * CB) + col];
                 Mc[out * ldm + col] = v;
             }
@@ -292,7 +300,7 @@ static void launch_exact_mttkrp(Session& s, int n, double* M, FactorPtrs f, cuda
                                                    s.vals, f, M, s.carry_first, s.carry_last, s.carry_row);
     count_launch();
     segfix_kernel<double, kSegChunk, CB><<<hb, 256, 0, st>>>(s.R, s.R, s.counters, s.nnz, s.carry_row, nullptr,
-                                                             s.key_sorted, s.carry_first, s.carry_last, M);
+                                                             nullptr, s.key_sorted, s.carry_first, s.carry_last, M);
     count_launch();
 }
 
@@ -567,7 +575,7 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
         segreduce_kernel<double, double><<<hb, 256, 0, st>>>(R, s.counters, s.nnz, s.key_sorted, s.pay_sorted, s.ex_j,
                                                              s.ex_val, (const double*)s.D, Mc, cf, cl, s.carry_row);
         count_launch();
-        segfix_kernel<double, kSegChunk><<<hb, 256, 0, st>>>(R, R, s.counters, s.nnz, s.carry_row, nullptr,
+        segfix_kernel<double, kSegChunk><<<hb, 256, 0, st>>>(R, R, s.counters, s.nnz, s.carry_row, nullptr, nullptr,
                                                              s.key_sorted, cf, cl, Mc);
         count_launch();
     } else {
@@ -593,7 +601,7 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
 #undef EXAFAC_SEG_F32
         count_launch();
         segfix_kernel<float, kSegChunkF32><<<hb, 256, 0, st>>>(R, RS, s.counters, s.nnz, s.carry_row, s.carry_seg,
-                                                               s.key_sorted, cf, cl, Mc);
+                                                               s.seg_start, s.key_sorted, cf, cl, Mc);
         count_launch();
     }
     EXAFAC_CHECK_LAUNCH();
@@ -633,13 +641,13 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
     using S = TileShape<KC>;
     __shared__ __align__(16) float phi[KC][KC];
     __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];  // at the end: the per-warp Gram slab
-    static_assert(sizeof(tile) >= sizeof(double) * kSolveWarps * (32 * 33 / 2), "slab does not fit");
+    static_assert(sizeof(tile) >= sizeof(float2) * kSolveWarps * (32 * 33 / 2), "slab does not fit");
     const int P = R * (R + 1) / 2;
     const int ldm = f32_row_stride(R);  // Mc row stride
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
         const int a = e / KC, b = e % KC;
-        phi[a][b] = (a < R && b < R) ? (float)Phi[a * R + b] : 0.0f;
+        phi[a][b] = (a < R && b < R) ? narrow_f64(Phi[a * R + b]) : 0.0f;
     }
     // this lane's lower-triangle 4x4 blocks
     int bi[S::kNB], bj[S::kNB];
@@ -722,11 +730,12 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
         }
         __syncwarp();
     }
-    // Block sum in warp order: every warp leaves its sums in its row of a slab
-    // over the (now free) tiles, each packed entry with one owner lane per
-    // warp; a thread per entry then adds the rows in order.
+    // Block sum in warp order: every warp leaves its (hi, lo) sums in its row
+    // of a slab over the (now free) tiles, each packed entry with one owner
+    // lane per warp; a thread per entry then adds the rows in order, still
+    // compensated, and widens once.
     __syncthreads();
-    double* slab = reinterpret_cast<double*>(&tile[0][0][0]);
+    float2* slab = reinterpret_cast<float2*>(&tile[0][0][0]);
 #pragma unroll
     for (int q = 0; q < S::kNB; q++) {
         if (bi[q] < 0) continue;
@@ -736,15 +745,19 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
             for (int y = 0; y < 4; y++) {
                 const int a = 4 * bi[q] + x, b = 4 * bj[q] + y;  // b's block <= a's block
                 if (a < R && b < R && b <= a)
-                    slab[w * P + packed_index(R, b, a)] = (double)ghi[q][x * 4 + y] + (double)glo[q][x * 4 + y];
+                    slab[w * P + packed_index(R, b, a)] = make_float2(ghi[q][x * 4 + y], glo[q][x * 4 + y]);
             }
     }
     __syncthreads();
     for (int e = threadIdx.x; e < P; e += blockDim.x) {
-        double acc = 0.0;
+        float hi = 0.0f, lo = 0.0f;
 #pragma unroll
-        for (int ww = 0; ww < kSolveWarps; ww++) acc += slab[ww * P + e];
-        part[(int64_t)blockIdx.x * P + e] = acc;
+        for (int ww = 0; ww < kSolveWarps; ww++) {
+            const float2 v = slab[ww * P + e];
+            two_sum_acc(hi, lo, v.x);
+            lo += v.y;
+        }
+        part[(int64_t)blockIdx.x * P + e] = widen_f32(hi) + widen_f32(lo);
     }
 }
 
@@ -771,7 +784,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
     const bool deg = *degenerate != 0;
     for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
         const int a = e / KC, b = e % KC;
-        psm[a][b] = (Pm && a < R && b < R) ? (float)Pm[a * R + b] : 0.0f;
+        psm[a][b] = (Pm && a < R && b < R) ? narrow_f64(Pm[a * R + b]) : 0.0f;
     }
     // Multiplying by fl32(1/sigma) differs from the reference's division by
     // at most two FP32 roundings.

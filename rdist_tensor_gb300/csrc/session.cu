@@ -70,6 +70,7 @@ static void carve(Session& s) {
     s.d_minj = a.take<int32_t>(s.dtab);
     s.d_count = a.take<int32_t>(s.dtab);
     s.slot_of = a.take<int32_t>(J);
+    s.dkey = a.take<Key128>(J);
     s.flags = a.take<uint32_t>(J);
     s.pos = a.take<int64_t>(J);
     s.sd = a.take<uint32_t>(J * N);
@@ -115,6 +116,7 @@ static void carve(Session& s) {
     s.carry_row = a.take<uint32_t>(chunks);
     s.carry_seg = a.take<uint32_t>(chunks);
     s.chunk_seg = a.take<uint32_t>(chunks);
+    s.expand_first = a.take<uint32_t>(ceil_div(nnz, kExpandChunk) + 1);
     if (s.cfg.precision != EXAFAC_PREC_FP64) s.Uc = a.take<float>(I * 32);
     s.rowbits = a.take<uint32_t>(ceil_div(I, 32));
     s.Df = a.take<float>(J * 32);  // rows padded to a multiple of 4 floats

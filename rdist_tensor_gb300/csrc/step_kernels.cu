@@ -35,15 +35,26 @@ static int grid_cap(int64_t work, int threads, int64_t cap = 152 * 16) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool keys_equal(Key128 a, Key128 b) { return a.lo == b.lo && a.hi == b.hi; }
 
+// Each sample's key is packed once and published (dkey[j], then a fence)
+// before the sample claims a slot, so a thread that meets the slot's owner
+// compares against the owner's stored key instead of re-packing it.
 __global__ void dedup_insert_kernel(KeySpec spec, int64_t J, const uint32_t* __restrict__ samples, int64_t mask,
-                                    int32_t* owner, int32_t* minj, int32_t* count, int32_t* __restrict__ slot_of) {
+                                    int32_t* owner, int32_t* minj, int32_t* count, int32_t* __restrict__ slot_of,
+                                    Key128* dkey) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= J) return;
     const Key128 key = pack_key(spec, samples + j * spec.N);
+    dkey[j] = key;
+    __threadfence();
     int64_t h = (int64_t)(hash_key(key) & (uint64_t)mask);
     for (int64_t probe = 0; probe <= mask; probe++) {
         int32_t o = atomicCAS(&owner[h], -1, (int32_t)j);
-        if (o == -1 || keys_equal(pack_key(spec, samples + (int64_t)o * spec.N), key)) break;
+        if (o == -1) break;
+        const volatile uint64_t* po = reinterpret_cast<const volatile uint64_t*>(&dkey[o]);
+        Key128 ko;
+        ko.lo = po[offsetof(Key128, lo) / 8];
+        ko.hi = po[offsetof(Key128, hi) / 8];
+        if (keys_equal(ko, key)) break;
         h = (h + 1) & mask;
     }
     atomicMin(&minj[h], (int32_t)j);
@@ -76,7 +87,7 @@ int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.d_count, 0, sizeof(int32_t) * s.dtab, st));
     const unsigned blocks = (unsigned)ceil_div(J, 256);
     dedup_insert_kernel<<<blocks, 256, 0, st>>>(s.look[n].spec, J, s.samples, s.dtab - 1, s.d_owner, s.d_minj,
-                                                s.d_count, s.slot_of); count_launch();
+                                                s.d_count, s.slot_of, s.dkey); count_launch();
     dedup_flag_kernel<<<blocks, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags); count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, J, s.counters + 0, s.scan_sc, st));
@@ -208,10 +219,16 @@ __global__ void design_kernel(int N, int n, int R, const int64_t* __restrict__ j
 // inputs rounded to TF32 (10-bit mantissa, round to nearest) or BF16 (7-bit)
 // on the tensor cores, accumulated in FP32 within a block of 32 rows and in
 // FP64 across blocks.
+// TF32 rounding (10 mantissa bits), to nearest with ties away from zero, in
+// integer arithmetic: adding half a TF32 ulp (bit 12) to the sign-magnitude
+// pattern and clearing the 13 dropped bits rounds the magnitude; a carry moves
+// the exponent up (to infinity past the largest TF32 value).  Infinities and
+// NaNs pass through.  Same results as cvt.rna.tf32.f32, without the
+// conversion unit.
 __device__ __forceinline__ float round_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    const uint32_t b = __float_as_uint(x);
+    if ((b & 0x7f800000u) == 0x7f800000u) return x;
+    return __uint_as_float((b + 0x1000u) & 0xffffe000u);
 }
 __device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
@@ -250,7 +267,7 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
     // the warps' tiles; at the end the per-warp Gram sums (kDesignWarps x P doubles)
     __shared__ __align__(16) float tile[kDesignWarps][32][kDStride];
     __shared__ uint32_t sidx[kDesignWarps][kMaxModes][32];  // the tile's sample indices, all modes
-    static_assert(sizeof(tile) >= sizeof(double) * kDesignWarps * (32 * 33 / 2), "slab does not fit");
+    static_assert(sizeof(tile) >= sizeof(float2) * kDesignWarps * (32 * 33 / 2), "slab does not fit");
     // lower-triangle (m-tile, n-tile) pairs of the 32 x 32 Gram: 16-row m-tiles, 8-column n-tiles
     constexpr int kPairs = 6;
     constexpr int kMt[kPairs] = {0, 0, 1, 1, 1, 1};
@@ -329,25 +346,30 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
             for (int i = 0; i < 4; i++) two_sum_acc(ghi[p][i], glo[p][i], c[p][i]);
         __syncwarp();
     }
-    // Block sum in warp order: every warp leaves its sums in its row of the
-    // slab (each packed entry has exactly one owner lane per warp), then a
-    // thread per entry adds the rows in order.
+    // Block sum in warp order: every warp leaves its (hi, lo) sums in its row
+    // of the slab (each packed entry has exactly one owner lane per warp),
+    // then a thread per entry adds the rows in order, still compensated, and
+    // widens once (no FP64 arithmetic but the final hi + lo).
     __syncthreads();
-    double* slab = reinterpret_cast<double*>(&tile[0][0][0]);
+    float2* slab = reinterpret_cast<float2*>(&tile[0][0][0]);
 #pragma unroll
     for (int p = 0; p < kPairs; p++)
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int row = 16 * kMt[p] + gid + 8 * (i >> 1);
             const int col = 8 * kNt[p] + 2 * tig + (i & 1);
-            if (row < R && col <= row) slab[w * P + packed_index(R, col, row)] = (double)ghi[p][i] + (double)glo[p][i];
+            if (row < R && col <= row) slab[w * P + packed_index(R, col, row)] = make_float2(ghi[p][i], glo[p][i]);
         }
     __syncthreads();
     for (int e = threadIdx.x; e < P; e += blockDim.x) {
-        double acc = 0.0;
+        float hi = 0.0f, lo = 0.0f;
 #pragma unroll
-        for (int ww = 0; ww < kDesignWarps; ww++) acc += slab[ww * P + e];
-        part[(int64_t)blockIdx.x * P + e] = acc;
+        for (int ww = 0; ww < kDesignWarps; ww++) {
+            const float2 v = slab[ww * P + e];
+            two_sum_acc(hi, lo, v.x);
+            lo += v.y;
+        }
+        part[(int64_t)blockIdx.x * P + e] = widen_f32(hi) + widen_f32(lo);
     }
 }
 
