@@ -23,6 +23,7 @@ constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr int64_t kExactCdfMax = 512;
 constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a power of two)
 constexpr int kExpandChunk = 256;  // hits per warp chunk in the hit expansion
+constexpr int kSortEpochSlot = 14;  // counters[] slot of the row sort's look-back epoch
 constexpr int kRngSlot = 15;              // counters[] slot of the session's Philox counter
 
 struct Slot1 {
@@ -130,8 +131,8 @@ struct Session {
     const uint32_t* pay_sorted = nullptr;       // their hit indices (FP64 form)
     uint64_t* pay64[2] = {nullptr, nullptr};    // nnz each, mixed forms: packed (sample, FP32 value) (ping-pong)
     const uint64_t* pay64_sorted = nullptr;     // the sorted packed hits (mixed forms)
-    uint32_t* hs_cnt = nullptr;       // 256 x tile stride: digit counts per tile
-    uint32_t* hs_tot = nullptr;       // 256: digit totals
+    uint64_t* os_status = nullptr;    // tile stride x 256: look-back status words of the row sort
+    uint32_t* os_aux = nullptr;       // 4 tile counters + 4 x 256 digit histograms of the row sort
     uint32_t* head_cnt = nullptr;     // chunks: touched-row starts per chunk of sorted hits
     int64_t* head_base = nullptr;     // chunks: their exclusive scan
     double* Mc = nullptr;             // Imax x R: MTTKRP rows, indexed by row

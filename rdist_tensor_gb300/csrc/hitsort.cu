@@ -6,9 +6,12 @@
 //   expand     hit h (in sample order) -> key[h] = its output row, plus the
 //              sample j and value of the hit (ex_j, ex_val; or, for the
 //              mixed forms, one packed 64-bit payload)
-//   sort       8-bit digits, per pass: per-tile digit counts (upsweep), a
-//              scan of each digit's counts across tiles (spine), a stable
-//              scatter of (key, hit index or packed hit) (downsweep)
+//   sort       8-bit digits, LSD.  One read of the keys counts every pass's
+//              digits (os_hist); then one kernel per pass (os_downsweep) ranks
+//              a tile, publishes its digit counts and resolves the counts of
+//              the tiles before it by a decoupled look-back (Merrill and
+//              Garland's single-pass scan, as in Adinets and Merrill's
+//              Onesweep), and scatters (key, hit index or packed hit) stably
 //   heads      runs of equal keys = touched rows: per-tile run counts, their
 //              scan, and the compaction into the touched list and the run
 //              starts (seg_start)
@@ -25,9 +28,14 @@ constexpr int kHsThreads = 256;
 constexpr int kHsItems = 16;
 constexpr int kHsTile = kHsThreads * kHsItems;  // 4096 hits per tile
 constexpr int kHsWarps = kHsThreads / 32;
-constexpr int kHsGrid = 152 * 4;      // upsweep / heads
-constexpr int kHsDownGrid = 152 * 2;        // downsweep: one resident wave (99 registers x 256 threads)
-constexpr int kHsDownGridPacked = 152 * 3;  // 64-bit payloads, 8 items per thread
+constexpr int kHsGrid = 152 * 4;      // heads
+constexpr int kHsDownGrid = 152 * 2;        // downsweep: one resident wave (256 threads)
+constexpr int kHsDownGridPacked = 152 * 2;  // 64-bit payloads, 16 items per thread
+constexpr int kHistGrid = 152 * 2;          // os_hist
+constexpr uint32_t kStatAgg = 1u << 30;     // look-back status: the tile's own count
+constexpr uint32_t kStatPrefix = 2u << 30;  // look-back status: the inclusive prefix
+constexpr uint32_t kStatValue = (1u << 30) - 1;
+constexpr uint32_t kSpinLimit = 1u << 22;   // look-back polls before a wait is declared failed
 constexpr uint32_t kNoItem = 0xffffffffu;
 
 __device__ __forceinline__ int64_t hit_count(const int64_t* counters, int64_t cap) { return min(counters[1], cap); }
@@ -104,18 +112,9 @@ __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t 
     }
 }
 
-// Lanes of the warp whose 9-bit value equals this lane's (the warp
-// multi-split: one ballot per bit; 256 marks an empty slot).
-__device__ __forceinline__ unsigned digit_peers(unsigned d) {
-    unsigned m = 0xffffffffu;
-#pragma unroll
-    for (int b = 0; b < 9; b++) {
-        const unsigned bit = (d >> b) & 1u;
-        const unsigned bal = __ballot_sync(0xffffffffu, bit);
-        m &= bit ? bal : ~bal;
-    }
-    return m;
-}
+// Lanes of the warp whose digit equals this lane's (the warp multi-split;
+// 256 marks an empty slot): one match instruction.
+__device__ __forceinline__ unsigned digit_peers(unsigned d) { return __match_any_sync(0xffffffffu, d); }
 
 // Inclusive warp scan.
 template <typename T>
@@ -142,109 +141,119 @@ __device__ __forceinline__ uint32_t block256_exclusive(uint32_t v, uint32_t* wsu
     return pre + inc - v;
 }
 
-// cnt[d * stride + t] = number of keys in tile t (ITEMS per thread) with digit d.
-template <int ITEMS>
-__global__ void __launch_bounds__(kHsThreads) hs_upsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
-                                                                const uint32_t* __restrict__ keys, int shift,
-                                                                uint32_t* __restrict__ cnt, int64_t stride) {
-    constexpr int kTile = kHsThreads * ITEMS;
-    __shared__ uint32_t c[256];
+// Digit counts of every pass in one read of the keys: hist[p * 256 + d] =
+// number of keys whose digit p is d (hist zeroed beforehand).  Each warp
+// counts its items by multi-split (one shared-memory add per distinct digit
+// of a round), each block adds its histograms once (aux cleared beforehand:
+// the passes' tile counters aux[0..3] and the histograms aux[4..]).  Block 0
+// also advances the look-back epoch (counters[kSortEpochSlot] += 4): every
+// pass of this sort marks its status words with a fresh epoch, so the status
+// array is never cleared.
+__global__ void __launch_bounds__(kHsThreads) os_hist_kernel(int64_t* __restrict__ counters, int64_t cap,
+                                                             const uint32_t* __restrict__ keys, int passes,
+                                                             uint32_t* __restrict__ aux) {
+    constexpr int kItems = 16;
+    constexpr int kTile = kHsThreads * kItems;
+    // per-warp histograms, so hot digits contend only within a warp
+    __shared__ uint32_t h[kHsWarps][4][256];
+    for (int e = threadIdx.x; e < kHsWarps * 4 * 256; e += blockDim.x) (&h[0][0][0])[e] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[kSortEpochSlot] += 4;
+    __syncthreads();
     const int64_t H = hit_count(counters, cap);
-    const int64_t ntiles = (H + kTile - 1) / kTile;
-    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        c[threadIdx.x] = 0;
-        __syncthreads();
-        const int64_t base = t * kTile;
-        unsigned dg[ITEMS];  // all of the thread's loads issued before the first use
+    for (int64_t base = (int64_t)blockIdx.x * kTile; base < H; base += (int64_t)gridDim.x * kTile) {
+        uint32_t k[kItems];  // all of the thread's loads in flight before the first use
+        bool on[kItems];
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) {
-            const int64_t g = base + threadIdx.x + r * kHsThreads;
-            dg[r] = g < H ? (keys[g] >> shift) & 255u : 256u;
+        for (int r = 0; r < kItems; r++) {
+            const int64_t g = base + r * kHsThreads + threadIdx.x;
+            on[r] = g < H;
+            k[r] = on[r] ? keys[g] : 0u;
         }
+        for (int p = 0; p < passes; p++) {
+            uint32_t* hw = h[w][p];
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) {
-            const unsigned d = dg[r];
-            const unsigned peers = digit_peers(d);
-            if (d < 256 && (peers & lt) == 0) atomicAdd(&c[d], (uint32_t)__popc(peers));
+            for (int r = 0; r < kItems; r++) {
+                const unsigned d = on[r] ? (k[r] >> (8 * p)) & 255u : 256u;
+                // a digit shared by the whole warp (the high digits of
+                // Zipf-distributed rows) is one add; otherwise one shared
+                // atomic per item
+                const unsigned d0 = __shfl_sync(0xffffffffu, d, 0);
+                if (__all_sync(0xffffffffu, d == d0)) {
+                    if (lane == 0 && d0 < 256) hw[d0] += 32u;
+                } else if (d < 256) {
+                    atomicAdd(&hw[d], 1u);
+                }
+            }
+            __syncwarp();
         }
-        __syncthreads();
-        cnt[(int64_t)threadIdx.x * stride + t] = c[threadIdx.x];
-        __syncthreads();
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < passes * 256; e += blockDim.x) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int ww = 0; ww < kHsWarps; ww++) v += (&h[ww][0][0])[e];
+        if (v) atomicAdd(&aux[4 + e], v);
     }
 }
 
-// Warp per digit: exclusive scan of the digit's tile counts in place (four
-// tiles per lane per round), the digit's total to tot[d].  32 blocks x 8 warps.
-template <int ITEMS>
-__global__ void hs_spine_kernel(const int64_t* __restrict__ counters, int64_t cap, uint32_t* __restrict__ cnt,
-                                int64_t stride, uint32_t* __restrict__ tot) {
-    constexpr int kTile = kHsThreads * ITEMS;
-    const int64_t H = hit_count(counters, cap);
-    const int64_t ntiles = (H + kTile - 1) / kTile;
-    const int lane = threadIdx.x & 31;
-    const int d = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (d >= 256) return;
-    uint32_t* row = cnt + (int64_t)d * stride;
-    uint32_t carry = 0;
-    for (int64_t b = 0; b < ntiles; b += 128) {
-        uint32_t v[4];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int64_t i = b + lane * 4 + k;
-            v[k] = i < ntiles ? row[i] : 0u;
-            sum += v[k];
-        }
-        const uint32_t inc = warp_inclusive(sum);
-        uint32_t run = carry + inc - sum;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int64_t i = b + lane * 4 + k;
-            if (i < ntiles) row[i] = run;
-            run += v[k];
-        }
-        carry += __shfl_sync(0xffffffffu, inc, 31);
-    }
-    if (lane == 0) tot[d] = carry;
-}
-
-// Stable scatter of (key, payload) by digit (payload PT: 32-bit hit index
-// or 64-bit packed hit).  Items of a tile are taken in
-// order warp by warp (warp w owns items [w*32*ITEMS, (w+1)*32*ITEMS) of the
-// tile, round r lane l = item w*32*ITEMS + r*32 + l); the multi-split gives each item
-// its rank among equal digits of its round, per-warp counters carry the rank
-// across rounds, and prefixes over warps and digits give its place in the
-// tile's digit order.  The tile is rearranged in shared memory first, so the
+// One pass: stable scatter of (key, payload) by digit (payload PT: 32-bit hit
+// index or 64-bit packed hit).  Blocks take tiles in order from a counter, so
+// a tile's predecessors are always held by running blocks.  Items of a tile
+// are taken warp by warp (warp w owns items [w*32*ITEMS, (w+1)*32*ITEMS) of
+// the tile, round r lane l = item w*32*ITEMS + r*32 + l); the multi-split
+// gives each item its rank among equal digits of its round, per-warp counters
+// carry the rank across rounds, and prefixes over warps and digits give its
+// place in the tile's digit order.  Thread d then publishes the tile's count
+// of digit d (status = epoch | kStatAgg | count), sums the counts of earlier
+// tiles back to the first inclusive prefix it meets, and publishes its own
+// inclusive prefix.  The tile is rearranged in shared memory first, so the
 // global writes run in contiguous pieces, one per digit.  pin == null: the
-// payload is the item's own index (the hit index of the first pass).
+// payload is the item's own index (the hit index of the first pass).  A
+// look-back wait that outlasts kSpinLimit polls records an error and counts
+// as a zero prefix (the output is then invalid, and reported).
+__device__ __forceinline__ uint64_t os_load(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void os_store(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 template <typename PT, int ITEMS>
-__global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
+__global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                                   const uint32_t* __restrict__ kin,
-                                                                  const PT* __restrict__ pin, int shift,
-                                                                  const uint32_t* __restrict__ cnt, int64_t stride,
-                                                                  const uint32_t* __restrict__ tot,
+                                                                  const PT* __restrict__ pin, int pass,
+                                                                  uint32_t* __restrict__ aux,
+                                                                  uint64_t* __restrict__ status,
                                                                   uint32_t* __restrict__ kout,
-                                                                  PT* __restrict__ pout) {
+                                                                  PT* __restrict__ pout, DeviceStatus* err) {
     extern __shared__ __align__(16) unsigned char hs_dyn[];  // payloads, then keys, of one tile
     constexpr int kTile = kHsThreads * ITEMS;
     PT* spay = reinterpret_cast<PT*>(hs_dyn);
     uint32_t* skey = reinterpret_cast<uint32_t*>(hs_dyn + sizeof(PT) * kTile);
     __shared__ uint32_t whist[kHsWarps][256];
-    __shared__ uint32_t dbase[256];  // digit start in the whole output
+    __shared__ uint32_t dbase[256];   // digit start in the whole output
     __shared__ uint32_t tstart[256];  // digit start within the tile
     __shared__ uint32_t gbase[256];   // digit start of this tile in the output
     __shared__ uint32_t wsum[kHsWarps];
+    __shared__ int64_t tile_sh;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    dbase[threadIdx.x] = block256_exclusive(tot[threadIdx.x], wsum);
+    const int shift = 8 * pass;
+    const uint64_t epoch = (uint64_t)(uint32_t)(counters[kSortEpochSlot] + pass) << 32;
+    dbase[threadIdx.x] = block256_exclusive(aux[4 + pass * 256 + threadIdx.x], wsum);
     const int64_t H = hit_count(counters, cap);
     const int64_t ntiles = (H + kTile - 1) / kTile;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (;;) {
+        if (threadIdx.x == 0) tile_sh = (int64_t)atomicAdd(&aux[pass], 1u);
 #pragma unroll
         for (int ww = 0; ww < kHsWarps; ww++) whist[ww][threadIdx.x] = 0;
         __syncthreads();
+        const int64_t t = tile_sh;
+        if (t >= ntiles) break;  // uniform
         const int64_t tile0 = t * kTile;
         const int64_t base = tile0 + (int64_t)w * 32 * ITEMS;
         uint32_t kk[ITEMS];
@@ -282,9 +291,45 @@ __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t*
                 whist[ww][d] = run;
                 run += c;
             }
+            // publish this tile's count, then look back for the prefix
+            uint64_t* my = status + t * 256 + d;
+            uint32_t excl = 0;
+            if (t == 0) {
+                os_store(my, epoch | kStatPrefix | run);
+            } else {
+                os_store(my, epoch | kStatAgg | run);
+                // windows of kLook predecessors: their status words are loaded
+                // together, then taken in order back to the first prefix
+                constexpr int kLook = 4;
+                bool done = false;
+                for (int64_t top = t - 1; top >= 0 && !done; top -= kLook) {
+                    uint64_t v[kLook];
+#pragma unroll
+                    for (int q = 0; q < kLook; q++) v[q] = top - q >= 0 ? os_load(status + (top - q) * 256 + d) : 0;
+#pragma unroll
+                    for (int q = 0; q < kLook; q++) {
+                        if (done || top - q < 0) continue;
+                        const uint64_t* src = status + (top - q) * 256 + d;
+                        uint64_t x = v[q];
+                        for (uint32_t it = 0; (x & 0xffffffff00000000ull) != epoch; it++) {
+                            // give up after kSpinLimit polls, or at once when another wait already did
+                            if (it >= kSpinLimit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
+                                report(err, EXAFAC_ERR_DEVICE, 9, top - q, t);
+                                x = epoch | kStatPrefix;
+                                break;
+                            }
+                            if (it >= 32) __nanosleep(64);
+                            x = os_load(src);
+                        }
+                        excl += (uint32_t)x & kStatValue;
+                        done = ((uint32_t)x & kStatPrefix) != 0;
+                    }
+                }
+                os_store(my, epoch | kStatPrefix | (excl + run));
+            }
             const uint32_t ts = block256_exclusive(run, wsum);
             tstart[d] = ts;
-            gbase[d] = dbase[d] + cnt[(int64_t)d * stride + t];
+            gbase[d] = dbase[d] + excl;
         }
         __syncthreads();
 #pragma unroll
@@ -302,8 +347,10 @@ __global__ void __launch_bounds__(kHsThreads) hs_downsweep_kernel(const int64_t*
             const uint32_t k = skey[i];
             const unsigned d = (k >> shift) & 255u;
             const uint32_t dst = gbase[d] + ((uint32_t)i - tstart[d]);
-            kout[dst] = k;
-            pout[dst] = spay[i];
+            if (dst < (uint64_t)H) {  // always, unless a failed look-back (reported) broke the prefixes
+                kout[dst] = k;
+                pout[dst] = spay[i];
+            }
         }
         __syncthreads();
     }
@@ -407,7 +454,7 @@ __global__ void __launch_bounds__(1024) hs_headscan_kernel(const int64_t* __rest
     }
 }
 
-constexpr int kHsItemsPacked = 8;  // 64-bit payloads: smaller tiles keep 3 blocks per SM resident
+constexpr int kHsItemsPacked = 16;  // 64-bit payloads: 4096-hit tiles, 2 blocks per SM
 
 size_t hitsort_tile_stride(int64_t nnz) {
     return (size_t)ceil_div(std::max<int64_t>(nnz, 1), kHsThreads * kHsItemsPacked);
@@ -423,32 +470,30 @@ static int key_bits(int64_t I) {
 // the packed hits in pay64[0].  Leaves key_sorted / pay_sorted / pay64_sorted.
 static int sort_keys(Session& s, int n, bool packed, cudaStream_t st) {
     const int64_t cap = s.nnz;
+    if (cap >= ((int64_t)1 << 30)) {
+        set_error("the row sort holds hit counts in 30 bits: at most 2^30 - 1 nonzeros");
+        return EXAFAC_ERR_ARG;
+    }
     const int passes = std::max(1, (key_bits(s.dims[n]) + 7) / 8);
-    const int64_t stride = (int64_t)hitsort_tile_stride(s.nnz);
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.os_aux, 0, sizeof(uint32_t) * (4 + 4 * 256), st));
+    os_hist_kernel<<<kHistGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[0], passes, s.os_aux);
+    count_launch();
     int src = 0;
     for (int p = 0; p < passes; p++) {
         const int dst = src ^ 1;
         if (packed) {
             constexpr int IT = kHsItemsPacked;
-            hs_upsweep_kernel<IT><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[src], 8 * p, s.hs_cnt,
-                                                                 stride);
-            count_launch();
-            hs_spine_kernel<IT><<<32, 256, 0, st>>>(s.counters, cap, s.hs_cnt, stride, s.hs_tot);
-            count_launch();
             const size_t smem = (sizeof(uint64_t) + sizeof(uint32_t)) * kHsThreads * IT;
-            hs_downsweep_kernel<uint64_t, IT><<<kHsDownGridPacked, kHsThreads, smem, st>>>(
-                s.counters, cap, s.hit_key[src], s.pay64[src], 8 * p, s.hs_cnt, stride, s.hs_tot, s.hit_key[dst],
-                s.pay64[dst]);
+            EXAFAC_CUDA_TRY(cudaFuncSetAttribute(os_downsweep_kernel<uint64_t, IT>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            os_downsweep_kernel<uint64_t, IT><<<kHsDownGridPacked, kHsThreads, smem, st>>>(
+                s.counters, cap, s.hit_key[src], s.pay64[src], p, s.os_aux, s.os_status, s.hit_key[dst], s.pay64[dst],
+                s.status);
         } else {
-            hs_upsweep_kernel<kHsItems><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[src], 8 * p,
-                                                                       s.hs_cnt, stride);
-            count_launch();
-            hs_spine_kernel<kHsItems><<<32, 256, 0, st>>>(s.counters, cap, s.hs_cnt, stride, s.hs_tot);
-            count_launch();
             const size_t smem = (sizeof(uint32_t) + sizeof(uint32_t)) * kHsTile;
-            hs_downsweep_kernel<uint32_t, kHsItems><<<kHsDownGrid, kHsThreads, smem, st>>>(
-                s.counters, cap, s.hit_key[src], p == 0 ? nullptr : s.hit_pay[src], 8 * p, s.hs_cnt, stride, s.hs_tot,
-                s.hit_key[dst], s.hit_pay[dst]);
+            os_downsweep_kernel<uint32_t, kHsItems><<<kHsDownGrid, kHsThreads, smem, st>>>(
+                s.counters, cap, s.hit_key[src], p == 0 ? nullptr : s.hit_pay[src], p, s.os_aux, s.os_status,
+                s.hit_key[dst], s.hit_pay[dst], s.status);
         }
         count_launch();
         EXAFAC_CHECK_LAUNCH();

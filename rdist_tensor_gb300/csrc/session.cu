@@ -101,8 +101,8 @@ static void carve(Session& s) {
         s.hit_pay[b] = a.take<uint32_t>(nnz);
         if (s.cfg.precision != EXAFAC_PREC_FP64) s.pay64[b] = a.take<uint64_t>(nnz);
     }
-    s.hs_cnt = a.take<uint32_t>(256 * (int64_t)hitsort_tile_stride(nnz));
-    s.hs_tot = a.take<uint32_t>(256);
+    s.os_status = a.take<uint64_t>(256 * (int64_t)hitsort_tile_stride(nnz));
+    s.os_aux = a.take<uint32_t>(4 + 4 * 256);
     s.Mc = a.take<double>(I * std::max(R, 16));  // FP64 rows of R, or FP32 rows padded to a multiple of 4
     const int64_t chunks = ceil_div(nnz, kSegChunkF32) + 1;
     s.head_cnt = a.take<uint32_t>(chunks);
@@ -354,6 +354,8 @@ extern "C" int exafac_als_init(exafac_als_t h, const uint32_t* idx, const double
     s.F = *F;
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.status, 0, sizeof(DeviceStatus), st));
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.counters, 0, sizeof(int64_t) * 16, st));
+    // look-back status words carry an epoch (counters[kSortEpochSlot]); both start at zero
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.os_status, 0, sizeof(uint64_t) * 256 * hitsort_tile_stride(s.nnz), st));
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.dims_dev, s.dims, sizeof(int64_t) * kMaxModes, cudaMemcpyHostToDevice, st));
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.idx, idx, sizeof(uint32_t) * s.nnz * s.N, cudaMemcpyDeviceToDevice, st));
     EXAFAC_TRY(preprocess_values(s, vals, st));
