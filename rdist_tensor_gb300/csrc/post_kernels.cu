@@ -10,8 +10,10 @@
 //            thread per row over 32-row tiles, Gram partials of U in registers
 //   normlev  u_r = U_r / sigma (renormalize_columns, distmat.hpp:85-138) and,
 //            for CP-ARLS-LEV, l_r = u_r^T P u_r (compute_DAGAT, common.h:727-746)
+#include "bulk.cuh"
 #include "dense.cuh"
 #include "engine.cuh"
+#include "mma.cuh"
 #include "prims.cuh"
 
 namespace exafac {
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __res
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const uint32_t jt = __shfl_sync(gmask, hj[b / 8], u, 8);
-                d[u] = (b + u < n && col) ? D4[(int64_t)jt * Q + sub] : zero4;
+                d[u] = (b + u < n && col) ? D4[(int64_t)jt * 8 + sub] : zero4;  // 128-byte rows
             }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
@@ -560,6 +562,7 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
 // Host side
 // ---------------------------------------------------------------------------
 constexpr int kSolveBlocks = 152 * 2;
+constexpr int kNormlevBlocks = 152 * 4;  // no per-block partials: four resident blocks per SM (64 registers)
 
 // MTTKRP rows of the touched rows into Mc: FP64 rows of R indexed by row
 // (TA = double), or compact FP32 rows of f32_row_stride(R) floats indexed by
@@ -623,136 +626,218 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
 //     block's warps in warp
 //     order (reproducible).
 // ---------------------------------------------------------------------------
-constexpr int kTileStride = 36;  // floats per staged row (16-byte aligned rows)
+
+// The FP32 solve on the tensor cores: per 32-row tile of compact M rows,
+// U = M Phi and the tile's Gram U^T U as mma.sync m16n8k8 products in 3xTF32
+// (each operand split as hi + lo, products hi*hi + hi*lo + lo*hi with FP32
+// accumulation: about 2^-21 relative, near FP32's own rounding), the Gram
+// summed over a warp's tiles in compensated FP32 and over the block's warps
+// in warp order (reproducible).  A warp owns a tile at a time:
+//   * the M tile (32 compact rows, contiguous) arrives by one bulk copy into
+//     Mbuf, rows of ldm floats as in Mc, the next tile's copy being issued as
+//     soon as this tile's M has been read (columns past ldm of a fragment
+//     are masked to zero);
+//   * U goes to two tiles, Th = TF32(U) and Tl = U - Th (exact), which hold
+//     the Gram's operands ready-split and give U back as Th + Tl for Uc.
+// Mbuf rows are ldm floats (the A-fragment loads are conflict-free when
+// ldm / 4 is odd, e.g. 28); Th and Tl rows are 8 KT + 4 floats.  Phi is held
+// split (hi, lo) with rows of 8 KT + 8 floats, for conflict-free B-fragment
+// loads.
+constexpr int kMmaWarps = 4;
+constexpr int kMmaBlocks = 152 * 3;
 
 template <int KC>
-struct TileShape {
-    static constexpr int kBlk = KC / 4;                        // 4-column blocks per side
-    static constexpr int kTri = kBlk * (kBlk + 1) / 2;         // lower-triangle blocks
-    static constexpr int kNB = (kTri + 31) / 32;               // blocks per lane
+struct MmaShape {
+    static constexpr int KT = (KC + 7) / 8;       // k-steps of the product and its n-tiles (8 KT >= R)
+    static constexpr int GM = (KC + 15) / 16;     // 16-row m-tiles of the Gram
+    static constexpr int kPairs = GM == 1 ? 2 : 6;  // lower-triangle (m-tile, n-tile) blocks of the Gram
+    static constexpr int kStride = 8 * KT + 4;
+    static constexpr int kPhiStride = 8 * KT + 8;
+    static constexpr size_t kTileBytes = sizeof(float) * 32 * kStride;
+    static constexpr size_t kWarpBytes = 3 * kTileBytes;  // Mbuf, Th, Tl
+    static constexpr size_t kSmem = kMmaWarps * kWarpBytes + 2 * sizeof(float) * (8 * KT) * kPhiStride;
 };
 
 template <int KC>
-__global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R, const int64_t* __restrict__ counters,
-                                                                         const float* __restrict__ Mc,
-                                                                         const double* __restrict__ Phi,
-                                                                         float* __restrict__ Uc,
-                                                                         double* __restrict__ part) {
-    using S = TileShape<KC>;
-    __shared__ __align__(16) float phi[KC][KC];
-    __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];  // at the end: the per-warp Gram slab
-    static_assert(sizeof(tile) >= sizeof(float2) * kSolveWarps * (32 * 33 / 2), "slab does not fit");
-    const int P = R * (R + 1) / 2;
-    const int ldm = f32_row_stride(R);  // Mc row stride
+__global__ void __launch_bounds__(kMmaWarps * 32) solve_gram_mma_kernel(int R, const int64_t* __restrict__ counters,
+                                                                        const float* __restrict__ Mc,
+                                                                        const double* __restrict__ Phi,
+                                                                        float* __restrict__ Uc,
+                                                                        double* __restrict__ part,
+                                                                        DeviceStatus* err) {
+    using S = MmaShape<KC>;
+    constexpr int KT = S::KT, TS = S::kStride, PS = S::kPhiStride, KP = 8 * KT;
+    extern __shared__ __align__(128) unsigned char mma_dyn[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
-        const int a = e / KC, b = e % KC;
-        phi[a][b] = (a < R && b < R) ? narrow_f64(Phi[a * R + b]) : 0.0f;
+    const int gid = lane >> 2, tig = lane & 3;
+    float* Mbuf = reinterpret_cast<float*>(mma_dyn + w * S::kWarpBytes);  // rows of ldm floats
+    float (*Th)[TS] = reinterpret_cast<float (*)[TS]>(mma_dyn + w * S::kWarpBytes + S::kTileBytes);
+    float (*Tl)[TS] = reinterpret_cast<float (*)[TS]>(mma_dyn + w * S::kWarpBytes + 2 * S::kTileBytes);
+    float (*phh)[PS] = reinterpret_cast<float (*)[PS]>(mma_dyn + kMmaWarps * S::kWarpBytes);
+    float (*phl)[PS] = phh + KP;
+    __shared__ __align__(8) uint64_t bars[kMmaWarps];
+    const int P = R * (R + 1) / 2;
+    const int ldm = f32_row_stride(R);  // Mc / Uc row stride
+    const uint32_t row_bytes = (uint32_t)(sizeof(float) * ldm);
+    for (int e = threadIdx.x; e < KP * KP; e += blockDim.x) {
+        const int a = e / KP, b = e % KP;
+        const float x = (a < R && b < R) ? narrow_f64(Phi[a * R + b]) : 0.0f;
+        uint32_t hi, lo;
+        split_tf32(x, hi, lo);
+        phh[a][b] = __uint_as_float(hi);
+        phl[a][b] = __uint_as_float(lo);
     }
-    // this lane's lower-triangle 4x4 blocks
-    int bi[S::kNB], bj[S::kNB];
-#pragma unroll
-    for (int q = 0; q < S::kNB; q++) {
-        int blk = lane + 32 * q, i = 0;
-        while (blk > i) {
-            blk -= i + 1;
-            i++;
-        }
-        bi[q] = (lane + 32 * q < S::kTri) ? i : -1;
-        bj[q] = blk;
+    {  // zero the warp's tiles once
+        float* z = Mbuf;
+        for (int e = lane; e < 3 * 32 * TS; e += 32) z[e] = 0.0f;
     }
-    float ghi[S::kNB][16], glo[S::kNB][16];  // compensated sums over the warp's tiles
-#pragma unroll
-    for (int q = 0; q < S::kNB; q++)
-#pragma unroll
-        for (int x = 0; x < 16; x++) ghi[q][x] = glo[q][x] = 0.0f;
+    if (lane == 0) mbar_init(&bars[w], 1);
+    fence_proxy_async_smem();
     __syncthreads();
-    float (*t)[kTileStride] = tile[w];
     const int64_t nt = counters[2];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t base = warp * 32; base < nt; base += nwarps * 32) {
+    auto issue = [&](int64_t b) {  // one copy of the tile's nr contiguous rows
+        const int nr = (int)min((int64_t)32, nt - b);
+        if (lane == 0) {
+            mbar_arrive_expect_tx(&bars[w], row_bytes * (uint32_t)nr);
+            bulk_g2s(Mbuf, Mc + b * ldm, row_bytes * (uint32_t)nr, &bars[w]);
+        }
+    };
+    float ghi[S::kPairs][4], glo[S::kPairs][4];  // compensated sums over the warp's tiles
+#pragma unroll
+    for (int p = 0; p < S::kPairs; p++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) ghi[p][i] = glo[p][i] = 0.0f;
+    uint32_t phase = 0;
+    int64_t base = warp * 32;
+    if (base < nt) issue(base);
+    for (; base < nt; base += nwarps * 32) {
         const int nrow = (int)min((int64_t)32, nt - base);
-        float v[32];  // stage M rows (compact: the tile is one contiguous block), zero padding
-#pragma unroll
-        for (int r = 0; r < 32; r++) v[r] = (r < nrow && lane < R) ? Mc[(base + r) * ldm + lane] : 0.0f;
-#pragma unroll
-        for (int r = 0; r < 32; r++)
-            if (lane < KC) t[r][lane] = v[r];
-        __syncwarp();
-        float m[KC], u[KC];
-#pragma unroll
-        for (int c = 0; c < KC; c += 4) {
-            const float4 v = *reinterpret_cast<const float4*>(&t[lane][c]);
-            m[c] = v.x;
-            m[c + 1] = v.y;
-            m[c + 2] = v.z;
-            m[c + 3] = v.w;
-            u[c] = u[c + 1] = u[c + 2] = u[c + 3] = 0.0f;
+        if (!mbar_wait(&bars[w], phase)) {  // (the block still meets its barriers)
+            if (lane == 0) report(err, EXAFAC_ERR_DEVICE, 10, base, nt);
+            break;
         }
+        phase ^= 1u;
+        for (int e = nrow * ldm + lane; e < 32 * ldm; e += 32) Mbuf[e] = 0.0f;  // rows past a short tile's end
+        __syncwarp();
+        // U = M Phi
+        float acc[2][KT][4];
 #pragma unroll
-        for (int k = 0; k < KC; k++) {
-            if (k < R) {
+        for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-                for (int c = 0; c < KC; c += 4) {
-                    const float4 p = *reinterpret_cast<const float4*>(&phi[k][c]);
-                    u[c] = fmaf(m[k], p.x, u[c]);
-                    u[c + 1] = fmaf(m[k], p.y, u[c + 1]);
-                    u[c + 2] = fmaf(m[k], p.z, u[c + 2]);
-                    u[c + 3] = fmaf(m[k], p.w, u[c + 3]);
+            for (int nt8 = 0; nt8 < KT; nt8++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) acc[mt][nt8][i] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < KT; ks++) {
+            uint32_t ah[2][4], al[2][4];
+            const int c0 = 8 * ks + tig, c1 = c0 + 4;  // columns; past ldm they read the next row: masked
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                const float* r0 = Mbuf + (16 * mt + gid) * ldm;
+                const float* r1 = r0 + 8 * ldm;
+                split_tf32(c0 < ldm ? r0[c0] : 0.0f, ah[mt][0], al[mt][0]);
+                split_tf32(c0 < ldm ? r1[c0] : 0.0f, ah[mt][1], al[mt][1]);
+                split_tf32(c1 < ldm ? r0[c1] : 0.0f, ah[mt][2], al[mt][2]);
+                split_tf32(c1 < ldm ? r1[c1] : 0.0f, ah[mt][3], al[mt][3]);
+            }
+#pragma unroll
+            for (int nt8 = 0; nt8 < KT; nt8++) {
+                const uint32_t bh[2] = {__float_as_uint(phh[8 * ks + tig][8 * nt8 + gid]),
+                                        __float_as_uint(phh[8 * ks + tig + 4][8 * nt8 + gid])};
+                const uint32_t bl[2] = {__float_as_uint(phl[8 * ks + tig][8 * nt8 + gid]),
+                                        __float_as_uint(phl[8 * ks + tig + 4][8 * nt8 + gid])};
+#pragma unroll
+                for (int mt = 0; mt < 2; mt++) {
+                    mma_tf32_16x8x8(acc[mt][nt8], al[mt], bh);
+                    mma_tf32_16x8x8(acc[mt][nt8], ah[mt], bl);
+                    mma_tf32_16x8x8(acc[mt][nt8], ah[mt], bh);
                 }
             }
         }
+        __syncwarp();  // the M tile is consumed: the next tile's copies may land
+        if (base + nwarps * 32 < nt) {
+            fence_proxy_async_smem();
+            issue(base + nwarps * 32);
+        }
 #pragma unroll
-        for (int c = 0; c < KC; c += 4)
-            *reinterpret_cast<float4*>(&t[lane][c]) = make_float4(u[c], u[c + 1], u[c + 2], u[c + 3]);
-        __syncwarp();
-        for (int r = 0; r < nrow; r++)  // store the solved rows, compact
-            if (lane < ldm) Uc[(base + r) * ldm + lane] = t[r][lane];
+        for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-        for (int q = 0; q < S::kNB; q++) {
-            if (bi[q] >= 0) {
-                float g[16];
+            for (int nt8 = 0; nt8 < KT; nt8++)
 #pragma unroll
-                for (int x = 0; x < 16; x++) g[x] = 0.0f;
-                for (int r = 0; r < 32; r++) {
-                    const float4 a = *reinterpret_cast<const float4*>(&t[r][4 * bi[q]]);
-                    const float4 b = *reinterpret_cast<const float4*>(&t[r][4 * bj[q]]);
-                    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-                    for (int x = 0; x < 4; x++)
-#pragma unroll
-                        for (int y = 0; y < 4; y++) g[x * 4 + y] = fmaf(av[x], bv[y], g[x * 4 + y]);
+                for (int i = 0; i < 4; i++) {
+                    const int row = 16 * mt + gid + 8 * (i >> 1), col = 8 * nt8 + 2 * tig + (i & 1);
+                    uint32_t hi, lo;
+                    split_tf32(acc[mt][nt8][i], hi, lo);
+                    Th[row][col] = __uint_as_float(hi);
+                    Tl[row][col] = __uint_as_float(lo);
                 }
+        __syncwarp();
+        for (int r = 0; r < nrow; r++)  // the solved rows, compact (hi + lo = U exactly)
+            if (lane < ldm) Uc[(base + r) * ldm + lane] = Th[r][lane] + Tl[r][lane];
+        // the tile's Gram: A = U^T (rows = columns of U), B = U, K = the 32 rows
+        float g[S::kPairs][4];
 #pragma unroll
-                for (int x = 0; x < 16; x++) two_sum_acc(ghi[q][x], glo[q][x], g[x]);
+        for (int p = 0; p < S::kPairs; p++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) g[p][i] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+            const int k0 = 8 * ks + tig;
+            uint32_t ah[S::GM][4], al[S::GM][4], bh[2 * S::GM][2], bl[2 * S::GM][2];
+#pragma unroll
+            for (int mt = 0; mt < S::GM; mt++) {
+                ah[mt][0] = __float_as_uint(Th[k0][16 * mt + gid]);
+                ah[mt][1] = __float_as_uint(Th[k0][16 * mt + gid + 8]);
+                ah[mt][2] = __float_as_uint(Th[k0 + 4][16 * mt + gid]);
+                ah[mt][3] = __float_as_uint(Th[k0 + 4][16 * mt + gid + 8]);
+                al[mt][0] = __float_as_uint(Tl[k0][16 * mt + gid]);
+                al[mt][1] = __float_as_uint(Tl[k0][16 * mt + gid + 8]);
+                al[mt][2] = __float_as_uint(Tl[k0 + 4][16 * mt + gid]);
+                al[mt][3] = __float_as_uint(Tl[k0 + 4][16 * mt + gid + 8]);
+            }
+#pragma unroll
+            for (int nt8 = 0; nt8 < 2 * S::GM; nt8++) {
+                bh[nt8][0] = __float_as_uint(Th[k0][8 * nt8 + gid]);
+                bh[nt8][1] = __float_as_uint(Th[k0 + 4][8 * nt8 + gid]);
+                bl[nt8][0] = __float_as_uint(Tl[k0][8 * nt8 + gid]);
+                bl[nt8][1] = __float_as_uint(Tl[k0 + 4][8 * nt8 + gid]);
+            }
+#pragma unroll
+            for (int p = 0; p < S::kPairs; p++) {
+                const int mt = p < 2 ? 0 : 1, nt8 = p < 2 ? p : p - 2;
+                mma_tf32_16x8x8(g[p], al[mt], bh[nt8]);
+                mma_tf32_16x8x8(g[p], ah[mt], bl[nt8]);
+                mma_tf32_16x8x8(g[p], ah[mt], bh[nt8]);
             }
         }
+#pragma unroll
+        for (int p = 0; p < S::kPairs; p++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) two_sum_acc(ghi[p][i], glo[p][i], g[p][i]);
         __syncwarp();
     }
     // Block sum in warp order: every warp leaves its (hi, lo) sums in its row
-    // of a slab over the (now free) tiles, each packed entry with one owner
+    // of a slab over the (now idle) tiles, each packed entry with one owner
     // lane per warp; a thread per entry then adds the rows in order, still
     // compensated, and widens once.
     __syncthreads();
-    float2* slab = reinterpret_cast<float2*>(&tile[0][0][0]);
+    float2* slab = reinterpret_cast<float2*>(mma_dyn);
+    static_assert(kMmaWarps * S::kWarpBytes >= sizeof(float2) * kMmaWarps * (KC * (KC + 1) / 2), "slab");
 #pragma unroll
-    for (int q = 0; q < S::kNB; q++) {
-        if (bi[q] < 0) continue;
+    for (int p = 0; p < S::kPairs; p++)
 #pragma unroll
-        for (int x = 0; x < 4; x++)
-#pragma unroll
-            for (int y = 0; y < 4; y++) {
-                const int a = 4 * bi[q] + x, b = 4 * bj[q] + y;  // b's block <= a's block
-                if (a < R && b < R && b <= a)
-                    slab[w * P + packed_index(R, b, a)] = make_float2(ghi[q][x * 4 + y], glo[q][x * 4 + y]);
-            }
-    }
+        for (int i = 0; i < 4; i++) {
+            const int mt = p < 2 ? 0 : 1, nt8 = p < 2 ? p : p - 2;
+            const int row = 16 * mt + gid + 8 * (i >> 1), col = 8 * nt8 + 2 * tig + (i & 1);
+            if (row < R && col <= row) slab[w * P + packed_index(R, col, row)] = make_float2(ghi[p][i], glo[p][i]);
+        }
     __syncthreads();
     for (int e = threadIdx.x; e < P; e += blockDim.x) {
         float hi = 0.0f, lo = 0.0f;
 #pragma unroll
-        for (int ww = 0; ww < kSolveWarps; ww++) {
+        for (int ww = 0; ww < kMmaWarps; ww++) {
             const float2 v = slab[ww * P + e];
             two_sum_acc(hi, lo, v.x);
             lo += v.y;
@@ -761,14 +846,18 @@ __global__ void __launch_bounds__(kSolveWarps * 32) solve_gram_f32_kernel(int R,
     }
 }
 
-// u_r = Uc_r / sigma (Uc: the compact rows of solve_gram_f32_kernel) written
+// u_r = Uc_r / sigma (Uc: the compact rows of solve_gram_mma_kernel) written
 // to U at the touched row, and, when P != null, l_r = u_r^T P u_r in FP32;
-// rows staged as in solve_gram_f32_kernel.  This is the one scattered pass
-// over the factor.  The scaling runs in FP32 (u = Uc * fl32(1 / sigma)) and
-// the result is widened to FP64 exactly, so no element goes through the FP64
-// pipe.
+// rows staged in shared memory, 32 per warp.  This is the one scattered pass
+// over the factor.  The scaling runs in FP32 (u = Uc * fl32(1 / sigma)); the
+// result is widened to FP64 by the hardware conversion, one FP64-pipe
+// operation per element: this kernel is bound by instruction issue, and the
+// conversions' FP64-pipe time stays well below its run time (the integer
+// widening would cost seven issue slots).
+constexpr int kTileStride = 36;  // floats per staged row of normlev_f32_kernel (16-byte aligned rows)
+
 template <int KC>
-__global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, const int64_t* __restrict__ counters,
+__global__ void __launch_bounds__(kSolveWarps * 32, 4) normlev_f32_kernel(int R, const int64_t* __restrict__ counters,
                                                                       const uint32_t* __restrict__ touched,
                                                                       const float* __restrict__ Uc,
                                                                       const double* __restrict__ sigma,
@@ -784,7 +873,8 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
     const bool deg = *degenerate != 0;
     for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
         const int a = e / KC, b = e % KC;
-        psm[a][b] = (Pm && a < R && b < R) ? narrow_f64(Pm[a * R + b]) : 0.0f;
+        // upper triangle, off-diagonal entries doubled (u^T P u with P symmetric)
+        psm[a][b] = (Pm && a < R && b < R && b >= a) ? narrow_f64((b == a ? 1.0 : 2.0) * Pm[a * R + b]) : 0.0f;
     }
     // Multiplying by fl32(1/sigma) differs from the reference's division by
     // at most two FP32 roundings.
@@ -818,7 +908,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
             int r = lane / R, c = lane % R;
             for (int e = lane; e < 32 * R; e += 32) {
                 const float y = t[r][c] * sg[c];
-                blk[e] = widen_f32(y);
+                blk[e] = (double)y;
                 t[r][c] = y;
                 c += 32;
                 while (c >= R) {
@@ -832,7 +922,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
                 const int64_t row = __shfl_sync(0xffffffffu, myrow, r);
                 if (lane < KC) {
                     const float y = t[r][lane] * sgl;
-                    if (lane < R) U[row * R + lane] = widen_f32(y);
+                    if (lane < R) U[row * R + lane] = (double)y;
                     t[r][lane] = y;
                 }
             }
@@ -848,13 +938,16 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
                 u[c + 2] = v.z;
                 u[c + 3] = v.w;
             }
+            // u^T P u over the upper triangle: psm holds P_aa on the diagonal,
+            // 2 P_ac above it and zeros below, so row a needs only the
+            // 4-column groups from a's own onwards
             float acc = 0.0f;
 #pragma unroll
             for (int a = 0; a < KC; a++) {
                 if (a < R) {
                     float y = 0.0f;
 #pragma unroll
-                    for (int c = 0; c < KC; c += 4) {
+                    for (int c = (a / 4) * 4; c < KC; c += 4) {
                         const float4 p = *reinterpret_cast<const float4*>(&psm[a][c]);
                         y = fmaf(p.x, u[c], y);
                         y = fmaf(p.y, u[c + 1], y);
@@ -864,21 +957,25 @@ __global__ void __launch_bounds__(kSolveWarps * 32) normlev_f32_kernel(int R, co
                     acc = fmaf(u[a], y, acc);
                 }
             }
-            scores[myrow] = widen_f32(acc);
+            scores[myrow] = (double)acc;
         }
         __syncwarp();
     }
 }
 
 template <int KC>
-static void launch_solve_f32(Session& s, int n, cudaStream_t st) {
-    solve_gram_f32_kernel<KC><<<kSolveBlocks, kSolveWarps * 32, 0, st>>>(
-        s.R, s.counters, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.Uc, s.part);
+static int launch_solve_f32(Session& s, int n, cudaStream_t st) {
+    const size_t smem = MmaShape<KC>::kSmem;
+    EXAFAC_CUDA_TRY(
+        cudaFuncSetAttribute(solve_gram_mma_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    solve_gram_mma_kernel<KC><<<kMmaBlocks, kMmaWarps * 32, smem, st>>>(
+        s.R, s.counters, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.Uc, s.part, s.status);
+    return EXAFAC_OK;
 }
 
 template <int KC>
 static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
-    normlev_f32_kernel<KC><<<kSolveBlocks, kSolveWarps * 32, 0, st>>>(
+    normlev_f32_kernel<KC><<<kNormlevBlocks, kSolveWarps * 32, 0, st>>>(
         s.R, s.counters, s.touched, s.Uc, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
         s.F.U[n], arls ? s.scores[n] : nullptr);
 }
@@ -886,9 +983,9 @@ static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
 static int solve_f32(Session& s, int n, cudaStream_t st) {
     EXAFAC_TRY(segmented_mttkrp<float>(s, st));
     EXAFAC_TRY(zero_factor_rows(s, n, st));
-    if (s.R <= 16) launch_solve_f32<16>(s, n, st);
-    else if (s.R <= 28) launch_solve_f32<28>(s, n, st);
-    else launch_solve_f32<32>(s, n, st);
+    if (s.R <= 16) EXAFAC_TRY(launch_solve_f32<16>(s, n, st));
+    else if (s.R <= 28) EXAFAC_TRY(launch_solve_f32<28>(s, n, st));
+    else EXAFAC_TRY(launch_solve_f32<32>(s, n, st));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
@@ -942,7 +1039,7 @@ int mttkrp_solve_balanced(Session& s, int n, cudaStream_t st) {
 int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st) {
     if (s.cfg.precision == EXAFAC_PREC_FP64) return normalize_typed<double>(s, n, arls, st);
     const int R = s.R;
-    EXAFAC_TRY(gram_reduce_to(s, kSolveBlocks, s.ugram, st));
+    EXAFAC_TRY(gram_reduce_to(s, kMmaBlocks, s.ugram, st));
     EXAFAC_TRY(sigma_and_gram(s, st));
     if (arls) EXAFAC_TRY(launch_pinv_leverage_f32(R, s.ngram, s.upinv, 1e-11, s.vt, st));
     if (R <= 16) launch_normlev_f32<16>(s, n, arls, st);

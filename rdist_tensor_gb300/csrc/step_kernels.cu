@@ -6,6 +6,7 @@
 
 #include "dense.cuh"
 #include "engine.cuh"
+#include "mma.cuh"
 #include "prims.cuh"
 
 namespace exafac {
@@ -219,24 +220,14 @@ __global__ void design_kernel(int N, int n, int R, const int64_t* __restrict__ j
 // inputs rounded to TF32 (10-bit mantissa, round to nearest) or BF16 (7-bit)
 // on the tensor cores, accumulated in FP32 within a block of 32 rows and in
 // FP64 across blocks.
-// TF32 rounding (10 mantissa bits), to nearest with ties away from zero, in
-// integer arithmetic: adding half a TF32 ulp (bit 12) to the sign-magnitude
-// pattern and clearing the 13 dropped bits rounds the magnitude; a carry moves
-// the exponent up (to infinity past the largest TF32 value).  Infinities and
-// NaNs pass through.  Same results as cvt.rna.tf32.f32, without the
-// conversion unit.
-__device__ __forceinline__ float round_tf32(float x) {
-    const uint32_t b = __float_as_uint(x);
-    if ((b & 0x7f800000u) == 0x7f800000u) return x;
-    return __uint_as_float((b + 0x1000u) & 0xffffe000u);
-}
 __device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
 // Tensor-core form.  A warp owns 32 design rows at a time:
 //   * factor rows are gathered one per load instruction (lane = column),
 //     32 rows in flight per mode, rounded to FP32 in integer arithmetic
 //     (narrow_f64, off the FP64 pipe) and multiplied in FP32;
-//   * D'_j = d_j * w_j goes to Df (FP32, rows of f32_row_stride(R) floats,
+//   * D'_j = d_j * w_j goes to Df (FP32, rows of 32 floats: one 128-byte
+//     line per row for the gathers of the segmented reduction,
 //     zero padded), the Gram input round(d_j sqrt(w_j))
 //     to a shared tile T (32 rows x kDStride, zero padded);
 //   * the tile's Gram T^T T comes from mma.sync m16n8k8 TF32 instructions with
@@ -249,13 +240,6 @@ constexpr int kDesignWarps = 8;
 constexpr int kDStride = 40;  // floats per tile row: fragment loads hit 32 distinct banks
 constexpr int kDesignBlocks = 152 * 2;
 
-__device__ __forceinline__ void mma_tf32_16x8x8(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 
 template <int kRound>  // 1: TF32, 2: BF16
 __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, int n, int R,
@@ -281,7 +265,7 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
 #pragma unroll
         for (int i = 0; i < 4; i++) ghi[p][i] = glo[p][i] = 0.0f;
     float (*t)[kDStride] = tile[w];
-    const int RS = (R + 3) & ~3;  // Df row stride (zero padded)
+    const int RS = (R + 3) & ~3;  // Df row length written (zero padded); the row stride is 32
     const int64_t ju = *ju_dev;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -312,7 +296,7 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
                 const float x = prod[r] * swr;
                 v = kRound == 1 ? round_tf32(x) : round_bf16(x);
             }
-            if (r < nrow && lane < RS) Df[(base + r) * RS + lane] = lane < R ? prod[r] * wr : 0.0f;
+            if (r < nrow && lane < RS) Df[(base + r) * 32 + lane] = lane < R ? prod[r] * wr : 0.0f;
             t[r][lane] = v;  // lanes >= R and rows >= nrow: zero
         }
         __syncwarp();
