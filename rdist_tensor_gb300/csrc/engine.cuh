@@ -164,6 +164,7 @@ int design_pinv(Session& s, cudaStream_t st);
 int gram_rows(Session& s, const double* A, int64_t rows, const uint32_t* rowlist, const int64_t* count_dev,
               double* out_full, cudaStream_t st);
 int lookup_hits(Session& s, int n, int64_t J, bool packed, cudaStream_t st);
+int keep_touched(Session& s, int n, cudaStream_t st);
 int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st);
 int gram_reduce_to(Session& s, int64_t nblk, double* out, cudaStream_t st);
 int sigma_and_gram(Session& s, cudaStream_t st);

@@ -440,8 +440,7 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
                                     cudaMemcpyDeviceToDevice, st));
     if (arls) EXAFAC_TRY(arls_build_cdf(s, n, s.touched, s.counters + 2, st));
     else EXAFAC_TRY(launch_tree_build(s.rtree[n], s.R, s.F.U[n], s.treeG[n], st));
-    EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.nzrows[n], s.touched, sizeof(uint32_t) * s.dims[n], cudaMemcpyDeviceToDevice, st));
-    EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.nzcount + n, s.counters + 2, sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+    EXAFAC_TRY(keep_touched(s, n, st));
     s.dense[n] = false;
     EXAFAC_TRY(mark(h, 5, st));
     if (h->timing) {

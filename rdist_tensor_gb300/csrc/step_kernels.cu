@@ -719,6 +719,23 @@ int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st) {
     return EXAFAC_OK;
 }
 
+// The step's touched rows become mode n's nonzero-row list (nzrows[n],
+// nzcount[n]): only the counters[2] listed entries are copied.
+__global__ void keep_touched_kernel(const int64_t* __restrict__ counters, const uint32_t* __restrict__ touched,
+                                    uint32_t* __restrict__ list, int64_t* __restrict__ count) {
+    const int64_t T = counters[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = T;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += (int64_t)gridDim.x * blockDim.x)
+        list[i] = touched[i];
+}
+
+int keep_touched(Session& s, int n, cudaStream_t st) {
+    keep_touched_kernel<<<152 * 4, 256, 0, st>>>(s.counters, s.touched, s.nzrows[n], s.nzcount + n);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
 // Warp per 32 listed rows: indices loaded together, then one row per store
 // instruction (lane = column).
 // Rows listed in `keep` (a bitmap over the rows) are skipped: they are
