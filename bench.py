@@ -329,6 +329,9 @@ def run_gpu(args, w):
     host_uni.copy_(torch.rand((args.steps, N, N, J), dtype=torch.float64))
     dev_uni = torch.empty((N, N, J), dtype=torch.float64, device="cuda")
     sig_host = torch.empty(R, dtype=torch.float64, pin_memory=True)
+    # one untimed sweep with these buffers: it captures the sweep graph for them
+    dev_uni.copy_(host_uni[0], non_blocking=True)
+    opt.execute_sweeps(1, J, dev_uni)
     torch.cuda.synchronize()
     barrier(ws)
     t0 = time.perf_counter()

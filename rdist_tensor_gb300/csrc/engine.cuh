@@ -172,7 +172,7 @@ int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st);
 
 // ---- load-balanced MTTKRP and post-processing, R <= 32 (post_kernels.cu)
 constexpr int kSegChunkHits = 128;  // hits per chunk of the FP64 segmented reduction
-constexpr int kSegChunkF32 = 32;    // hits per chunk of the FP32 segmented reduction
+constexpr int kSegChunkF32 = 64;    // hits per chunk of the FP32 segmented reduction (a multiple of 32)
 // FP32 row stride of the design rows (Df) and MTTKRP rows (Mc): R rounded up
 // to a multiple of 4, so a row is a whole number of float4s.
 __host__ __device__ inline int f32_row_stride(int R) { return (R + 3) & ~3; }
@@ -191,7 +191,8 @@ int mttkrp_scatter_out(Session& s, double* out, cudaStream_t st);
 int spmm_solve(Session& s, int n, cudaStream_t st);
 int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStream_t st);
 int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st);
-int zero_factor_rows(Session& s, int n, cudaStream_t st);
+int clear_dense_factor(Session& s, int n, cudaStream_t st);
+int zero_old_rows(Session& s, int n, cudaStream_t st);
 int fit_residual(Session& s, double* out_dev, cudaStream_t st);
 int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st);
 int matmul_rows_sym(Session& s, const double* M, const double* Phi, double* U, int64_t rows, cudaStream_t st);

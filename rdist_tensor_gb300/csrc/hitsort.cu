@@ -358,8 +358,9 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
 
 // Run heads (first hit of a row) of the sorted keys, per tile: the tile's
 // count, or (compact) the heads themselves written to touched / seg_start at
-// the tile's base, and for every chunk of kSegChunkF32 hits the index of the
-// run holding its first hit (chunk_seg).  Same item order as the downsweep.
+// the tile's base and marked in the step's row bitmap (rowbits, cleared
+// beforehand), and for every chunk of kSegChunkF32 hits the index of the run
+// holding its first hit (chunk_seg).  Same item order as the downsweep.
 template <bool kCompact>
 __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                               const uint32_t* __restrict__ keys,
@@ -367,7 +368,8 @@ __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __r
                                                               const int64_t* __restrict__ tile_base,
                                                               uint32_t* __restrict__ touched,
                                                               int64_t* __restrict__ seg_start,
-                                                              uint32_t* __restrict__ chunk_seg) {
+                                                              uint32_t* __restrict__ chunk_seg,
+                                                              uint32_t* __restrict__ rowbits) {
     __shared__ uint32_t wsum[kHsWarps];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -403,14 +405,29 @@ __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __r
             for (int ww = 0; ww < w; ww++) at += wsum[ww];
 #pragma unroll
             for (int r = 0; r < kHsItems; r++) {
-                if ((heads[r] >> lane) & 1u) {
+                const bool hd = (heads[r] >> lane) & 1u;
+                if (hd) {
                     const int64_t q = at + __popc(heads[r] & lt);
                     touched[q] = kk[r];
                     seg_start[q] = base + r * 32 + lane;
                 }
-                // each round is one chunk of kSegChunkF32 hits: the index of
-                // the run holding its first hit
-                if (lane == 0 && base + r * 32 < H)
+                {  // the step's row bitmap: the round's rows are sorted, so equal
+                    // 32-row words are runs of lanes; a segmented OR-scan leaves each
+                    // run's bits in its last lane, which makes the one atomic
+                    const unsigned word = kk[r] >> 5;
+                    unsigned bits = hd ? 1u << (kk[r] & 31) : 0u;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const unsigned b = __shfl_up_sync(0xffffffffu, bits, o);
+                        const unsigned wo = __shfl_up_sync(0xffffffffu, word, o);
+                        if (lane >= o && wo == word) bits |= b;
+                    }
+                    const unsigned wn = __shfl_down_sync(0xffffffffu, word, 1);
+                    if (bits && (lane == 31 || wn != word)) atomicOr(&rowbits[word], bits);
+                }
+                // a round that starts a chunk of kSegChunkF32 hits: the index
+                // of the run holding its first hit
+                if (lane == 0 && base + r * 32 < H && (base + r * 32) % kSegChunkF32 == 0)
                     chunk_seg[(base + r * 32) / kSegChunkF32] = (uint32_t)(at + (heads[r] & 1u) - 1);
                 at += __popc(heads[r]);
             }
@@ -525,12 +542,13 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(sort_keys(s, n, packed, st));
     hs_heads_kernel<false><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, s.head_cnt, nullptr,
-                                                          nullptr, nullptr, nullptr);
+                                                          nullptr, nullptr, nullptr, nullptr);
     count_launch();
     hs_headscan_kernel<<<1, 1024, 0, st>>>(s.counters, cap, s.head_cnt, s.head_base, s.counters + 2, s.seg_start);
     count_launch();
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowbits, 0, sizeof(uint32_t) * ceil_div(s.dims[n], 32), st));
     hs_heads_kernel<true><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, nullptr, s.head_base,
-                                                         s.touched, s.seg_start, s.chunk_seg);
+                                                         s.touched, s.seg_start, s.chunk_seg, s.rowbits);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

@@ -324,9 +324,9 @@ int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st) {
 // of kSegChunkF32 hits; within a group lane `sub` holds column block
 // [4 sub, 4 sub + 4) of a float4 row (Q = f32_row_stride(R) / 4 blocks), so
 // one 16-byte load brings a hit's four columns and the warp advances four
-// hits per instruction.  Each lane loads four of its group's hits (row and
-// the packed (sample, value) that travelled through the sort); hit t of the
-// chunk is broadcast from lane t % 8 of the group.  Design rows are gathered 8 hits at a time before their FMAs.  Rows
+// hits per instruction.  Each lane loads its share of the group's hits (row and
+// the packed (sample, value) that travelled through the sort) for every 8
+// of the chunk; hit t of the chunk is broadcast from lane t % 8 of the group.  Design rows are gathered 8 hits at a time before their FMAs.  Rows
 // inside a chunk go straight to Mc (row stride 4Q floats); crossing rows
 // leave the same carries as the FP64 form (kCarryStride floats per chunk).
 template <int Q>
@@ -353,38 +353,41 @@ __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __res
         const int n = (int)min((int64_t)C, H - cs);
         const uint32_t prev_row = cs > 0 ? keys[cs - 1] : kNoRow;
         const uint32_t next_row = cs + n < H ? keys[cs + n] : kNoRow;
-        uint32_t hr[4], hj[4];
-        float hv[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {  // hit sub + 8 i of the chunk
-            const int t = sub + 8 * i;
-            hr[i] = kNoRow;
-            hj[i] = 0;
-            hv[i] = 0.f;
+        // this lane's hit of the round (hit b + sub), loaded one round ahead
+        auto load_hit = [&](int t, uint32_t& r, uint32_t& j, float& v) {
+            r = kNoRow;
+            j = 0;
+            v = 0.f;
             if (t < n) {
-                hr[i] = keys[cs + t];
+                r = keys[cs + t];
                 const uint64_t p = pay64[cs + t];
-                hj[i] = (uint32_t)p;
-                hv[i] = __uint_as_float((uint32_t)(p >> 32));
+                j = (uint32_t)p;
+                v = __uint_as_float((uint32_t)(p >> 32));
             }
-        }
-        uint32_t cur = __shfl_sync(gmask, hr[0], 0, 8);
+        };
+        uint32_t nr_, nj_;
+        float nv_;
+        load_hit(sub, nr_, nj_, nv_);
+        uint32_t cur = __shfl_sync(gmask, nr_, 0, 8);
         int64_t seg = chunk_seg[c];  // compact index of the run holding hit cs
         bool first_seg = true;
         float4 acc = zero4;
-#pragma unroll
-        for (int b = 0; b < C; b += 8) {
+#pragma unroll 1
+        for (int b = 0; b < C && b < n; b += 8) {
+            const uint32_t hr = nr_, hj = nj_;
+            const float hv = nv_;
+            if (b + 8 < C) load_hit(b + 8 + sub, nr_, nj_, nv_);
             float4 d[8];
 #pragma unroll
             for (int u = 0; u < 8; u++) {
-                const uint32_t jt = __shfl_sync(gmask, hj[b / 8], u, 8);
+                const uint32_t jt = __shfl_sync(gmask, hj, u, 8);
                 d[u] = (b + u < n && col) ? D4[(int64_t)jt * 8 + sub] : zero4;  // 128-byte rows
             }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const int t = b + u;
-                const uint32_t rt = __shfl_sync(gmask, hr[b / 8], u, 8);
-                const float vt = __shfl_sync(gmask, hv[b / 8], u, 8);
+                const uint32_t rt = __shfl_sync(gmask, hr, u, 8);
+                const float vt = __shfl_sync(gmask, hv, u, 8);
                 if (t < n) {
                     if (rt != cur) {  // the open segment ends inside the chunk
                         if (col) {
@@ -982,7 +985,7 @@ static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
 
 static int solve_f32(Session& s, int n, cudaStream_t st) {
     EXAFAC_TRY(segmented_mttkrp<float>(s, st));
-    EXAFAC_TRY(zero_factor_rows(s, n, st));
+    EXAFAC_TRY(clear_dense_factor(s, n, st));  // the old rows are cleared beside the update
     if (s.R <= 16) EXAFAC_TRY(launch_solve_f32<16>(s, n, st));
     else if (s.R <= 28) EXAFAC_TRY(launch_solve_f32<28>(s, n, st));
     else EXAFAC_TRY(launch_solve_f32<32>(s, n, st));
@@ -995,7 +998,7 @@ template <typename TA>
 static int solve_typed(Session& s, int n, cudaStream_t st) {
     const int R = s.R;
     EXAFAC_TRY(segmented_mttkrp<TA>(s, st));
-    EXAFAC_TRY(zero_factor_rows(s, n, st));
+    EXAFAC_TRY(clear_dense_factor(s, n, st));  // the old rows are cleared beside the update
     const int P = packed_size(R);
     const int Q = (P + 31) / 32;
     const TA* Mc = reinterpret_cast<const TA*>(s.Mc);

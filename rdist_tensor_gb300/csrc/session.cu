@@ -228,6 +228,11 @@ struct exafac_als_s {
     // lookup and the hit sort (fork / join events on the caller's stream).
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // and, queued after it, the clearing of the factor rows the previous
+    // update of the mode wrote and this one does not (disjoint from the rows
+    // the update writes), beside the MTTKRP and solve; joined before the
+    // renormalisation
+    cudaEvent_t fork2 = nullptr, join2 = nullptr;
     // One captured sweep (exafac_als_sweeps), keyed by J and the uniforms
     // pointer it was captured with, and the kernels it launches.
     cudaStream_t cap = nullptr;
@@ -241,6 +246,8 @@ struct exafac_als_s {
             if (e) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
+        if (fork2) cudaEventDestroy(fork2);
+        if (join2) cudaEventDestroy(join2);
         if (side) cudaStreamDestroy(side);
         if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
         if (cap_ev) cudaEventDestroy(cap_ev);
@@ -255,6 +262,8 @@ static int fork_design_pinv(exafac_als_s* h, cudaStream_t st) {
         EXAFAC_CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
+        EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->fork2, cudaEventDisableTiming));
+        EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->join2, cudaEventDisableTiming));
     }
     EXAFAC_CUDA_TRY(cudaEventRecord(h->fork, st));
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork, 0));
@@ -415,13 +424,20 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     const bool arls = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV;
     const bool tiled = s.R <= 32;
     EXAFAC_TRY(lookup_hits(s, n, J, tiled && s.cfg.precision != EXAFAC_PREC_FP64, st));
+    // rowbits is set: the old rows are cleared on the side stream
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->fork2, st));
+    EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork2, 0));
+    EXAFAC_TRY(zero_old_rows(s, n, h->side));
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->join2, h->side));
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join, 0));
     if (tiled) {
         EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
     } else {
-        EXAFAC_TRY(zero_factor_rows(s, n, st));
+        EXAFAC_TRY(clear_dense_factor(s, n, st));
         EXAFAC_TRY(spmm_solve(s, n, st));
     }
+    // the old rows are cleared (the renormalisation may rescale every row)
+    EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join2, 0));
     EXAFAC_TRY(mark(h, 3, st));
     // R5 (dense reduce) is empty at one rank.  R6: renormalise (and, for
     // CP-ARLS-LEV, the new leverage scores of the touched rows).

@@ -762,33 +762,30 @@ __global__ void zero_rows_kernel(int R, const uint32_t* __restrict__ list, const
     }
 }
 
-__global__ void mark_rows_kernel(const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
-                                 uint32_t* __restrict__ bits) {
-    const int64_t cnt = *cnt_dev;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t r = list[i];
-        atomicOr(&bits[r >> 5], 1u << (r & 31));
-    }
-}
 
 // Clears the rows of U_n (and their leverage scores) that the previous update
-// left nonzero and the current one (s.touched, counters[2]) does not write;
-// a factor that was never updated is cleared entirely.
-int zero_factor_rows(Session& s, int n, cudaStream_t st) {
-    const int R = s.R;
+// left nonzero and the current one (s.touched, counters[2]) does not write.
+// A factor that was never updated is cleared entirely, here (dense[n]: must
+// precede the writes of the update); otherwise the clearing touches only rows
+// that the update does not write, so the step runs it beside the update
+// (zero_old_rows, on a side stream once rowbits is set by the hit grouping).
+int clear_dense_factor(Session& s, int n, cudaStream_t st) {
+    if (!s.dense[n]) return EXAFAC_OK;
     double* sc = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV ? s.scores[n] : nullptr;
-    if (s.dense[n]) {
-        EXAFAC_CUDA_TRY(cudaMemsetAsync(s.F.U[n], 0, sizeof(double) * s.dims[n] * R, st));
-        if (sc) EXAFAC_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * s.dims[n], st));
-    } else {
-        EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowbits, 0, sizeof(uint32_t) * ceil_div(s.dims[n], 32), st));
-        mark_rows_kernel<<<152 * 8, 256, 0, st>>>(s.touched, s.counters + 2, s.rowbits); count_launch();
-        zero_rows_kernel<<<152 * 8, 256, 0, st>>>(R, s.nzrows[n], s.nzcount + n, s.rowbits, s.F.U[n], sc);
-        count_launch();
-        EXAFAC_CHECK_LAUNCH();
-    }
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.F.U[n], 0, sizeof(double) * s.dims[n] * s.R, st));
+    if (sc) EXAFAC_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * s.dims[n], st));
     return EXAFAC_OK;
 }
+
+int zero_old_rows(Session& s, int n, cudaStream_t st) {
+    if (s.dense[n]) return EXAFAC_OK;
+    double* sc = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV ? s.scores[n] : nullptr;
+    zero_rows_kernel<<<152 * 8, 256, 0, st>>>(s.R, s.nzrows[n], s.nzcount + n, s.rowbits, s.F.U[n], sc);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
 
 // ---------------------------------------------------------------------------
 // Exact fit (SparseTensor::compute_exact_fit + compute_2bmb,
