@@ -65,6 +65,7 @@ struct Session {
 
     // CP-ARLS-LEV state
     double* scores[kMaxModes] = {nullptr};
+    double* scores_c = nullptr;  // Imax: the step's leverage scores by touched-row index (compact, for the CDF)
     double* cdf[kMaxModes] = {nullptr};
     uint32_t* guide[kMaxModes] = {nullptr};
     bool cdf_compact[kMaxModes] = {false};  // CDF over nzrows[k] (a sampled update) rather than all rows  // kGuideBuckets + 1: guide[b] = lower_bound(cdf, b / kGuideBuckets)

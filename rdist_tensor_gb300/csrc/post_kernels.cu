@@ -518,7 +518,8 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
                                                                  const double* __restrict__ sigma,
                                                                  const double* __restrict__ Pm,
                                                                  const int* __restrict__ degenerate,
-                                                                 double* __restrict__ U, double* __restrict__ scores) {
+                                                                 double* __restrict__ U, double* __restrict__ scores,
+                                                                 double* __restrict__ scores_c) {
     __shared__ TA psm[32 * 32];
     __shared__ double sg[32];
     __shared__ TA tile[kNormWarps][32][33];  // a warp's 32 rows, padded
@@ -556,6 +557,7 @@ __global__ void __launch_bounds__(kNormWarps * 32) normlev_kernel(int R, const i
                 acc = fma(ut[lane][a], y, acc);
             }
             scores[touched[i]] = (double)acc;
+            scores_c[i] = (double)acc;
         }
         __syncwarp();
     }
@@ -867,7 +869,8 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) normlev_f32_kernel(int R,
                                                                       const double* __restrict__ Pm,
                                                                       const int* __restrict__ degenerate,
                                                                       double* __restrict__ U,
-                                                                      double* __restrict__ scores) {
+                                                                      double* __restrict__ scores,
+                                                                      double* __restrict__ scores_c) {
     __shared__ __align__(16) float psm[KC][KC];
     __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
     __shared__ float sg[32];
@@ -960,7 +963,9 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) normlev_f32_kernel(int R,
                     acc = fmaf(u[a], y, acc);
                 }
             }
-            scores[myrow] = (double)acc;
+            const double l = (double)acc;
+            scores[myrow] = l;
+            scores_c[base + lane] = l;  // by touched-row index, for the CDF
         }
         __syncwarp();
     }
@@ -980,7 +985,7 @@ template <int KC>
 static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
     normlev_f32_kernel<KC><<<kNormlevBlocks, kSolveWarps * 32, 0, st>>>(
         s.R, s.counters, s.touched, s.Uc, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
-        s.F.U[n], arls ? s.scores[n] : nullptr);
+        s.F.U[n], arls ? s.scores[n] : nullptr, s.scores_c);
 }
 
 static int solve_f32(Session& s, int n, cudaStream_t st) {
@@ -1028,7 +1033,7 @@ static int normalize_typed(Session& s, int n, bool arls, cudaStream_t st) {
     if (arls) EXAFAC_TRY(launch_pinv(R, s.ngram, s.upinv, 1e-11, s.vt, st));
     normlev_kernel<TA><<<grid_capped(s.dims[n], kNormWarps * 32), kNormWarps * 32, 0, st>>>(
         R, s.counters, s.touched, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
-        s.F.U[n], arls ? s.scores[n] : nullptr);
+        s.F.U[n], arls ? s.scores[n] : nullptr, s.scores_c);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return scale_rows_if_degenerate(s, n, st);

@@ -108,7 +108,10 @@ __global__ void cdf_guide_kernel(const double* __restrict__ cdf, int64_t n, uint
 // be nonzero after a sampled update): the partial sums at those rows are the
 // ones the full CDF takes there (the other rows add exactly zero), so a draw
 // lands on the same row; only the final 1.0 sits at the last listed row.
+// The listed rows' scores are read from scores_c, where the leverage kernels
+// left them by list position (contiguous, no gather).
 int arls_build_cdf(Session& s, int k, const uint32_t* list, const int64_t* count_dev, cudaStream_t st) {
+    const double* w = list ? s.scores_c : s.scores[k];
     const int64_t n = s.dims[k];
     s.cdf_compact[k] = list != nullptr;
     if (n < 2) {
@@ -125,10 +128,10 @@ int arls_build_cdf(Session& s, int k, const uint32_t* list, const int64_t* count
         if (smem > 48 * 1024)
             EXAFAC_CUDA_TRY(cudaFuncSetAttribute(cdf_sequential_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)smem));
-        cdf_sequential_kernel<<<1, 256, smem, st>>>(s.scores[k], n, s.cdf[k], s.cdf_total + k, list, count_dev);
+        cdf_sequential_kernel<<<1, 256, smem, st>>>(w, n, s.cdf[k], s.cdf_total + k, nullptr, count_dev);
         count_launch();
     } else {
-        EXAFAC_TRY(scan_cdf_f64(s.scores[k], s.cdf[k], n, s.cdf_total + k, s.scan_sc, st, list, count_dev));
+        EXAFAC_TRY(scan_cdf_f64(w, s.cdf[k], n, s.cdf_total + k, s.scan_sc, st, nullptr, count_dev));
     }
     cdf_guide_kernel<<<(unsigned)ceil_div(kGuideBuckets + 1, 256), 256, 0, st>>>(s.cdf[k], n, s.guide[k], count_dev);
     count_launch();
@@ -140,7 +143,7 @@ int arls_build_cdf(Session& s, int k, const uint32_t* list, const int64_t* count
 // y = P u (dsymm) then the dot product.  Warp per row.
 __global__ void leverage_kernel(int R, const double* __restrict__ U, const double* __restrict__ Pm, int64_t rows,
                                 const uint32_t* __restrict__ list, const int64_t* __restrict__ count_dev,
-                                double* __restrict__ scores) {
+                                double* __restrict__ scores, double* __restrict__ scores_c) {
     extern __shared__ double sm[];
     double* Psm = sm;
     const int warps = blockDim.x >> 5;
@@ -160,7 +163,10 @@ __global__ void leverage_kernel(int R, const double* __restrict__ U, const doubl
             acc = fma(usm[a], y, acc);
         }
         acc = warp_sum(acc);
-        if (lane == 0) scores[r] = acc;
+        if (lane == 0) {
+            scores[r] = acc;
+            if (list) scores_c[i] = acc;  // by list position, for the CDF
+        }
         __syncwarp();
     }
 }
@@ -174,7 +180,7 @@ int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStre
     int64_t rows = all_rows ? s.dims[k] : s.dims[k];
     int blocks = (int)std::min<int64_t>(ceil_div(rows, warps), 152 * 16);
     leverage_kernel<<<blocks, warps * 32, smem, st>>>(R, s.F.U[k], pinv, s.dims[k], all_rows ? nullptr : s.touched,
-                                                      s.counters + 2, s.scores[k]); count_launch();
+                                                      s.counters + 2, s.scores[k], s.scores_c); count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

@@ -48,6 +48,9 @@ static void carve(Session& s) {
             s.cdf[k] = a.take<double>(s.dims[k]);
             s.guide[k] = a.take<uint32_t>(kGuideBuckets + 1);
         }
+        int64_t imax = 1;
+        for (int k = 0; k < N; k++) imax = std::max<int64_t>(imax, s.dims[k]);
+        s.scores_c = a.take<double>(imax);
     } else {
         for (int k = 0; k < N; k++) s.treeG[k] = a.take<double>(s.rtree[k].node_count * P);
         s.eigG = a.take<double>((int64_t)N * s.etree.node_count * P);
