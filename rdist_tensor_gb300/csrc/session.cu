@@ -227,8 +227,9 @@ struct exafac_als_s {
     bool timing = false;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     double region[7] = {0, 0, 0, 0, 0, 0, 0};
-    // Side stream for the design pseudo-inverse, which runs beside the fiber
-    // lookup and the hit sort (fork / join events on the caller's stream).
+    // Side stream for the design rows, their Gram and its pseudo-inverse,
+    // which run beside the fiber lookup and the hit sort (fork / join events
+    // on the caller's stream).
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     // and, queued after it, the clearing of the factor rows the previous
@@ -258,9 +259,12 @@ struct exafac_als_s {
     }
 };
 
-// Launches the design pseudo-inverse on the side stream after the work
-// already queued on st; st must wait on h->join before reading Phi.
-static int fork_design_pinv(exafac_als_s* h, cudaStream_t st) {
+// Launches the design rows, their Gram and its pseudo-inverse on the side
+// stream after the work already queued on st (the deduplicated samples):
+// they need nothing of the fibre lookup and hit grouping that st runs next,
+// and those write nothing they read.  st must wait on h->join before reading
+// the design rows or Phi.
+static int fork_design(exafac_als_s* h, int n, int64_t J, cudaStream_t st) {
     if (!h->side) {
         EXAFAC_CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
@@ -270,6 +274,7 @@ static int fork_design_pinv(exafac_als_s* h, cudaStream_t st) {
     }
     EXAFAC_CUDA_TRY(cudaEventRecord(h->fork, st));
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork, 0));
+    EXAFAC_TRY(design_gram(h->s, n, J, h->side));
     EXAFAC_TRY(design_pinv(h->s, h->side));
     EXAFAC_CUDA_TRY(cudaEventRecord(h->join, h->side));
     return EXAFAC_OK;
@@ -417,10 +422,10 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     EXAFAC_TRY(draw_into_session(s, n, J, uni, perms, st));
     EXAFAC_TRY(mark(h, 1, st));
     // R2 (row gather) is a no-op on one GPU: factors are read in place.
-    // R3: deduplicate, design rows, Gram, pseudo-inverse.
+    // R3: deduplicate; the design rows, Gram and pseudo-inverse go to the
+    // side stream.
     EXAFAC_TRY(dedup(s, n, J, st));
-    EXAFAC_TRY(design_gram(s, n, J, st));
-    EXAFAC_TRY(fork_design_pinv(h, st));
+    EXAFAC_TRY(fork_design(h, n, J, st));
     EXAFAC_TRY(mark(h, 2, st));
     // R4: fiber lookup, hits grouped by output row, MTTKRP rows, then
     // U = MTTKRP * Phi on the touched rows (the other rows are zero).
