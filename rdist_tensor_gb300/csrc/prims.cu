@@ -63,11 +63,19 @@ __global__ void scan_block_sums(const Tin* __restrict__ in, int64_t n, Tacc* __r
     __shared__ Tacc red[33];
     if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
-    Tacc acc = 0;
-    for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
-        int64_t g = base + i;
-        if (g < n) acc += (Tacc)in[gather ? (int64_t)gather[g] : g];
+    if (base >= n) {  // uniform per block
+        if (threadIdx.x == 0) partial[blockIdx.x] = Tacc(0);
+        return;
     }
+    Tacc v[kScanItems];  // all of the thread's loads in flight before the first add
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        const int64_t g = base + threadIdx.x + k * kScanThreads;
+        v[k] = g < n ? (Tacc)in[gather ? (int64_t)gather[g] : g] : Tacc(0);
+    }
+    Tacc acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) acc += v[k];
     Tacc s = block_reduce_sum(acc, red);
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
@@ -102,9 +110,16 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
     if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     if (base >= n) return;  // uniform per block
-    for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
-        int64_t g = base + i;
-        tile[scan_pad(i)] = g < n ? (Tacc)in[gather ? (int64_t)gather[g] : g] : Tacc(0);
+    {
+        Tacc v[kScanItems];  // all of the thread's loads in flight before the first store
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            const int i = threadIdx.x + k * kScanThreads;
+            const int64_t g = base + i;
+            v[k] = g < n ? (Tacc)in[gather ? (int64_t)gather[g] : g] : Tacc(0);
+        }
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) tile[scan_pad(threadIdx.x + k * kScanThreads)] = v[k];
     }
     __syncthreads();
     Tacc loc[kScanItems];
