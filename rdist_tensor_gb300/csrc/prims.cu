@@ -101,14 +101,45 @@ __global__ void scan_partials_kernel(Tacc* partial, int64_t nb, Tacc* total) {
 // distinct banks.
 __device__ __forceinline__ int scan_pad(int i) { return i + (i >> 4); }
 
+// fold_nb > 0: partial[] holds the nb = fold_nb raw block sums (no partials
+// kernel ran): every block adds those before it itself, in a fixed order, and
+// the total of all of them (the same value in every block); block 0 writes it
+// to *total_out and adds it to *accum when given.  fold_nb == 0: partial[]
+// holds the scanned prefixes and *total the total.
 template <typename Tin, typename Tacc, bool kInclusive, bool kNormalize = false>
 __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, int64_t n,
                            const Tacc* __restrict__ partial, const Tacc* __restrict__ total = nullptr,
-                           const uint32_t* __restrict__ gather = nullptr, const int64_t* n_dev = nullptr) {
+                           const uint32_t* __restrict__ gather = nullptr, const int64_t* n_dev = nullptr,
+                           int64_t fold_nb = 0, Tacc* total_out = nullptr, int64_t* accum = nullptr) {
     __shared__ Tacc tile[kScanTile + kScanTile / 16];
     __shared__ Tacc red[33];
+    __shared__ Tacc fold[2];
     if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    Tacc prefix = 0, all = 0;
+    if (fold_nb > 0) {
+        Tacc a = 0, t = 0;
+        for (int64_t i = threadIdx.x; i < fold_nb; i += kScanThreads) {
+            const Tacc v = partial[i];
+            t += v;
+            if (i < (int64_t)blockIdx.x) a += v;
+        }
+        const Tacc ra = block_reduce_sum(a, red);
+        if (threadIdx.x == 0) fold[0] = ra;
+        __syncthreads();
+        const Tacc rt = block_reduce_sum(t, red);
+        if (threadIdx.x == 0) fold[1] = rt;
+        __syncthreads();
+        prefix = fold[0];
+        all = fold[1];
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            if (total_out) *total_out = all;
+            if (accum) *accum += (int64_t)all;
+        }
+    } else {
+        if (base < n) prefix = partial[blockIdx.x];
+        if (kNormalize) all = *total;
+    }
     if (base >= n) return;  // uniform per block
     {
         Tacc v[kScanItems];  // all of the thread's loads in flight before the first store
@@ -130,7 +161,7 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
         sum += loc[k];
     }
     Tacc tot;
-    Tacc run = block_exclusive_scan(sum, red, &tot) + partial[blockIdx.x];
+    Tacc run = block_exclusive_scan(sum, red, &tot) + prefix;
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
         if (kInclusive) {
@@ -145,7 +176,7 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
     if (kNormalize) {
         // One reciprocal per block; the products differ from division by at
         // most one rounding.
-        const Tacc rt = Tacc(1) / *total;
+        const Tacc rt = Tacc(1) / all;
         for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
             int64_t g = base + i;
             if (g < n) out[g] = (g == n - 1) ? Tacc(1) : tile[scan_pad(i)] * rt;
@@ -158,8 +189,16 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
     }
 }
 
+// Scans of up to kFoldMaxBlocks tiles fold the block sums into the apply
+// kernel (each block reads at most that many partials).
+constexpr int64_t kFoldMaxBlocks = 2048;
+
+template <typename Tacc>
+__global__ void accumulate_total(int64_t* accum, const Tacc* total) { *accum += (int64_t)*total; }
+
 template <typename Tin, typename Tacc, bool kInclusive>
-static int scan_impl(const Tin* in, Tacc* out, int64_t n, Tacc* total, void* scratch, cudaStream_t s) {
+static int scan_impl(const Tin* in, Tacc* out, int64_t n, Tacc* total, void* scratch, cudaStream_t s,
+                     int64_t* accum = nullptr) {
     if (n <= 0) {
         if (total) EXAFAC_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(Tacc), s));
         return EXAFAC_OK;
@@ -167,8 +206,15 @@ static int scan_impl(const Tin* in, Tacc* out, int64_t n, Tacc* total, void* scr
     int64_t nb = ceil_div(n, kScanTile);
     Tacc* partial = reinterpret_cast<Tacc*>(scratch);
     scan_block_sums<Tin, Tacc><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial); count_launch();
-    scan_partials_kernel<Tacc><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
-    scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial); count_launch();
+    if (nb <= kFoldMaxBlocks) {  // each block folds the block sums itself: no partials kernel
+        scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, nullptr, nullptr,
+                                                                              nullptr, nb, total, accum);
+    } else {
+        scan_partials_kernel<Tacc><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
+        if (accum) accumulate_total<<<1, 1, 0, s>>>(accum, total), count_launch();
+        scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial);
+    }
+    count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -177,8 +223,8 @@ int scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* tota
     return scan_impl<int64_t, int64_t, false>(in, out, n, total, scratch, s);
 }
 int scan_exclusive_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, int64_t* total, void* scratch,
-                              cudaStream_t s) {
-    return scan_impl<uint32_t, int64_t, false>(in, out, n, total, scratch, s);
+                              cudaStream_t s, int64_t* accum) {
+    return scan_impl<uint32_t, int64_t, false>(in, out, n, total, scratch, s, accum);
 }
 int scan_inclusive_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s) {
     return scan_impl<double, double, true>(in, out, n, total, scratch, s);
@@ -190,6 +236,8 @@ int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* 
     double* partial = reinterpret_cast<double*>(scratch);
     scan_block_sums<double, double><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial, gather, n_dev);
     count_launch();
+    // (the grid is sized for the mode, most blocks past the touched count:
+    // folding there would cost every block a pass over all partials)
     scan_partials_kernel<double><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
     scan_apply<double, double, true, true><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, total, gather,
                                                                                    n_dev);

@@ -13,7 +13,7 @@ inline size_t scan_scratch_bytes(int64_t n) { return sizeof(double) * (size_t)(c
 // Sums are formed blockwise (not in sequential order).
 int scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* total, void* scratch, cudaStream_t s);
 int scan_exclusive_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, int64_t* total, void* scratch,
-                              cudaStream_t s);
+                              cudaStream_t s, int64_t* accum = nullptr);
 
 // Inclusive scan of doubles.
 int scan_inclusive_f64(const double* in, double* out, int64_t n, double* total, void* scratch, cudaStream_t s);

@@ -565,8 +565,6 @@ __global__ void lookup_kernel(KeySpec spec, int64_t J, const int64_t* __restrict
     f_len[j] = len;
 }
 
-// counters[5] += counters[1]: running total of the hits (nonzeros_iterated).
-__global__ void accumulate_kernel(int64_t* total, const int64_t* add) { *total += *add; }
 
 int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st) {
     const Lookup& L = s.look[n];
@@ -579,8 +577,8 @@ int lookup_fibers(Session& s, int n, int64_t J, cudaStream_t st) {
         lookup_kernel<Slot2><<<blocks, 256, 0, st>>>(L.spec, J, s.counters + 0, s.sd, (const Slot2*)L.slots,
                                                     L.nslots - 1, s.f_start, s.f_len);
     EXAFAC_CHECK_LAUNCH();
-    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.f_len, s.f_off, J, s.counters + 1, s.scan_sc, st));
-    accumulate_kernel<<<1, 1, 0, st>>>(s.counters + 5, s.counters + 1); count_launch();
+    // H to counters[1]; counters[5] accumulates the hits of all steps
+    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.f_len, s.f_off, J, s.counters + 1, s.scan_sc, st, s.counters + 5));
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
