@@ -378,9 +378,8 @@ __device__ bool pinv_sweep_f32(int R, const double* __restrict__ A, double* __re
     return true;
 }
 
-__global__ void __launch_bounds__(kSmallPinvThreads)
-    spd_pinv_small_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
-                          double* vt_scratch, int refine) {
+__device__ void pinv_small_block(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
+                                 double* vt_scratch, int refine) {
     extern __shared__ double smem[];  // Jacobi fallback; in the accepted path A, X and E staged for refinement
     __shared__ double rowbuf[2][kSmallPinvMaxR];  // pivot row k (unscaled), ping-pong
     __shared__ double rp[kSmallPinvMaxR];         // pivot row k times 1/pivot
@@ -495,6 +494,39 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
     if (refine == 1) newton_refine(R, A, out, smem);
 }
 
+__global__ void __launch_bounds__(kSmallPinvThreads)
+    spd_pinv_small_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
+                          double* vt_scratch, int refine) {
+    pinv_small_block(R, A, out, tol, vt_scratch, refine);
+}
+
+// The mixed forms' normalisation head in one block: column norms sigma_c =
+// sqrt(G_cc) of the factor Gram (DistMat1D::renormalize_columns,
+// distmat.hpp:85-138), the normalised Gram ngram = G_ab / (sigma_a sigma_b)
+// (as products with 1 / sigma: the leverage inverse is an FP32 quantity),
+// the degenerate flag, then the leverage pseudo-inverse of ngram (FP32 sweep
+// first).
+__global__ void __launch_bounds__(kSmallPinvThreads)
+    sigma_pinv_kernel(int R, const double* __restrict__ ugram, double* __restrict__ sigma,
+                      double* __restrict__ ngram, int* __restrict__ degenerate, double* __restrict__ out, double tol,
+                      double* vt_scratch) {
+    __shared__ double rinv[kSmallPinvMaxR];
+    __shared__ int deg;
+    if (threadIdx.x == 0) deg = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < R; c += blockDim.x) {
+        const double v = sqrt(ugram[c * R + c]);
+        sigma[c] = v;
+        rinv[c] = 1.0 / v;
+        if (!(v > 0.0)) deg = 1;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) ngram[e] = ugram[e] * rinv[e / R] * rinv[e % R];
+    if (threadIdx.x == 0) *degenerate = deg;
+    __syncthreads();  // the block's writes of ngram are visible to it
+    pinv_small_block(R, ngram, out, tol, vt_scratch, 2);
+}
+
 // Shared memory of the Cholesky path (L, L^{-1}, and the Newton step's
 // third matrix).  The Cholesky path is used when its buffers fit under
 // kPinvSmemCap (R <= 92); larger ranks go straight to Jacobi, unrefined
@@ -533,6 +565,16 @@ int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scra
 
 int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream) {
     return launch_pinv_impl(R, A, out, tol, vt_scratch, 1, stream);
+}
+
+int launch_sigma_pinv_f32(int R, const double* ugram, double* sigma, double* ngram, int* degenerate, double* out,
+                          double tol, double* vt_scratch, cudaStream_t stream) {
+    const size_t smem = std::max(syev_smem_bytes(R), chol_smem_bytes(R));
+    sigma_pinv_kernel<<<1, kSmallPinvThreads, smem, stream>>>(R, ugram, sigma, ngram, degenerate, out, tol,
+                                                              vt_scratch);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
 }
 
 int launch_pinv_leverage_f32(int R, const double* A, double* out, double tol, double* vt_scratch,

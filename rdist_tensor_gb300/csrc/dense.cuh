@@ -22,6 +22,10 @@ int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scra
 int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
 // The leverage-score pseudo-inverse of the mixed forms (unit-diagonal Gram):
 // the sweep in FP32 when its error bound allows, else the FP64 path.
+// R <= 32: sigma, ngram and the degenerate flag from the factor Gram, then
+// the FP32-first leverage pseudo-inverse of ngram, in one launch.
+int launch_sigma_pinv_f32(int R, const double* ugram, double* sigma, double* ngram, int* degenerate, double* out,
+                          double tol, double* vt_scratch, cudaStream_t stream);
 int launch_pinv_leverage_f32(int R, const double* A, double* out, double tol, double* vt_scratch,
                              cudaStream_t stream);
 

@@ -1048,8 +1048,11 @@ int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st) {
     if (s.cfg.precision == EXAFAC_PREC_FP64) return normalize_typed<double>(s, n, arls, st);
     const int R = s.R;
     EXAFAC_TRY(gram_reduce_to(s, kMmaBlocks, s.ugram, st));
-    EXAFAC_TRY(sigma_and_gram(s, st));
-    if (arls) EXAFAC_TRY(launch_pinv_leverage_f32(R, s.ngram, s.upinv, 1e-11, s.vt, st));
+    if (arls)
+        EXAFAC_TRY(launch_sigma_pinv_f32(R, s.ugram, s.F.sigma, s.ngram, reinterpret_cast<int*>(s.counters + 6),
+                                         s.upinv, 1e-11, s.vt, st));
+    else
+        EXAFAC_TRY(sigma_and_gram(s, st));
     if (R <= 16) launch_normlev_f32<16>(s, n, arls, st);
     else if (R <= 28) launch_normlev_f32<28>(s, n, arls, st);
     else launch_normlev_f32<32>(s, n, arls, st);
