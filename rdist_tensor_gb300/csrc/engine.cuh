@@ -99,8 +99,7 @@ struct Session {
     int32_t* d_count = nullptr;
     int32_t* slot_of = nullptr;
     Key128* dkey = nullptr;         // J: packed dedup key of each sample
-    uint32_t* flags = nullptr;
-    int64_t* pos = nullptr;
+    uint32_t* flags = nullptr;  // J: per-tile representative counts of the deduplication
     uint32_t* sd = nullptr;
     double* wd = nullptr;
     int64_t* counters = nullptr;  // [0] J_u, [1] H, [2] touched, [3..] scratch, [kRngSlot] Philox counter

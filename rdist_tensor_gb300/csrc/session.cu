@@ -75,7 +75,6 @@ static void carve(Session& s) {
     s.slot_of = a.take<int32_t>(J);
     s.dkey = a.take<Key128>(J);
     s.flags = a.take<uint32_t>(J);
-    s.pos = a.take<int64_t>(J);
     s.sd = a.take<uint32_t>(J * N);
     s.wd = a.take<double>(J);
     s.counters = a.take<int64_t>(16);

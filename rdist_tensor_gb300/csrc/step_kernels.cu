@@ -63,23 +63,104 @@ __global__ void dedup_insert_kernel(KeySpec spec, int64_t J, const uint32_t* __r
     slot_of[j] = (int32_t)h;
 }
 
-__global__ void dedup_flag_kernel(int64_t J, const int32_t* __restrict__ minj, const int32_t* __restrict__ slot_of,
-                                  uint32_t* __restrict__ flags) {
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= J) return;
-    flags[j] = minj[slot_of[j]] == (int32_t)j ? 1u : 0u;
+// The representatives (first occurrences) in order, in two passes over tiles
+// of kDedupTile samples (thread t holds samples 4t .. 4t + 3 of its tile):
+// dedup_count_kernel counts each tile's representatives; dedup_place_kernel
+// adds the counts of the tiles before its own (at most J / kDedupTile of
+// them), scans its tile and writes the representatives' coordinates and
+// weight x multiplicity at their places, and block 0 writes J_u to
+// counters[0].
+constexpr int kDedupTile = 1024;
+
+__device__ __forceinline__ uint32_t dedup_rep_bits(int64_t J, int64_t j0, const int32_t* __restrict__ minj,
+                                                   const int32_t* __restrict__ slot_of) {
+    uint32_t bits = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int64_t j = j0 + k;
+        if (j < J && minj[slot_of[j]] == (int32_t)j) bits |= 1u << k;
+    }
+    return bits;
 }
 
-__global__ void dedup_compact_kernel(int N, int64_t J, const uint32_t* __restrict__ flags,
-                                     const int64_t* __restrict__ pos, const int32_t* __restrict__ slot_of,
-                                     const int32_t* __restrict__ count, const uint32_t* __restrict__ samples,
-                                     const double* __restrict__ weights, uint32_t* __restrict__ sd,
-                                     double* __restrict__ wd) {
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= J || !flags[j]) return;
-    const int64_t p = pos[j];
-    for (int k = 0; k < N; k++) sd[p * N + k] = samples[j * N + k];
-    wd[p] = weights[j] * (double)count[slot_of[j]];
+__global__ void __launch_bounds__(256) dedup_count_kernel(int64_t J, const int32_t* __restrict__ minj,
+                                                          const int32_t* __restrict__ slot_of,
+                                                          uint32_t* __restrict__ tile_count) {
+    __shared__ uint32_t wsum[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t j0 = (int64_t)blockIdx.x * kDedupTile + 4 * threadIdx.x;
+    uint32_t c = (uint32_t)__popc(dedup_rep_bits(J, j0, minj, slot_of));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) wsum[w] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int ww = 0; ww < 8; ww++) t += wsum[ww];
+        tile_count[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) dedup_place_kernel(int N, int64_t J, int64_t ntiles,
+                                                          const uint32_t* __restrict__ tile_count,
+                                                          const int32_t* __restrict__ minj,
+                                                          const int32_t* __restrict__ slot_of,
+                                                          const int32_t* __restrict__ count,
+                                                          const uint32_t* __restrict__ samples,
+                                                          const double* __restrict__ weights,
+                                                          uint32_t* __restrict__ sd, double* __restrict__ wd,
+                                                          int64_t* __restrict__ ju_out) {
+    __shared__ uint32_t wsum[8];
+    __shared__ int64_t before_sh;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // representatives of the tiles before this one, and of all tiles (block 0)
+    int64_t a = 0, all = 0;
+    for (int64_t i = threadIdx.x; i < ntiles; i += blockDim.x) {
+        const int64_t v = tile_count[i];
+        all += v;
+        if (i < (int64_t)blockIdx.x) a += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        all += __shfl_xor_sync(0xffffffffu, all, o);
+    }
+    __shared__ int64_t red_a[8], red_all[8];
+    if (lane == 0) {
+        red_a[w] = a;
+        red_all[w] = all;
+    }
+    const int64_t j0 = (int64_t)blockIdx.x * kDedupTile + 4 * threadIdx.x;
+    const uint32_t bits = dedup_rep_bits(J, j0, minj, slot_of);
+    const uint32_t c = (uint32_t)__popc(bits);
+    uint32_t inc = c;  // inclusive scan of the threads' counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t ta = 0, tall = 0;
+        for (int ww = 0; ww < 8; ww++) {
+            ta += red_a[ww];
+            tall += red_all[ww];
+        }
+        before_sh = ta;
+        if (blockIdx.x == 0) *ju_out = tall;
+    }
+    __syncthreads();
+    int64_t p = before_sh + inc - c;
+    for (int ww = 0; ww < w; ww++) p += wsum[ww];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (!((bits >> k) & 1u)) continue;
+        const int64_t j = j0 + k;
+        for (int m = 0; m < N; m++) sd[p * N + m] = samples[j * N + m];
+        wd[p] = weights[j] * (double)count[slot_of[j]];
+        p++;
+    }
 }
 
 int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
@@ -89,11 +170,11 @@ int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
     const unsigned blocks = (unsigned)ceil_div(J, 256);
     dedup_insert_kernel<<<blocks, 256, 0, st>>>(s.look[n].spec, J, s.samples, s.dtab - 1, s.d_owner, s.d_minj,
                                                 s.d_count, s.slot_of, s.dkey); count_launch();
-    dedup_flag_kernel<<<blocks, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags); count_launch();
-    EXAFAC_CHECK_LAUNCH();
-    EXAFAC_TRY(scan_exclusive_u32_to_i64(s.flags, s.pos, J, s.counters + 0, s.scan_sc, st));
-    dedup_compact_kernel<<<blocks, 256, 0, st>>>(s.N, J, s.flags, s.pos, s.slot_of, s.d_count, s.samples, s.weights,
-                                                 s.sd, s.wd); count_launch();
+    const int64_t ntiles = ceil_div(J, kDedupTile);
+    dedup_count_kernel<<<(unsigned)ntiles, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags); count_launch();
+    dedup_place_kernel<<<(unsigned)ntiles, 256, 0, st>>>(s.N, J, ntiles, s.flags, s.d_minj, s.slot_of, s.d_count,
+                                                         s.samples, s.weights, s.sd, s.wd, s.counters + 0);
+    count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
