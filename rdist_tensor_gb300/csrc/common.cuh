@@ -194,6 +194,39 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
     hi = s;
 }
 
+// Programmatic dependent launch.  A kernel launched by launch_dependent()
+// may be scheduled while the kernel before it in the stream is finishing; it
+// calls pdl_wait() before anything else, which returns once that kernel has
+// completed and its writes are visible.  pdl_trigger() lets the next such
+// kernel be scheduled as soon as every block of this one has started.  Both
+// are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// dependent = false gives an ordinary launch (for a launch whose stream
+// predecessor is not always a kernel).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent_if(bool dependent, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                       cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = dependent ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args... args) {
+    return launch_dependent_if(true, kernel, grid, block, smem, st, args...);
+}
+
 // Number of bits needed to hold coordinates in [0, dim).
 inline int bits_for(int64_t dim) {
     int b = 0;

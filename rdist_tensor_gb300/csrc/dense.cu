@@ -512,6 +512,8 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
                       double* vt_scratch) {
     __shared__ double rinv[kSmallPinvMaxR];
     __shared__ int deg;
+    pdl_wait();
+    pdl_trigger();
     if (threadIdx.x == 0) deg = 0;
     __syncthreads();
     for (int c = threadIdx.x; c < R; c += blockDim.x) {
@@ -570,8 +572,8 @@ int launch_pinv_refined(int R, const double* A, double* out, double tol, double*
 int launch_sigma_pinv_f32(int R, const double* ugram, double* sigma, double* ngram, int* degenerate, double* out,
                           double tol, double* vt_scratch, cudaStream_t stream) {
     const size_t smem = std::max(syev_smem_bytes(R), chol_smem_bytes(R));
-    sigma_pinv_kernel<<<1, kSmallPinvThreads, smem, stream>>>(R, ugram, sigma, ngram, degenerate, out, tol,
-                                                              vt_scratch);
+    EXAFAC_CUDA_TRY(launch_dependent(sigma_pinv_kernel, 1, kSmallPinvThreads, smem, stream, R, ugram, sigma, ngram,
+                                     degenerate, out, tol, vt_scratch));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

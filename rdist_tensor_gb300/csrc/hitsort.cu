@@ -57,6 +57,8 @@ __device__ __forceinline__ int64_t owner_in(const int64_t* __restrict__ f_off, i
 __global__ void expand_owner_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                     const int64_t* __restrict__ f_off, const uint32_t* __restrict__ f_len,
                                     uint32_t* __restrict__ first) {
+    pdl_wait();
+    pdl_trigger();
     const int64_t ju = counters[0];
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < ju; j += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t len = f_len[j];
@@ -84,6 +86,8 @@ __global__ void hit_expand_kernel(const int64_t* __restrict__ counters, int64_t 
                                   const double* __restrict__ vals_n, uint32_t* __restrict__ key,
                                   uint32_t* __restrict__ ex_j, double* __restrict__ ex_val,
                                   uint64_t* __restrict__ pay64, DeviceStatus* status) {
+    pdl_wait();
+    pdl_trigger();
     const int64_t ju = counters[0];
     int64_t H = counters[1];
     if (H > cap) {
@@ -155,6 +159,7 @@ __global__ void __launch_bounds__(kHsThreads) os_hist_kernel(int64_t* __restrict
     constexpr int kItems = 16;
     constexpr int kTile = kHsThreads * kItems;
     // per-warp histograms, so hot digits contend only within a warp
+    pdl_trigger();
     __shared__ uint32_t h[kHsWarps][4][256];
     for (int e = threadIdx.x; e < kHsWarps * 4 * 256; e += blockDim.x) (&h[0][0][0])[e] = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) counters[kSortEpochSlot] += 4;
@@ -240,6 +245,8 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
     __shared__ uint32_t gbase[256];   // digit start of this tile in the output
     __shared__ uint32_t wsum[kHsWarps];
     __shared__ int64_t tile_sh;
+    pdl_wait();
+    pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int shift = 8 * pass;
@@ -371,6 +378,8 @@ __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __r
                                                               uint32_t* __restrict__ chunk_seg,
                                                               uint32_t* __restrict__ rowbits) {
     __shared__ uint32_t wsum[kHsWarps];
+    pdl_wait();
+    pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int64_t H = hit_count(counters, cap);
@@ -445,6 +454,8 @@ __global__ void __launch_bounds__(1024) hs_headscan_kernel(const int64_t* __rest
                                                            int64_t* __restrict__ touched_count,
                                                            int64_t* __restrict__ seg_start) {
     __shared__ int64_t wsum[32];
+    pdl_wait();
+    pdl_trigger();
     const int64_t H = hit_count(counters, cap);
     const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -503,14 +514,14 @@ static int sort_keys(Session& s, int n, bool packed, cudaStream_t st) {
             const size_t smem = (sizeof(uint64_t) + sizeof(uint32_t)) * kHsThreads * IT;
             EXAFAC_CUDA_TRY(cudaFuncSetAttribute(os_downsweep_kernel<uint64_t, IT>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            os_downsweep_kernel<uint64_t, IT><<<kHsDownGridPacked, kHsThreads, smem, st>>>(
-                s.counters, cap, s.hit_key[src], s.pay64[src], p, s.os_aux, s.os_status, s.hit_key[dst], s.pay64[dst],
-                s.status);
+            EXAFAC_CUDA_TRY(launch_dependent(os_downsweep_kernel<uint64_t, IT>, kHsDownGridPacked, kHsThreads, smem, st,
+                                             s.counters, cap, s.hit_key[src], s.pay64[src], p, s.os_aux, s.os_status,
+                                             s.hit_key[dst], s.pay64[dst], s.status));
         } else {
             const size_t smem = (sizeof(uint32_t) + sizeof(uint32_t)) * kHsTile;
-            os_downsweep_kernel<uint32_t, kHsItems><<<kHsDownGrid, kHsThreads, smem, st>>>(
-                s.counters, cap, s.hit_key[src], p == 0 ? nullptr : s.hit_pay[src], p, s.os_aux, s.os_status,
-                s.hit_key[dst], s.hit_pay[dst], s.status);
+            EXAFAC_CUDA_TRY(launch_dependent(os_downsweep_kernel<uint32_t, kHsItems>, kHsDownGrid, kHsThreads, smem, st,
+                                             s.counters, cap, s.hit_key[src], p == 0 ? nullptr : s.hit_pay[src], p,
+                                             s.os_aux, s.os_status, s.hit_key[dst], s.hit_pay[dst], s.status));
         }
         count_launch();
         EXAFAC_CHECK_LAUNCH();
@@ -532,19 +543,21 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
     expand_owner_kernel<<<152 * 4, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_len, s.expand_first);
     count_launch();
     if (packed)
-        hit_expand_kernel<true><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, s.expand_first, L.rows,
-                                                         L.vals, s.hit_key[0], nullptr, nullptr, s.pay64[0], s.status);
+        EXAFAC_CUDA_TRY(launch_dependent(hit_expand_kernel<true>, 152 * 8, 256, 0, st, s.counters, cap, s.f_off,
+                                         s.f_start, s.expand_first, L.rows, L.vals, s.hit_key[0], nullptr, nullptr,
+                                         s.pay64[0], s.status));
     else
-        hit_expand_kernel<false><<<152 * 8, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_start, s.expand_first,
-                                                          L.rows, L.vals, s.hit_key[0], s.ex_j, s.ex_val, nullptr,
-                                                          s.status);
+        EXAFAC_CUDA_TRY(launch_dependent(hit_expand_kernel<false>, 152 * 8, 256, 0, st, s.counters, cap, s.f_off,
+                                         s.f_start, s.expand_first, L.rows, L.vals, s.hit_key[0], s.ex_j, s.ex_val,
+                                         nullptr, s.status));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(sort_keys(s, n, packed, st));
-    hs_heads_kernel<false><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, s.head_cnt, nullptr,
-                                                          nullptr, nullptr, nullptr, nullptr);
+    EXAFAC_CUDA_TRY(launch_dependent(hs_heads_kernel<false>, kHsGrid, kHsThreads, 0, st, s.counters, cap, s.key_sorted,
+                                     s.head_cnt, nullptr, nullptr, nullptr, nullptr, nullptr));
     count_launch();
-    hs_headscan_kernel<<<1, 1024, 0, st>>>(s.counters, cap, s.head_cnt, s.head_base, s.counters + 2, s.seg_start);
+    EXAFAC_CUDA_TRY(launch_dependent(hs_headscan_kernel, 1, 1024, 0, st, s.counters, cap, s.head_cnt, s.head_base,
+                                     s.counters + 2, s.seg_start));
     count_launch();
     EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowbits, 0, sizeof(uint32_t) * ceil_div(s.dims[n], 32), st));
     hs_heads_kernel<true><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, nullptr, s.head_base,

@@ -127,6 +127,8 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
                                                      const uint32_t* __restrict__ keys,
                                                      const TA* __restrict__ carry_first,
                                                      const TA* __restrict__ carry_last, TA* __restrict__ Mc) {
+    pdl_wait();
+    pdl_trigger();
     const int64_t H = min(counters[1], cap);
     const int64_t nchunks = (H + kChunk - 1) / kChunk;
     const int lane = threadIdx.x & 31;
@@ -339,6 +341,7 @@ __global__ void __launch_bounds__(256) segreduce_f32_kernel(const int64_t* __res
                                                             float4* __restrict__ carry_last4,
                                                             uint32_t* __restrict__ carry_row,
                                                             uint32_t* __restrict__ carry_seg) {
+    pdl_trigger();
     constexpr int C = kSegChunkF32;
     const int64_t H = min(counters[1], cap);
     const int64_t nchunks = (H + C - 1) / C;
@@ -608,8 +611,8 @@ static int segmented_mttkrp(Session& s, cudaStream_t st) {
         }
 #undef EXAFAC_SEG_F32
         count_launch();
-        segfix_kernel<float, kSegChunkF32><<<hb, 256, 0, st>>>(R, RS, s.counters, s.nnz, s.carry_row, s.carry_seg,
-                                                               s.seg_start, s.key_sorted, cf, cl, Mc);
+        EXAFAC_CUDA_TRY(launch_dependent(segfix_kernel<float, kSegChunkF32>, hb, 256, 0, st, R, RS, s.counters, s.nnz,
+                                         s.carry_row, s.carry_seg, s.seg_start, s.key_sorted, cf, cl, Mc));
         count_launch();
     }
     EXAFAC_CHECK_LAUNCH();
@@ -681,6 +684,8 @@ __global__ void __launch_bounds__(kMmaWarps * 32) solve_gram_mma_kernel(int R, c
     float (*phh)[PS] = reinterpret_cast<float (*)[PS]>(mma_dyn + kMmaWarps * S::kWarpBytes);
     float (*phl)[PS] = phh + KP;
     __shared__ __align__(8) uint64_t bars[kMmaWarps];
+    pdl_wait();
+    pdl_trigger();
     const int P = R * (R + 1) / 2;
     const int ldm = f32_row_stride(R);  // Mc / Uc row stride
     const uint32_t row_bytes = (uint32_t)(sizeof(float) * ldm);
@@ -874,6 +879,8 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) normlev_f32_kernel(int R,
     __shared__ __align__(16) float psm[KC][KC];
     __shared__ __align__(16) float tile[kSolveWarps][32][kTileStride];
     __shared__ float sg[32];
+    pdl_wait();
+    pdl_trigger();
     // A zero column norm: write the unscaled rows and leave the division of
     // every row (as the reference does) to scale_rows_if_degenerate.
     const bool deg = *degenerate != 0;
@@ -976,16 +983,20 @@ static int launch_solve_f32(Session& s, int n, cudaStream_t st) {
     const size_t smem = MmaShape<KC>::kSmem;
     EXAFAC_CUDA_TRY(
         cudaFuncSetAttribute(solve_gram_mma_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    solve_gram_mma_kernel<KC><<<kMmaBlocks, kMmaWarps * 32, smem, st>>>(
-        s.R, s.counters, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.Uc, s.part, s.status);
+    // follows segfix, unless a dense factor was cleared in between
+    EXAFAC_CUDA_TRY(launch_dependent_if(!s.dense[n], solve_gram_mma_kernel<KC>, kMmaBlocks, kMmaWarps * 32, smem, st,
+                                        s.R, s.counters, reinterpret_cast<const float*>(s.Mc), s.dpinv, s.Uc, s.part,
+                                        s.status));
     return EXAFAC_OK;
 }
 
 template <int KC>
-static void launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
-    normlev_f32_kernel<KC><<<kNormlevBlocks, kSolveWarps * 32, 0, st>>>(
-        s.R, s.counters, s.touched, s.Uc, s.F.sigma, arls ? s.upinv : nullptr, reinterpret_cast<int*>(s.counters + 6),
-        s.F.U[n], arls ? s.scores[n] : nullptr, s.scores_c);
+static int launch_normlev_f32(Session& s, int n, bool arls, cudaStream_t st) {
+    EXAFAC_CUDA_TRY(launch_dependent(normlev_f32_kernel<KC>, kNormlevBlocks, kSolveWarps * 32, 0, st, s.R, s.counters,
+                                     s.touched, (const float*)s.Uc, s.F.sigma, arls ? s.upinv : nullptr,
+                                     reinterpret_cast<int*>(s.counters + 6), s.F.U[n], arls ? s.scores[n] : nullptr,
+                                     s.scores_c));
+    return EXAFAC_OK;
 }
 
 static int solve_f32(Session& s, int n, cudaStream_t st) {
@@ -1053,9 +1064,9 @@ int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st) {
                                          s.upinv, 1e-11, s.vt, st));
     else
         EXAFAC_TRY(sigma_and_gram(s, st));
-    if (R <= 16) launch_normlev_f32<16>(s, n, arls, st);
-    else if (R <= 28) launch_normlev_f32<28>(s, n, arls, st);
-    else launch_normlev_f32<32>(s, n, arls, st);
+    if (R <= 16) EXAFAC_TRY(launch_normlev_f32<16>(s, n, arls, st));
+    else if (R <= 28) EXAFAC_TRY(launch_normlev_f32<28>(s, n, arls, st));
+    else EXAFAC_TRY(launch_normlev_f32<32>(s, n, arls, st));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return scale_rows_if_degenerate(s, n, st);

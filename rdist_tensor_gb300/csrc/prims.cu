@@ -61,6 +61,8 @@ template <typename Tin, typename Tacc>
 __global__ void scan_block_sums(const Tin* __restrict__ in, int64_t n, Tacc* __restrict__ partial,
                                 const uint32_t* __restrict__ gather = nullptr, const int64_t* n_dev = nullptr) {
     __shared__ Tacc red[33];
+    pdl_wait();
+    pdl_trigger();
     if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     if (base >= n) {  // uniform per block
@@ -83,6 +85,8 @@ __global__ void scan_block_sums(const Tin* __restrict__ in, int64_t n, Tacc* __r
 template <typename Tacc>
 __global__ void scan_partials_kernel(Tacc* partial, int64_t nb, Tacc* total) {
     __shared__ Tacc red[33];
+    pdl_wait();
+    pdl_trigger();
     Tacc carry = 0;
     for (int64_t base = 0; base < nb; base += blockDim.x) {
         int64_t i = base + threadIdx.x;
@@ -114,6 +118,8 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
     __shared__ Tacc tile[kScanTile + kScanTile / 16];
     __shared__ Tacc red[33];
     __shared__ Tacc fold[2];
+    pdl_wait();
+    pdl_trigger();
     if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     Tacc prefix = 0, all = 0;
@@ -194,7 +200,10 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
 constexpr int64_t kFoldMaxBlocks = 2048;
 
 template <typename Tacc>
-__global__ void accumulate_total(int64_t* accum, const Tacc* total) { *accum += (int64_t)*total; }
+__global__ void accumulate_total(int64_t* accum, const Tacc* total) {
+    pdl_wait();
+    *accum += (int64_t)*total;
+}
 
 template <typename Tin, typename Tacc, bool kInclusive>
 static int scan_impl(const Tin* in, Tacc* out, int64_t n, Tacc* total, void* scratch, cudaStream_t s,
@@ -207,12 +216,17 @@ static int scan_impl(const Tin* in, Tacc* out, int64_t n, Tacc* total, void* scr
     Tacc* partial = reinterpret_cast<Tacc*>(scratch);
     scan_block_sums<Tin, Tacc><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial); count_launch();
     if (nb <= kFoldMaxBlocks) {  // each block folds the block sums itself: no partials kernel
-        scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, nullptr, nullptr,
-                                                                              nullptr, nb, total, accum);
+        EXAFAC_CUDA_TRY(launch_dependent(scan_apply<Tin, Tacc, kInclusive>, (unsigned)nb, kScanThreads, 0, s, in, out,
+                                         n, partial, nullptr, nullptr, nullptr, nb, total, accum));
     } else {
-        scan_partials_kernel<Tacc><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
-        if (accum) accumulate_total<<<1, 1, 0, s>>>(accum, total), count_launch();
-        scan_apply<Tin, Tacc, kInclusive><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial);
+        EXAFAC_CUDA_TRY(launch_dependent(scan_partials_kernel<Tacc>, 1, 1024, 0, s, partial, nb, total));
+        count_launch();
+        if (accum) {
+            EXAFAC_CUDA_TRY(launch_dependent(accumulate_total<Tacc>, 1, 1, 0, s, accum, (const Tacc*)total));
+            count_launch();
+        }
+        EXAFAC_CUDA_TRY(launch_dependent(scan_apply<Tin, Tacc, kInclusive>, (unsigned)nb, kScanThreads, 0, s, in, out,
+                                         n, (const Tacc*)partial, nullptr, nullptr, nullptr, 0, nullptr, nullptr));
     }
     count_launch();
     EXAFAC_CHECK_LAUNCH();
@@ -238,9 +252,11 @@ int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* 
     count_launch();
     // (the grid is sized for the mode, most blocks past the touched count:
     // folding there would cost every block a pass over all partials)
-    scan_partials_kernel<double><<<1, 1024, 0, s>>>(partial, nb, total); count_launch();
-    scan_apply<double, double, true, true><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partial, total, gather,
-                                                                                   n_dev);
+    EXAFAC_CUDA_TRY(launch_dependent(scan_partials_kernel<double>, 1, 1024, 0, s, partial, nb, total));
+    count_launch();
+    EXAFAC_CUDA_TRY(launch_dependent(scan_apply<double, double, true, true>, (unsigned)nb, kScanThreads, 0, s, in, out,
+                                     n, (const double*)partial, (const double*)total, gather, n_dev, 0, nullptr,
+                                     nullptr));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

@@ -86,6 +86,8 @@ __global__ void cdf_sequential_kernel(const double* __restrict__ w, int64_t n, d
 // b/B and floor(u B) are exact.
 __global__ void cdf_guide_kernel(const double* __restrict__ cdf, int64_t n, uint32_t* __restrict__ guide,
                                  const int64_t* __restrict__ n_dev) {
+    pdl_wait();
+    pdl_trigger();
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > kGuideBuckets) return;
     if (n_dev) n = min(n, *n_dev);
@@ -133,7 +135,8 @@ int arls_build_cdf(Session& s, int k, const uint32_t* list, const int64_t* count
     } else {
         EXAFAC_TRY(scan_cdf_f64(w, s.cdf[k], n, s.cdf_total + k, s.scan_sc, st, nullptr, count_dev));
     }
-    cdf_guide_kernel<<<(unsigned)ceil_div(kGuideBuckets + 1, 256), 256, 0, st>>>(s.cdf[k], n, s.guide[k], count_dev);
+    EXAFAC_CUDA_TRY(launch_dependent(cdf_guide_kernel, (unsigned)ceil_div(kGuideBuckets + 1, 256), 256, 0, st,
+                                     (const double*)s.cdf[k], n, s.guide[k], count_dev));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

@@ -42,6 +42,7 @@ __device__ __forceinline__ bool keys_equal(Key128 a, Key128 b) { return a.lo == 
 __global__ void dedup_insert_kernel(KeySpec spec, int64_t J, const uint32_t* __restrict__ samples, int64_t mask,
                                     int32_t* owner, int32_t* minj, int32_t* count, int32_t* __restrict__ slot_of,
                                     Key128* dkey) {
+    pdl_trigger();
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= J) return;
     const Key128 key = pack_key(spec, samples + j * spec.N);
@@ -87,6 +88,8 @@ __global__ void __launch_bounds__(256) dedup_count_kernel(int64_t J, const int32
                                                           const int32_t* __restrict__ slot_of,
                                                           uint32_t* __restrict__ tile_count) {
     __shared__ uint32_t wsum[8];
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t j0 = (int64_t)blockIdx.x * kDedupTile + 4 * threadIdx.x;
     uint32_t c = (uint32_t)__popc(dedup_rep_bits(J, j0, minj, slot_of));
@@ -110,6 +113,8 @@ __global__ void __launch_bounds__(256) dedup_place_kernel(int N, int64_t J, int6
                                                           const double* __restrict__ weights,
                                                           uint32_t* __restrict__ sd, double* __restrict__ wd,
                                                           int64_t* __restrict__ ju_out) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ uint32_t wsum[8];
     __shared__ int64_t before_sh;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -171,9 +176,11 @@ int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
     dedup_insert_kernel<<<blocks, 256, 0, st>>>(s.look[n].spec, J, s.samples, s.dtab - 1, s.d_owner, s.d_minj,
                                                 s.d_count, s.slot_of, s.dkey); count_launch();
     const int64_t ntiles = ceil_div(J, kDedupTile);
-    dedup_count_kernel<<<(unsigned)ntiles, 256, 0, st>>>(J, s.d_minj, s.slot_of, s.flags); count_launch();
-    dedup_place_kernel<<<(unsigned)ntiles, 256, 0, st>>>(s.N, J, ntiles, s.flags, s.d_minj, s.slot_of, s.d_count,
-                                                         s.samples, s.weights, s.sd, s.wd, s.counters + 0);
+    EXAFAC_CUDA_TRY(launch_dependent(dedup_count_kernel, (unsigned)ntiles, 256, 0, st, J, s.d_minj, s.slot_of, s.flags));
+    count_launch();
+    EXAFAC_CUDA_TRY(launch_dependent(dedup_place_kernel, (unsigned)ntiles, 256, 0, st, s.N, J, ntiles, s.flags,
+                                     s.d_minj, s.slot_of, s.d_count, s.samples, s.weights, s.sd, s.wd,
+                                     s.counters + 0));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
@@ -184,6 +191,8 @@ int dedup(Session& s, int n, int64_t J, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 __global__ void gram_reduce_kernel(const double* __restrict__ part, int64_t nblk, int R, double* __restrict__ out) {
     __shared__ double red[256];
+    pdl_wait();
+    pdl_trigger();
     const int P = packed_size(R);
     const int e = blockIdx.x;
     if (e >= P) return;
@@ -625,6 +634,7 @@ template <typename Slot>
 __global__ void lookup_kernel(KeySpec spec, int64_t J, const int64_t* __restrict__ ju_dev,
                               const uint32_t* __restrict__ sd, const Slot* __restrict__ slots, int64_t mask,
                               uint32_t* __restrict__ f_start, uint32_t* __restrict__ f_len) {
+    pdl_trigger();
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= J) return;
     uint32_t start = 0, len = 0;
@@ -751,6 +761,8 @@ __global__ void sigma_kernel(int R, const double* __restrict__ ugram, double* __
 __global__ void scale_rows_kernel(int R, int64_t I, const uint32_t* __restrict__ list, const int64_t* __restrict__ cnt_dev,
                                   const double* __restrict__ sigma, const int* __restrict__ degenerate,
                                   double* __restrict__ U, int only_degenerate) {
+    pdl_wait();
+    pdl_trigger();
     if (only_degenerate && *degenerate == 0) return;
     const bool all = *degenerate != 0 || list == nullptr;
     const int64_t rows = all ? I : *cnt_dev;
@@ -791,8 +803,8 @@ int sigma_and_gram(Session& s, cudaStream_t st) {
 // the rows outside the touched list turn into NaN there too.  Exits at once
 // unless a norm is zero.
 int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st) {
-    scale_rows_kernel<<<152 * 4, 256, 0, st>>>(s.R, s.dims[n], nullptr, s.counters + 2, s.F.sigma,
-                                               reinterpret_cast<int*>(s.counters + 6), s.F.U[n], 1);
+    EXAFAC_CUDA_TRY(launch_dependent(scale_rows_kernel, 152 * 4, 256, 0, st, s.R, s.dims[n], nullptr, s.counters + 2,
+                                     s.F.sigma, reinterpret_cast<int*>(s.counters + 6), s.F.U[n], 1));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
@@ -802,6 +814,8 @@ int scale_rows_if_degenerate(Session& s, int n, cudaStream_t st) {
 // nzcount[n]): only the counters[2] listed entries are copied.
 __global__ void keep_touched_kernel(const int64_t* __restrict__ counters, const uint32_t* __restrict__ touched,
                                     uint32_t* __restrict__ list, int64_t* __restrict__ count) {
+    pdl_wait();
+    pdl_trigger();
     const int64_t T = counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) *count = T;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += (int64_t)gridDim.x * blockDim.x)
@@ -809,7 +823,9 @@ __global__ void keep_touched_kernel(const int64_t* __restrict__ counters, const 
 }
 
 int keep_touched(Session& s, int n, cudaStream_t st) {
-    keep_touched_kernel<<<152 * 4, 256, 0, st>>>(s.counters, s.touched, s.nzrows[n], s.nzcount + n);
+    // follows the CDF build's last kernel (CP-ARLS-LEV)
+    EXAFAC_CUDA_TRY(launch_dependent_if(s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV, keep_touched_kernel, 152 * 4, 256,
+                                        0, st, s.counters, s.touched, s.nzrows[n], s.nzcount + n));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
