@@ -108,8 +108,10 @@ __device__ __forceinline__ int scan_pad(int i) { return i + (i >> 4); }
 // fold_nb > 0: partial[] holds the nb = fold_nb raw block sums (no partials
 // kernel ran): every block adds those before it itself, in a fixed order, and
 // the total of all of them (the same value in every block); block 0 writes it
-// to *total_out and adds it to *accum when given.  fold_nb == 0: partial[]
-// holds the scanned prefixes and *total the total.
+// to *total_out and adds it to *accum when given.  Only the blocks holding
+// elements (those below n, after the n_dev cap) take part; the others exit at
+// once.  fold_nb == 0: partial[] holds the scanned prefixes and *total the
+// total.
 template <typename Tin, typename Tacc, bool kInclusive, bool kNormalize = false>
 __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, int64_t n,
                            const Tacc* __restrict__ partial, const Tacc* __restrict__ total = nullptr,
@@ -124,8 +126,10 @@ __global__ void scan_apply(const Tin* __restrict__ in, Tacc* __restrict__ out, i
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     Tacc prefix = 0, all = 0;
     if (fold_nb > 0) {
+        if (base >= n && blockIdx.x != 0) return;  // uniform per block; block 0 always writes the total
+        const int64_t nb_act = min(fold_nb, (n + kScanTile - 1) / kScanTile);
         Tacc a = 0, t = 0;
-        for (int64_t i = threadIdx.x; i < fold_nb; i += kScanThreads) {
+        for (int64_t i = threadIdx.x; i < nb_act; i += kScanThreads) {
             const Tacc v = partial[i];
             t += v;
             if (i < (int64_t)blockIdx.x) a += v;
@@ -250,13 +254,18 @@ int scan_cdf_f64(const double* in, double* out, int64_t n, double* total, void* 
     double* partial = reinterpret_cast<double*>(scratch);
     scan_block_sums<double, double><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial, gather, n_dev);
     count_launch();
-    // (the grid is sized for the mode, most blocks past the touched count:
-    // folding there would cost every block a pass over all partials)
-    EXAFAC_CUDA_TRY(launch_dependent(scan_partials_kernel<double>, 1, 1024, 0, s, partial, nb, total));
-    count_launch();
-    EXAFAC_CUDA_TRY(launch_dependent(scan_apply<double, double, true, true>, (unsigned)nb, kScanThreads, 0, s, in, out,
-                                     n, (const double*)partial, (const double*)total, gather, n_dev, 0, nullptr,
-                                     nullptr));
+    if (nb <= kFoldMaxBlocks) {
+        // the grid is sized for the mode; only the blocks below the listed
+        // count fold their predecessors' sums
+        EXAFAC_CUDA_TRY(launch_dependent(scan_apply<double, double, true, true>, (unsigned)nb, kScanThreads, 0, s, in,
+                                         out, n, (const double*)partial, nullptr, gather, n_dev, nb, total, nullptr));
+    } else {
+        EXAFAC_CUDA_TRY(launch_dependent(scan_partials_kernel<double>, 1, 1024, 0, s, partial, nb, total));
+        count_launch();
+        EXAFAC_CUDA_TRY(launch_dependent(scan_apply<double, double, true, true>, (unsigned)nb, kScanThreads, 0, s, in,
+                                         out, n, (const double*)partial, (const double*)total, gather, n_dev, 0,
+                                         nullptr, nullptr));
+    }
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
