@@ -221,6 +221,7 @@ __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __r
     extern __shared__ double smem[];
     __shared__ int fail;
     __shared__ double fro;
+    __shared__ double fro_w[32];  // per-warp parts, summed in warp order (no atomics: the result repeats)
     double* L = smem;
     double* Li = smem + R * R;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -275,7 +276,13 @@ __global__ void spd_pinv_kernel(int R, const double* __restrict__ A, double* __r
             part += acc * acc;
         }
         part = warp_sum(part);
-        if ((tid & 31) == 0) atomicAdd(&fro, part);
+        if ((tid & 31) == 0) fro_w[tid >> 5] = part;
+        __syncthreads();
+        if (tid == 0) {
+            double f = 0.0;
+            for (int q = 0; q < (nt + 31) / 32; q++) f += fro_w[q];
+            fro = f;
+        }
         __syncthreads();
         const double bound = 1.0 / sqrt(fro);
         if (isfinite(fro) && bound > 10.0 * tol) {
@@ -387,6 +394,7 @@ __device__ void pinv_small_block(int R, const double* __restrict__ A, double* __
     __shared__ int bad;
     __shared__ double Xs[kSmallPinvMaxR][kSmallPinvMaxR + 1];
     __shared__ double fro;
+    __shared__ double fro_w[kSmallPinvThreads / 32];  // per-warp parts, summed in warp order
     if (refine == 2 && pinv_sweep_f32(R, A, out)) return;
     const int tid = threadIdx.x;
     const int P = R * (R + 1) / 2;
@@ -456,7 +464,13 @@ __device__ void pinv_small_block(int R, const double* __restrict__ A, double* __
             Xs[jj[m]][ii[m]] = x;
         }
         part = warp_sum(part);
-        if ((tid & 31) == 0) atomicAdd(&fro, part);
+        if ((tid & 31) == 0) fro_w[tid >> 5] = part;
+        __syncthreads();
+        if (tid == 0) {
+            double f = 0.0;
+            for (int q = 0; q < kSmallPinvThreads / 32; q++) f += fro_w[q];
+            fro = f;
+        }
         __syncthreads();
         ok = isfinite(fro) && 1.0 / sqrt(fro) > 10.0 * tol;
     }

@@ -132,9 +132,7 @@ struct Session {
     uint64_t* pay64[2] = {nullptr, nullptr};    // nnz each, mixed forms: packed (sample, FP32 value) (ping-pong)
     const uint64_t* pay64_sorted = nullptr;     // the sorted packed hits (mixed forms)
     uint64_t* os_status = nullptr;    // tile stride x 256: look-back status words of the row sort
-    uint32_t* os_aux = nullptr;       // 4 tile counters + 4 x 256 digit histograms of the row sort
-    uint32_t* head_cnt = nullptr;     // chunks: touched-row starts per chunk of sorted hits
-    int64_t* head_base = nullptr;     // chunks: their exclusive scan
+    uint32_t* os_aux = nullptr;       // row sort: 4 tile counters, 4 x 256 digit histograms; run pass: 1 tile counter
     double* Mc = nullptr;             // Imax x R: MTTKRP rows, indexed by row
     double* carry_first = nullptr;  // chunks x kCarryStride
     double* carry_last = nullptr;   // chunks x kCarryStride

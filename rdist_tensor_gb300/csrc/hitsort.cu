@@ -150,7 +150,7 @@ __device__ __forceinline__ uint32_t block256_exclusive(uint32_t v, uint32_t* wsu
 // counts its items by multi-split (one shared-memory add per distinct digit
 // of a round), each block adds its histograms once (aux cleared beforehand:
 // the passes' tile counters aux[0..3] and the histograms aux[4..]).  Block 0
-// also advances the look-back epoch (counters[kSortEpochSlot] += 4): every
+// also advances the look-back epoch (counters[kSortEpochSlot] += 5): every
 // pass of this sort marks its status words with a fresh epoch, so the status
 // array is never cleared.
 __global__ void __launch_bounds__(kHsThreads) os_hist_kernel(int64_t* __restrict__ counters, int64_t cap,
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kHsThreads) os_hist_kernel(int64_t* __restrict
     pdl_trigger();
     __shared__ uint32_t h[kHsWarps][4][256];
     for (int e = threadIdx.x; e < kHsWarps * 4 * 256; e += blockDim.x) (&h[0][0][0])[e] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters[kSortEpochSlot] += 4;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[kSortEpochSlot] += 5;
     __syncthreads();
     const int64_t H = hit_count(counters, cap);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -363,28 +363,51 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
     }
 }
 
-// Run heads (first hit of a row) of the sorted keys, per tile: the tile's
-// count, or (compact) the heads themselves written to touched / seg_start at
-// the tile's base and marked in the step's row bitmap (rowbits, cleared
-// beforehand), and for every chunk of kSegChunkF32 hits the index of the run
-// holding its first hit (chunk_seg).  Same item order as the downsweep.
-template <bool kCompact>
-__global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __restrict__ counters, int64_t cap,
-                                                              const uint32_t* __restrict__ keys,
-                                                              uint32_t* __restrict__ tile_heads,
-                                                              const int64_t* __restrict__ tile_base,
-                                                              uint32_t* __restrict__ touched,
-                                                              int64_t* __restrict__ seg_start,
-                                                              uint32_t* __restrict__ chunk_seg,
-                                                              uint32_t* __restrict__ rowbits) {
+// Runs of equal rows in the sorted keys, in one pass: each tile of kHsTile
+// hits (claimed in order through aux[kRunsTileSlot]) counts its run heads
+// (first hit of a row), publishes the count in its status word (slot 0 of
+// its status row, under the sort's epoch + 4: the digit passes use + 0..3)
+// and takes its exclusive prefix from a warp-wide look-back over earlier
+// tiles, which have all been claimed by running blocks and publish their
+// counts before they look back themselves.  It then writes its heads to
+// touched / seg_start at that prefix, marks their rows in the step's row
+// bitmap (rowbits, cleared beforehand) and, for every chunk of kSegChunkF32
+// hits, records the index of the run holding its first hit (chunk_seg).  The
+// last tile writes the number of runs T to *touched_count and seg_start[T] =
+// H.  A look-back wait that outlasts kSpinLimit polls records an error and
+// counts as a zero prefix (the output is then invalid, and reported).
+constexpr int kRunsTileSlot = 4 + 4 * 256;  // in os_aux, after the sort's tile counters and histograms
+
+__global__ void __launch_bounds__(kHsThreads) hs_runs_kernel(const int64_t* __restrict__ counters, int64_t cap,
+                                                             const uint32_t* __restrict__ keys,
+                                                             uint32_t* __restrict__ aux, uint64_t* __restrict__ status,
+                                                             uint32_t* __restrict__ touched,
+                                                             int64_t* __restrict__ seg_start,
+                                                             uint32_t* __restrict__ chunk_seg,
+                                                             uint32_t* __restrict__ rowbits,
+                                                             int64_t* __restrict__ touched_count, DeviceStatus* err) {
     __shared__ uint32_t wsum[kHsWarps];
+    __shared__ int64_t tile_sh;
+    __shared__ uint32_t excl_sh;
     pdl_wait();
     pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int64_t H = hit_count(counters, cap);
     const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint64_t epoch = (uint64_t)(uint32_t)(counters[kSortEpochSlot] + 4) << 32;
+    if (ntiles == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            *touched_count = 0;
+            seg_start[0] = 0;
+        }
+        return;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) tile_sh = (int64_t)atomicAdd(&aux[kRunsTileSlot], 1u);
+        __syncthreads();
+        const int64_t t = tile_sh;
+        if (t >= ntiles) break;  // uniform
         const int64_t base = t * kHsTile + (int64_t)w * 32 * kHsItems;
         unsigned heads[kHsItems];
         uint32_t kk[kHsItems];
@@ -403,82 +426,86 @@ __global__ void __launch_bounds__(kHsThreads) hs_heads_kernel(const int64_t* __r
         }
         if (lane == 0) wsum[w] = n;
         __syncthreads();
-        if (!kCompact) {
-            if (threadIdx.x == 0) {
-                uint32_t s = 0;
-                for (int ww = 0; ww < kHsWarps; ww++) s += wsum[ww];
-                tile_heads[t] = s;
-            }
-        } else {
-            int64_t at = tile_base[t];
-            for (int ww = 0; ww < w; ww++) at += wsum[ww];
+        if (w == 0) {
+            uint32_t run = 0;
 #pragma unroll
-            for (int r = 0; r < kHsItems; r++) {
-                const bool hd = (heads[r] >> lane) & 1u;
-                if (hd) {
-                    const int64_t q = at + __popc(heads[r] & lt);
-                    touched[q] = kk[r];
-                    seg_start[q] = base + r * 32 + lane;
-                }
-                {  // the step's row bitmap: the round's rows are sorted, so equal
-                    // 32-row words are runs of lanes; a segmented OR-scan leaves each
-                    // run's bits in its last lane, which makes the one atomic
-                    const unsigned word = kk[r] >> 5;
-                    unsigned bits = hd ? 1u << (kk[r] & 31) : 0u;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const unsigned b = __shfl_up_sync(0xffffffffu, bits, o);
-                        const unsigned wo = __shfl_up_sync(0xffffffffu, word, o);
-                        if (lane >= o && wo == word) bits |= b;
+            for (int ww = 0; ww < kHsWarps; ww++) run += wsum[ww];
+            uint64_t* my = status + t * 256;
+            uint32_t excl = 0;
+            if (t == 0) {
+                if (lane == 0) os_store(my, epoch | kStatPrefix | run);
+            } else {
+                if (lane == 0) os_store(my, epoch | kStatAgg | run);
+                // windows of 32 predecessors, lane q on tile top - q
+                bool done = false;
+                for (int64_t top = t - 1; top >= 0 && !done; top -= 32) {
+                    const int64_t src_t = top - lane;
+                    uint64_t x = epoch | kStatAgg;  // lanes past tile 0 hold a zero count
+                    if (src_t >= 0) {
+                        const uint64_t* src = status + src_t * 256;
+                        x = os_load(src);
+                        for (uint32_t it = 0; (x & 0xffffffff00000000ull) != epoch; it++) {
+                            // give up after kSpinLimit polls, or at once when another wait already did
+                            if (it >= kSpinLimit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
+                                report(err, EXAFAC_ERR_DEVICE, 12, src_t, t);
+                                x = epoch | kStatPrefix;
+                                break;
+                            }
+                            if (it >= 32) __nanosleep(64);
+                            x = os_load(src);
+                        }
                     }
-                    const unsigned wn = __shfl_down_sync(0xffffffffu, word, 1);
-                    if (bits && (lane == 31 || wn != word)) atomicOr(&rowbits[word], bits);
+                    const unsigned pm = __ballot_sync(0xffffffffu, ((uint32_t)x & kStatPrefix) != 0);
+                    // the nearest prefix (lowest lane) ends the look-back: lanes up to it count
+                    const int last = pm ? __ffs(pm) - 1 : 31;
+                    uint32_t v = lane <= last ? ((uint32_t)x & kStatValue) : 0u;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    excl += v;
+                    done = pm != 0;
                 }
-                // a round that starts a chunk of kSegChunkF32 hits: the index
-                // of the run holding its first hit
-                if (lane == 0 && base + r * 32 < H && (base + r * 32) % kSegChunkF32 == 0)
-                    chunk_seg[(base + r * 32) / kSegChunkF32] = (uint32_t)(at + (heads[r] & 1u) - 1);
-                at += __popc(heads[r]);
+                if (lane == 0) os_store(my, epoch | kStatPrefix | (excl + run));
+            }
+            if (lane == 0) {
+                excl_sh = excl;
+                if (t == ntiles - 1) {
+                    *touched_count = (int64_t)excl + run;
+                    seg_start[(int64_t)excl + run] = H;
+                }
             }
         }
         __syncthreads();
-    }
-}
-
-// One block: exclusive scan of the per-tile head counts into tile_base; the
-// number of runs T to *touched_count and seg_start[T] = H.  Thread i scans a
-// contiguous slice of the tiles.
-__global__ void __launch_bounds__(1024) hs_headscan_kernel(const int64_t* __restrict__ counters, int64_t cap,
-                                                           const uint32_t* __restrict__ tile_heads,
-                                                           int64_t* __restrict__ tile_base,
-                                                           int64_t* __restrict__ touched_count,
-                                                           int64_t* __restrict__ seg_start) {
-    __shared__ int64_t wsum[32];
-    pdl_wait();
-    pdl_trigger();
-    const int64_t H = hit_count(counters, cap);
-    const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t per = (ntiles + blockDim.x - 1) / blockDim.x;
-    const int64_t i0 = min(ntiles, (int64_t)threadIdx.x * per), i1 = min(ntiles, i0 + per);
-    int64_t sum = 0;
-    for (int64_t i = i0; i < i1; i++) sum += tile_heads[i];
-    const int64_t inc = warp_inclusive(sum);
-    if (lane == 31) wsum[w] = inc;
-    __syncthreads();
-    int64_t pre = 0, all = 0;
-    for (int ww = 0; ww < 32; ww++) {
-        pre += (ww < w) ? wsum[ww] : 0;
-        all += wsum[ww];
-    }
-    int64_t run = pre + inc - sum;
-    for (int64_t i = i0; i < i1; i++) {
-        tile_base[i] = run;
-        run += tile_heads[i];
-    }
-    if (threadIdx.x == 0) {
-        *touched_count = all;
-        seg_start[all] = H;
+        int64_t at = excl_sh;
+        for (int ww = 0; ww < w; ww++) at += wsum[ww];
+#pragma unroll
+        for (int r = 0; r < kHsItems; r++) {
+            const bool hd = (heads[r] >> lane) & 1u;
+            if (hd) {
+                const int64_t q = at + __popc(heads[r] & lt);
+                touched[q] = kk[r];
+                seg_start[q] = base + r * 32 + lane;
+            }
+            {  // the step's row bitmap: the round's rows are sorted, so equal
+                // 32-row words are runs of lanes; a segmented OR-scan leaves each
+                // run's bits in its last lane, which makes the one atomic
+                const unsigned word = kk[r] >> 5;
+                unsigned bits = hd ? 1u << (kk[r] & 31) : 0u;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned b = __shfl_up_sync(0xffffffffu, bits, o);
+                    const unsigned wo = __shfl_up_sync(0xffffffffu, word, o);
+                    if (lane >= o && wo == word) bits |= b;
+                }
+                const unsigned wn = __shfl_down_sync(0xffffffffu, word, 1);
+                if (bits && (lane == 31 || wn != word)) atomicOr(&rowbits[word], bits);
+            }
+            // a round that starts a chunk of kSegChunkF32 hits: the index
+            // of the run holding its first hit
+            if (lane == 0 && base + r * 32 < H && (base + r * 32) % kSegChunkF32 == 0)
+                chunk_seg[(base + r * 32) / kSegChunkF32] = (uint32_t)(at + (heads[r] & 1u) - 1);
+            at += __popc(heads[r]);
+        }
+        __syncthreads();
     }
 }
 
@@ -503,7 +530,7 @@ static int sort_keys(Session& s, int n, bool packed, cudaStream_t st) {
         return EXAFAC_ERR_ARG;
     }
     const int passes = std::max(1, (key_bits(s.dims[n]) + 7) / 8);
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.os_aux, 0, sizeof(uint32_t) * (4 + 4 * 256), st));
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.os_aux, 0, sizeof(uint32_t) * (kRunsTileSlot + 1), st));
     os_hist_kernel<<<kHistGrid, kHsThreads, 0, st>>>(s.counters, cap, s.hit_key[0], passes, s.os_aux);
     count_launch();
     int src = 0;
@@ -540,6 +567,7 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
         set_error("packed hits need a session in a mixed precision");
         return EXAFAC_ERR_ARG;
     }
+    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowbits, 0, sizeof(uint32_t) * ceil_div(s.dims[n], 32), st));
     expand_owner_kernel<<<152 * 4, 256, 0, st>>>(s.counters, cap, s.f_off, s.f_len, s.expand_first);
     count_launch();
     if (packed)
@@ -553,15 +581,9 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     EXAFAC_TRY(sort_keys(s, n, packed, st));
-    EXAFAC_CUDA_TRY(launch_dependent(hs_heads_kernel<false>, kHsGrid, kHsThreads, 0, st, s.counters, cap, s.key_sorted,
-                                     s.head_cnt, nullptr, nullptr, nullptr, nullptr, nullptr));
-    count_launch();
-    EXAFAC_CUDA_TRY(launch_dependent(hs_headscan_kernel, 1, 1024, 0, st, s.counters, cap, s.head_cnt, s.head_base,
-                                     s.counters + 2, s.seg_start));
-    count_launch();
-    EXAFAC_CUDA_TRY(cudaMemsetAsync(s.rowbits, 0, sizeof(uint32_t) * ceil_div(s.dims[n], 32), st));
-    hs_heads_kernel<true><<<kHsGrid, kHsThreads, 0, st>>>(s.counters, cap, s.key_sorted, nullptr, s.head_base,
-                                                         s.touched, s.seg_start, s.chunk_seg, s.rowbits);
+    EXAFAC_CUDA_TRY(launch_dependent(hs_runs_kernel, kHsGrid, kHsThreads, 0, st, s.counters, cap, s.key_sorted,
+                                     s.os_aux, s.os_status, s.touched, s.seg_start, s.chunk_seg, s.rowbits,
+                                     s.counters + 2, s.status));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

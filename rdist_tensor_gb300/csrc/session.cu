@@ -104,11 +104,9 @@ static void carve(Session& s) {
         if (s.cfg.precision != EXAFAC_PREC_FP64) s.pay64[b] = a.take<uint64_t>(nnz);
     }
     s.os_status = a.take<uint64_t>(256 * (int64_t)hitsort_tile_stride(nnz));
-    s.os_aux = a.take<uint32_t>(4 + 4 * 256);
+    s.os_aux = a.take<uint32_t>(4 + 4 * 256 + 1);
     s.Mc = a.take<double>(I * std::max(R, 16));  // FP64 rows of R, or FP32 rows padded to a multiple of 4
     const int64_t chunks = ceil_div(nnz, kSegChunkF32) + 1;
-    s.head_cnt = a.take<uint32_t>(chunks);
-    s.head_base = a.take<int64_t>(chunks);
     // carries: FP32 chunks of 32 hits x 32 columns, or FP64 chunks of 128 x
     // up to 128 columns (the exact MTTKRP at R > 32)
     const int64_t carry = std::max(chunks * kCarryStride,
