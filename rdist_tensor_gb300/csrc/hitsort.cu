@@ -29,8 +29,8 @@ constexpr int kHsItems = 16;
 constexpr int kHsTile = kHsThreads * kHsItems;  // 4096 hits per tile
 constexpr int kHsWarps = kHsThreads / 32;
 constexpr int kHsGrid = 152 * 4;      // heads
-constexpr int kHsDownGrid = 152 * 3;        // downsweep: one resident wave (256 threads)
-constexpr int kHsDownGridPacked = 152 * 3;  // 64-bit payloads, 16 items per thread
+constexpr int kHsDownGrid = 152 * 2;        // downsweep: one resident wave (256 threads)
+constexpr int kHsDownGridPacked = 152 * 2;  // 64-bit payloads, 16 items per thread
 constexpr int kHistGrid = 152 * 2;          // os_hist
 constexpr uint32_t kStatAgg = 1u << 30;     // look-back status: the tile's own count
 constexpr uint32_t kStatPrefix = 2u << 30;  // look-back status: the inclusive prefix
@@ -228,7 +228,7 @@ __device__ __forceinline__ void os_store(uint64_t* p, uint64_t v) {
 }
 
 template <typename PT, int ITEMS>
-__global__ void __launch_bounds__(kHsThreads, 3) os_downsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
+__global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t* __restrict__ counters, int64_t cap,
                                                                   const uint32_t* __restrict__ kin,
                                                                   const PT* __restrict__ pin, int pass,
                                                                   uint32_t* __restrict__ aux,
