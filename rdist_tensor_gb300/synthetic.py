@@ -113,9 +113,12 @@ def zipf_tensor_device(dims, nnz, alpha=1.2, values="lognormal", seed=0, max_rou
         raise ValueError("coordinates need more than 126 key bits")
     cdfs = []
     for d in dims:
-        k = torch.arange(1, d + 1, dtype=torch.float64, device=device)
-        c = torch.cumsum(k.pow(-alpha), 0)
-        cdfs.append(c / c[-1])
+        # Summed on the host, in order: a device scan need not add in the same
+        # order on every run, and a last-bit change of one CDF entry moves the
+        # rare draw that lands on it, which changes the tensor.
+        k = np.arange(1, d + 1, dtype=np.float64)
+        c = np.cumsum(k ** (-alpha))
+        cdfs.append(torch.from_numpy(c / c[-1]).to(device))
 
     def pack(idx):
         hi = torch.zeros(idx.shape[0], dtype=torch.int64, device=device)
