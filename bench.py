@@ -56,30 +56,70 @@ def log(*a):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons every 50 ms, started before the
+    warm-up; the samples whose timestamps fall inside the timed region
+    (begin() .. end(), host clock) are reported, or the one nearest to it
+    when the region is shorter than the sampling interval."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.t_begin = self.t_end = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
 
+    def begin(self):
+        import datetime
+        self.t_begin = datetime.datetime.now()
+
+    def end(self):
+        import datetime
+        self.t_end = datetime.datetime.now()
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    @classmethod
+    def summarise(cls, lines, t_begin, t_end):
+        """(sm MHz median, max MHz, reasons, samples in the region) of nvidia-smi CSV lines."""
+        import datetime
+        rows = []
+        for line in lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 10:
+                continue
+            try:
+                ts = datetime.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(p[2]), float(p[3]), p[6:10]))
+            except ValueError:
+                continue
+        inside = [r for r in rows if t_begin is not None and t_end is not None and t_begin <= r[0] <= t_end]
+        if not inside and rows and t_begin is not None and t_end is not None:
+            mid = t_begin + (t_end - t_begin) / 2
+            inside = [min(rows, key=lambda r: abs((r[0] - mid).total_seconds()))]
+        reasons = set()
+        for r in inside:
+            for nm, v in zip(cls.REASONS, r[3]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm = [r[1] for r in inside]
+        return (statistics.median(sm) if sm else None, inside[-1][2] if inside else None, sorted(reasons),
+                len(inside))
 
     def stop(self):
         if self.proc is None:
@@ -89,22 +129,9 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
-            p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
-                continue
-            try:
-                sm.append(float(p[1]))
-                smax = float(p[2])
-            except ValueError:
-                continue
-            for nm, v in zip(names, p[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        sm, smax, reasons, n = self.summarise(self.lines, self.t_begin, self.t_end)
+        return {"sm_mhz": sm, "sm_max_mhz": smax, "reasons": reasons, "samples": n,
+                "sampled": "every 50 ms; the samples inside the timed region, else the nearest one"}
 
 
 # DRAM bytes (read + write) of the sampled-MTTKRP region per sweep, summed over its
@@ -267,18 +294,22 @@ def run_gpu(args, w):
     def timed(opt, clocks=None):
         # execute_sweeps: the first sweep runs step by step, later ones replay
         # one captured sweep (a CUDA graph); the capture happens in the warm-up.
-        opt.execute_sweeps(args.warmup, J)
-        torch.cuda.synchronize()
         if clocks:
             clocks.start()
+        opt.execute_sweeps(args.warmup, J)
+        torch.cuda.synchronize()
         l0 = lib.exafac_kernel_launches()
         barrier(ws)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if clocks:
+            clocks.begin()
         e0.record()
         opt.execute_sweeps(args.steps, J)
         e1.record()
         torch.cuda.synchronize()
+        if clocks:
+            clocks.end()
         barrier(ws)
         el = max_over_ranks(e0.elapsed_time(e1) * 1e-3, ws)
         return el, lib.exafac_kernel_launches() - l0, opt.compute_exact_fit()
@@ -331,8 +362,9 @@ def run_gpu(args, w):
     # computes; a device copy moves it into the buffer the captured sweep
     # reads.  The host reads sweep s-1's sigma (and checks it) once sweep s is
     # queued, so at most two sweeps are in flight.
-    host_uni = torch.empty((args.steps, N, N, J), dtype=torch.float64, pin_memory=True)
-    host_uni.copy_(torch.rand((args.steps, N, N, J), dtype=torch.float64))
+    nbuf = min(args.steps, 8)  # distinct pinned input blocks, used in turn (16.8 MB each)
+    host_uni = torch.empty((nbuf, N, N, J), dtype=torch.float64, pin_memory=True)
+    host_uni.copy_(torch.rand((nbuf, N, N, J), dtype=torch.float64))
     dev_uni = torch.empty((N, N, J), dtype=torch.float64, device="cuda")
     stage = [torch.empty_like(dev_uni) for _ in range(2)]
     sig_host = torch.empty((args.steps, R), dtype=torch.float64, pin_memory=True)
@@ -346,7 +378,7 @@ def run_gpu(args, w):
         b = s % 2
         with torch.cuda.stream(copy_st):
             copy_st.wait_event(ev_free[b])  # the device copy out of this buffer is done
-            stage[b].copy_(host_uni[s], non_blocking=True)
+            stage[b].copy_(host_uni[s % nbuf], non_blocking=True)
             ev_staged[b].record(copy_st)
 
     def check_sigma(s):
@@ -416,7 +448,7 @@ def run_gpu(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="zipf4", choices=sorted(WORKLOADS))
