@@ -367,9 +367,10 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
 // hits (claimed in order through aux[kRunsTileSlot]) counts its run heads
 // (first hit of a row), publishes the count in its status word (slot 0 of
 // its status row, under the sort's epoch + 4: the digit passes use + 0..3)
-// and takes its exclusive prefix from a warp-wide look-back over earlier
-// tiles, which have all been claimed by running blocks and publish their
-// counts before they look back themselves.  It then writes its heads to
+// and takes its exclusive prefix from a block-wide look-back over earlier
+// tiles (kHsThreads of them per window, one per thread), which have all been
+// claimed by running blocks and publish their counts before they look back
+// themselves.  It then writes its heads to
 // touched / seg_start at that prefix, marks their rows in the step's row
 // bitmap (rowbits, cleared beforehand) and, for every chunk of kSegChunkF32
 // hits, records the index of the run holding its first hit (chunk_seg).  The
@@ -388,7 +389,8 @@ __global__ void __launch_bounds__(kHsThreads) hs_runs_kernel(const int64_t* __re
                                                              int64_t* __restrict__ touched_count, DeviceStatus* err) {
     __shared__ uint32_t wsum[kHsWarps];
     __shared__ int64_t tile_sh;
-    __shared__ uint32_t excl_sh;
+    __shared__ int first_sh;
+    __shared__ uint32_t red[kHsWarps];
     pdl_wait();
     pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -426,56 +428,56 @@ __global__ void __launch_bounds__(kHsThreads) hs_runs_kernel(const int64_t* __re
         }
         if (lane == 0) wsum[w] = n;
         __syncthreads();
-        if (w == 0) {
-            uint32_t run = 0;
+        uint32_t run = 0;
 #pragma unroll
-            for (int ww = 0; ww < kHsWarps; ww++) run += wsum[ww];
-            uint64_t* my = status + t * 256;
-            uint32_t excl = 0;
-            if (t == 0) {
-                if (lane == 0) os_store(my, epoch | kStatPrefix | run);
-            } else {
-                if (lane == 0) os_store(my, epoch | kStatAgg | run);
-                // windows of 32 predecessors, lane q on tile top - q
-                bool done = false;
-                for (int64_t top = t - 1; top >= 0 && !done; top -= 32) {
-                    const int64_t src_t = top - lane;
-                    uint64_t x = epoch | kStatAgg;  // lanes past tile 0 hold a zero count
-                    if (src_t >= 0) {
-                        const uint64_t* src = status + src_t * 256;
-                        x = os_load(src);
-                        for (uint32_t it = 0; (x & 0xffffffff00000000ull) != epoch; it++) {
-                            // give up after kSpinLimit polls, or at once when another wait already did
-                            if (it >= kSpinLimit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
-                                report(err, EXAFAC_ERR_DEVICE, 12, src_t, t);
-                                x = epoch | kStatPrefix;
-                                break;
-                            }
-                            if (it >= 32) __nanosleep(64);
-                            x = os_load(src);
+        for (int ww = 0; ww < kHsWarps; ww++) run += wsum[ww];
+        uint64_t* my = status + t * 256;
+        uint32_t excl = 0;  // the same in every thread: block-wide sums of the same words
+        if (t == 0) {
+            if (threadIdx.x == 0) os_store(my, epoch | kStatPrefix | run);
+        } else {
+            if (threadIdx.x == 0) os_store(my, epoch | kStatAgg | run);
+            // windows of kHsThreads predecessors, thread i on tile top - i
+            for (int64_t top = t - 1; top >= 0; top -= kHsThreads) {
+                const int64_t src_t = top - threadIdx.x;
+                uint64_t x = epoch | kStatAgg;  // threads past tile 0 hold a zero count
+                if (src_t >= 0) {
+                    const uint64_t* src = status + src_t * 256;
+                    x = os_load(src);
+                    for (uint32_t it = 0; (x & 0xffffffff00000000ull) != epoch; it++) {
+                        // give up after kSpinLimit polls, or at once when another wait already did
+                        if (it >= kSpinLimit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
+                            report(err, EXAFAC_ERR_DEVICE, 12, src_t, t);
+                            x = epoch | kStatPrefix;
+                            break;
                         }
+                        if (it >= 32) __nanosleep(64);
+                        x = os_load(src);
                     }
-                    const unsigned pm = __ballot_sync(0xffffffffu, ((uint32_t)x & kStatPrefix) != 0);
-                    // the nearest prefix (lowest lane) ends the look-back: lanes up to it count
-                    const int last = pm ? __ffs(pm) - 1 : 31;
-                    uint32_t v = lane <= last ? ((uint32_t)x & kStatValue) : 0u;
+                }
+                // the nearest prefix (lowest thread) ends the look-back: threads up to it count
+                if (threadIdx.x == 0) first_sh = kHsThreads;
+                __syncthreads();
+                if (((uint32_t)x & kStatPrefix) != 0) atomicMin(&first_sh, (int)threadIdx.x);
+                __syncthreads();
+                const int first = first_sh;
+                uint32_t v = (int)threadIdx.x <= first ? ((uint32_t)x & kStatValue) : 0u;
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    excl += v;
-                    done = pm != 0;
-                }
-                if (lane == 0) os_store(my, epoch | kStatPrefix | (excl + run));
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0) red[w] = v;
+                __syncthreads();
+#pragma unroll
+                for (int ww = 0; ww < kHsWarps; ww++) excl += red[ww];
+                __syncthreads();  // red and first_sh are rewritten by the next window
+                if (first < kHsThreads) break;  // uniform
             }
-            if (lane == 0) {
-                excl_sh = excl;
-                if (t == ntiles - 1) {
-                    *touched_count = (int64_t)excl + run;
-                    seg_start[(int64_t)excl + run] = H;
-                }
-            }
+            if (threadIdx.x == 0) os_store(my, epoch | kStatPrefix | (excl + run));
         }
-        __syncthreads();
-        int64_t at = excl_sh;
+        if (threadIdx.x == 0 && t == ntiles - 1) {
+            *touched_count = (int64_t)excl + run;
+            seg_start[(int64_t)excl + run] = H;
+        }
+        int64_t at = excl;
         for (int ww = 0; ww < w; ww++) at += wsum[ww];
 #pragma unroll
         for (int r = 0; r < kHsItems; r++) {
