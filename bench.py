@@ -138,7 +138,7 @@ class ClockSampler:
 # kernels from one ncu capture of this bench on the same workload and form (the
 # capture and its command: profiles/sweep_launches_zipf4_1e8_{tf32,fp64}.md).  The
 # bench cannot run ncu itself; other workloads and forms report null.
-REGION_TRAFFIC = {("zipf4", "tf32"): 2.1251e9, ("zipf4", "fp64"): 3.2366e9}
+REGION_TRAFFIC = {("zipf4", "tf32"): 2.0958e9, ("zipf4", "fp64"): 3.2366e9}
 
 
 def measured_peaks():
