@@ -12,9 +12,10 @@
 //              the tiles before it by a decoupled look-back (Merrill and
 //              Garland's single-pass scan, as in Adinets and Merrill's
 //              Onesweep), and scatters (key, hit index or packed hit) stably
-//   heads      runs of equal keys = touched rows: per-tile run counts, their
-//              scan, and the compaction into the touched list and the run
-//              starts (seg_start)
+//   runs       runs of equal keys = touched rows, in one pass (hs_runs):
+//              each tile counts its run heads, takes the count of the heads
+//              before it by the same kind of look-back, and writes its heads
+//              to the touched list and the run starts (seg_start)
 //
 // The hit count H lives on the device (counters[1]); every kernel reads it
 // there and loops over its tiles with a fixed grid, so nothing here waits on
