@@ -726,6 +726,10 @@ __global__ void __launch_bounds__(kMmaWarps * 32) solve_gram_mma_kernel(int R, c
         const int nrow = (int)min((int64_t)32, nt - base);
         if (!mbar_wait(&bars[w], phase)) {  // (the block still meets its barriers)
             if (lane == 0) report(err, EXAFAC_ERR_DEVICE, 10, base, nt);
+            // the tile's copy is the warp's only one in flight (the next is
+            // issued after this tile is consumed): give it one more bounded
+            // wait before the warp leaves its shared memory
+            mbar_wait(&bars[w], phase);
             break;
         }
         phase ^= 1u;
