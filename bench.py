@@ -26,7 +26,6 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
-import math
 import os
 import statistics
 import subprocess

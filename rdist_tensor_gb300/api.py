@@ -11,7 +11,6 @@ from __future__ import annotations
 
 import ctypes
 import json
-import math
 import time
 
 import numpy as np
