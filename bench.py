@@ -1,23 +1,35 @@
 #!/usr/bin/env python
-"""Sampled-ALS throughput on one GB300 (sweeps/s).
+"""Sampled-ALS throughput on one GB300 (sweeps/s), mixed vs FP64 form.
 
-Workload (default): the 4-mode Zipf tensor 5e6 x 5e6 x 2e4 x 1e3 with 1e8
-nonzeros (alpha 1.2, log-normal float32 values, seed 0), CP-ARLS-LEV, R=25,
-J=2^17 samples per least-squares solve.  A sweep updates every mode once.
-Randomly initialised factors give this very sparse tensor empty sampled
-fibres (zero factors, then NaN), so one exact-ALS sweep runs first, untimed —
-the reference's "-p exact" preprocessing (decompose.py:82-96).
+Workloads (--workload; the seeded synthetic stand-ins for the shapes the
+sampled-ALS solvers are quoted on; no public dataset is named):
 
-  value      sweeps/s, tensor resident on the GPU, K timed sweeps after W
-             warm-up sweeps (CUDA events, synchronised on both sides).
-  e2e        same metric through the public API with host buffers: every
+  zipf5         (default) 5-mode Zipf(1.1) tensor 1e6 x 1e6 x 1e5 x 1e3 x 100,
+                2e8 nonzeros, N(0,1) float32 values, STS-CP, R=128, J=2^19,
+                BF16 design products vs the FP64 form, 10 sweeps.
+  planted3_r64  3-mode 2000^3 planted rank-10 tensor, 2e6 nonzeros, STS-CP,
+                R=64, J=2^18, TF32 (and BF16) vs the FP64 form.
+  planted3      the same tensor, STS-CP, R=25, J=65536, FP64 form.
+  zipf4         4-mode Zipf(1.2) tensor 5e6 x 5e6 x 2e4 x 1e3, 1e8 nonzeros,
+                log-normal values, CP-ARLS-LEV, R=25, J=2^17, TF32 vs FP64.
+
+A sweep updates every mode once.  Randomly initialised factors give the Zipf
+tensors empty sampled fibres (zero factors, then NaN, in the reference too),
+so one exact-ALS sweep runs first, untimed: the reference's "-p exact"
+preprocessing (decompose.py:82-96).
+
+  value      sweeps/s of the measured form, tensor resident on the GPU, K
+             timed sweeps after W warm-up sweeps (CUDA events, synchronised on
+             both sides), replayed from one captured CUDA graph.
+  e2e        the same metric through the public API with host buffers: every
              sweep copies its uniform draws from pinned host memory (on a copy
              stream, overlapping the previous sweep) and reads sigma back.
-  roofline   sampled MTTKRP (fibre lookup, hit gather/sort, weighted scatter
+  roofline   sampled MTTKRP (fibre lookup, hit grouping, weighted reduction
              fused with the R x R solve) against the measured HBM copy
              bandwidth; algorithmic bytes per step (see algorithmic_bytes)
              summed over a sweep, divided by the region's CUDA-event time.
-  cpu_baseline  the oracle port of the reference on this machine's cores.
+  cpu_baseline  the oracle port of the reference on this machine's cores
+             (a bounded sample, scaled to the workload: see its "sample").
 
 --impl reference times the CPU port alone and prints its own line.
 """
@@ -40,14 +52,30 @@ sys.path.insert(0, ROOT)
 
 METRIC = "sampled-ALS sweeps/s at equal fit (±1e-3): mixed vs FP64 form, 1 GB300"
 WORKLOADS = {
+    "zipf5": dict(desc="5-mode Zipf(1.1) tensor 1e6 x 1e6 x 1e5 x 1e3 x 100, 2e8 nonzeros, N(0,1) values, STS-CP, "
+                       "R=128, J=2^19",
+                  gen="zipf", dims=(1_000_000, 1_000_000, 100_000, 1_000, 100), nnz=200_000_000, alpha=1.1,
+                  values="normal", R=128, J=1 << 19, sampler="sts_cp", precision="bf16", exact_pre=True, steps=10,
+                  cpu_nnz=20_000_000, cpu_J=1 << 15),
+    "planted3_r64": dict(desc="3-mode 2000^3 planted rank-10 tensor (|N(0,1)| factors, noise variance 0.01), "
+                              "2e6 nonzeros, STS-CP, R=64, J=2^18",
+                         gen="planted", dims=(2000, 2000, 2000), nnz=2_000_000, R=64, J=1 << 18, sampler="sts_cp",
+                         precision="tf32", other_forms=("bf16",), exact_pre=False, steps=20, cpu_J=1 << 15),
+    "planted3": dict(desc="3-mode 2000^3 planted rank-10 tensor (|N(0,1)| factors, noise variance 0.01), "
+                          "2e6 nonzeros, STS-CP, R=25, J=65536",
+                     gen="planted", dims=(2000, 2000, 2000), nnz=2_000_000, R=25, J=65536, sampler="sts_cp",
+                     precision="fp64", exact_pre=False, steps=20, cpu_J=65536),
     "zipf4": dict(desc="4-mode Zipf(1.2) tensor 5e6 x 5e6 x 2e4 x 1e3, 1e8 nonzeros, log-normal values, "
                        "CP-ARLS-LEV, R=25, J=2^17",
-                  dims=(5_000_000, 5_000_000, 20_000, 1_000), nnz=100_000_000, alpha=1.2, R=25, J=1 << 17,
-                  sampler="cp_arls_lev"),
+                  gen="zipf", dims=(5_000_000, 5_000_000, 20_000, 1_000), nnz=100_000_000, alpha=1.2,
+                  values="lognormal", R=25, J=1 << 17, sampler="cp_arls_lev", precision="tf32", exact_pre=True,
+                  steps=100, cpu_J=1 << 17),
     "zipf4_small": dict(desc="4-mode Zipf(1.2) tensor 5e5 x 5e5 x 2e4 x 1e3, 1e7 nonzeros (reduced)",
-                        dims=(500_000, 500_000, 20_000, 1_000), nnz=10_000_000, alpha=1.2, R=25, J=1 << 17,
-                        sampler="cp_arls_lev"),
+                        gen="zipf", dims=(500_000, 500_000, 20_000, 1_000), nnz=10_000_000, alpha=1.2,
+                        values="lognormal", R=25, J=1 << 17, sampler="cp_arls_lev", precision="tf32", exact_pre=True,
+                        steps=100, cpu_J=1 << 17),
 }
+DEFAULT_WORKLOAD = "zipf5"
 
 
 def log(*a):
@@ -133,13 +161,6 @@ class ClockSampler:
                 "sampled": "every 50 ms; the samples inside the timed region, else the nearest one"}
 
 
-# DRAM bytes (read + write) of the sampled-MTTKRP region per sweep, summed over its
-# kernels from one ncu capture of this bench on the same workload and form (the
-# capture and its command: profiles/sweep_launches_zipf4_1e8_{tf32,fp64}.md).  The
-# bench cannot run ncu itself; other workloads and forms report null.
-REGION_TRAFFIC = {("zipf4", "tf32"): 2.0958e9, ("zipf4", "fp64"): 3.2366e9}
-
-
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -150,13 +171,20 @@ def measured_peaks():
 
 
 def make_workload(w, seed=0):
+    """Seeded synthetic tensor of the workload on the GPU: (dims, int32
+    coordinates, values) as device tensors."""
     import torch
 
     from rdist_tensor_gb300 import synthetic
 
     t = time.perf_counter()
-    dims, idx, vals = synthetic.zipf_tensor_device(w["dims"], w["nnz"], alpha=w["alpha"], values="lognormal",
-                                                   seed=seed, device="cuda")
+    if w["gen"] == "planted":
+        dims, idx, vals = synthetic.planted_uniform(dims=w["dims"], nnz=w["nnz"], seed=seed)
+        idx = torch.as_tensor(idx.astype(np.int32)).cuda()
+        vals = torch.as_tensor(vals).cuda()
+    else:
+        dims, idx, vals = synthetic.zipf_tensor_device(w["dims"], w["nnz"], alpha=w["alpha"], values=w["values"],
+                                                       seed=seed, device="cuda")
     torch.cuda.synchronize()
     log(f"generated {idx.shape[0]} nonzeros in {time.perf_counter() - t:.1f}s")
     return dims, idx, vals
@@ -179,46 +207,64 @@ def build_optimizer(w, dims, idx, vals, J, precision="fp64"):
     t = time.perf_counter()
     opt.initialize_ground_truth_for_als()
     torch.cuda.synchronize()
-    log(f"initialised (sorted copies, hash tables, sampler) in {time.perf_counter() - t:.1f}s")
-    t = time.perf_counter()
-    for n in range(N):
-        opt.exact_step(n)
-    torch.cuda.synchronize()
-    log(f"exact-ALS preprocessing sweep in {time.perf_counter() - t:.2f}s, fit {opt.compute_exact_fit():.6f}")
+    log(f"{precision}: initialised (sorted copies, hash tables, sampler) in {time.perf_counter() - t:.1f}s")
+    if w["exact_pre"]:
+        t = time.perf_counter()
+        for n in range(N):
+            opt.exact_step(n)
+        torch.cuda.synchronize()
+        log(f"{precision}: exact-ALS preprocessing sweep in {time.perf_counter() - t:.2f}s, "
+            f"fit {opt.compute_exact_fit():.6f}")
     return opt, lr, st
 
 
-def algorithmic_bytes(N, R, Ju, H, touched):
+def design_bytes(precision):
+    """Bytes of one design-row element the sampled MTTKRP reads: FP64 rows in
+    the FP64 form, FP32 rows in the mixed forms."""
+    return 8 if precision == "fp64" else 4
+
+
+def algorithmic_bytes(N, R, Ju, H, touched, s_d=8):
     """Sampled MTTKRP bytes of one step: sample keys, weights and design rows
-    read once, each hit's mode-n index and value, touched output rows written
-    once (zeroing of the previous rows and the write of the new ones)."""
-    return Ju * (N - 1) * 4 + Ju * 8 + Ju * R * 8 + H * (4 + 8) + 2 * touched * R * 8
+    (s_d bytes per element) read once, each hit's mode-n index and value,
+    touched output rows written once (zeroing of the previous rows and the
+    write of the new ones)."""
+    return Ju * (N - 1) * 4 + Ju * 8 + Ju * R * s_d + H * (4 + 8) + 2 * touched * R * 8
 
 
-def cpu_port_sweeps(dims, idx_np, vals_np, R, J, sweeps, warmup, sampler="cp_arls_lev"):
+def uniforms_per_step(N, J, sampler):
+    return N * (2 if sampler == "sts_cp" else 1) * J
+
+
+def cpu_port_sample(w, dims, ora, sweeps, warmup):
     """The oracle port of the reference (OpenMP C loops + numpy/LAPACK) on the
-    host cores: set-up and one exact sweep untimed, then sampled sweeps."""
+    host cores: `sweeps` sampled sweeps at the workload's CPU sample size
+    (J = cpu_J samples per step; the first cpu_nnz nonzeros when the workload
+    names a subsample), after set-up and `warmup` untimed sweeps.  Returns
+    (sweeps/s scaled to the workload's J, elapsed s, threads, fit, sample
+    text).  The sampling (tree descents or CDF draws) and the design rows cost
+    J per step; the scaling by cpu_J / J holds for them, and is stated."""
     from oracle import oracle as O
-    from rdist_tensor_gb300 import synthetic
 
-    factors = synthetic.gaussian_factors(dims, R, seed=1)
-    t = time.perf_counter()
-    ora = O.OracleALS(dims, idx_np, vals_np, factors, sampler)
-    log(f"cpu port: set-up {time.perf_counter() - t:.1f}s")
-    t = time.perf_counter()
-    O.exact_als_sweep(ora, 1)
-    log(f"cpu port: exact sweep {time.perf_counter() - t:.1f}s")
+    J = w.get("cpu_J", w["J"])
     rng = np.random.default_rng(3)
     N = len(dims)
+    shape = (N, J) if w["sampler"] == "cp_arls_lev" else (N, 2, J)
     for _ in range(warmup):
         for n in range(N):
-            ora.step(n, J, rng.random((N, J)))
+            ora.step(n, J, rng.random(shape))
     t = time.perf_counter()
     for _ in range(sweeps):
         for n in range(N):
-            ora.step(n, J, rng.random((N, J)))
+            ora.step(n, J, rng.random(shape))
     el = time.perf_counter() - t
-    return sweeps / el, el, O.lib().or_num_threads(), ora.fit()
+    scale = J / w["J"]
+    sample = (f"{sweeps} sampled sweep(s) at J={J} per step" +
+              (f" on the first {ora.idx.shape[0]} nonzeros" if w.get("cpu_nnz") else " on the full tensor") +
+              (f", scaled by {J}/{w['J']} to the workload's J (sampling cost is linear in J)" if scale != 1 else "") +
+              f"; starting factors {'after one exact-ALS sweep on the GPU' if w['exact_pre'] else 'N(0,1)'}; "
+              "oracle restatement (pinned to the reference by golden vectors), OpenMP over all host threads")
+    return sweeps / el * scale, el, O.lib().or_num_threads(), ora.fit(), sample
 
 
 def dist_init():
@@ -250,6 +296,32 @@ def max_over_ranks(x, ws):
     return float(t.item())
 
 
+def host_copy(dims, idx, vals):
+    return idx.cpu().numpy().astype(np.uint32), vals.cpu().numpy().astype(np.float64)
+
+
+def oracle_start(w, dims, idx_np, vals_np):
+    """The oracle port on the CPU sample's nonzeros (the first cpu_nnz when
+    the workload names a subsample), from N(0,1) factors with normalised
+    columns, after (Zipf workloads) one exact-ALS sweep as the GPU arm's
+    preprocessing.  Set-up and that sweep are untimed."""
+    from oracle import oracle as O
+    from rdist_tensor_gb300 import synthetic
+
+    nnz = w.get("cpu_nnz")
+    if nnz is not None and nnz < len(vals_np):
+        idx_np, vals_np = idx_np[:nnz], vals_np[:nnz]
+    factors = synthetic.gaussian_factors(dims, w["R"], seed=1)
+    t = time.perf_counter()
+    ora = O.OracleALS(dims, idx_np, vals_np, factors, w["sampler"])
+    log(f"cpu port: set-up {time.perf_counter() - t:.1f}s")
+    if w["exact_pre"]:
+        t = time.perf_counter()
+        O.exact_als_sweep(ora, 1)
+        log(f"cpu port: exact-ALS sweep {time.perf_counter() - t:.1f}s")
+    return ora
+
+
 def run_reference(args, w):
     ws, rank, local = dist_init()
     if rank != 0:
@@ -257,22 +329,21 @@ def run_reference(args, w):
     import torch
 
     dims, idx, vals = make_workload(w)
-    idx_np = idx.cpu().numpy().astype(np.uint32)
-    vals_np = vals.cpu().numpy().astype(np.float64)
+    idx_np, vals_np = host_copy(dims, idx, vals)
     del idx, vals
     torch.cuda.empty_cache()
     sweeps = max(1, min(args.steps, args.ref_sweeps))
     warm = min(args.warmup, 1)
-    value, el, cores, fit = cpu_port_sweeps(dims, idx_np, vals_np, w["R"], w["J"], sweeps, warm)
+    ora = oracle_start(w, dims, idx_np, vals_np)
+    value, el, cores, fit, sample = cpu_port_sample(w, dims, ora, sweeps, warm)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": args.gpus,
-            "steps": sweeps, "warmup": warm, "ms_per_step": 1000.0 * el / sweeps, "higher_is_better": True,
+            "steps": sweeps, "warmup": warm, "ms_per_step": 1000.0 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, see config)",
-            "config": {"workload": w["desc"], "nnz": int(len(vals_np)), "preprocessing": "one exact-ALS sweep",
-                       "fit_after": fit},
+            "config": {"workload": w["desc"], "nnz": int(len(vals_np)), "R": w["R"], "J": w["J"],
+                       "sampler": w["sampler"], "fit_after_sample": fit},
             "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port",
-                             "sample": f"{sweeps} sampled sweep(s) of the full workload after one warm-up; the "
-                                       "reference's C++ cannot be rebuilt on this machine, so the oracle "
-                                       "restatement (pinned to it by golden vectors) runs"},
+                             "sample": sample + "; the reference's C++ cannot be rebuilt on this machine (its "
+                                                "sources are not here), so the oracle restatement runs"},
             "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -289,13 +360,16 @@ def run_gpu(args, w):
     dims, idx, vals = make_workload(w, seed=args.seed + rank)
     N, R, J = len(dims), w["R"], w["J"]
     nnz = int(idx.shape[0])
+    precision = args.precision or w["precision"]
+    steps = args.steps if args.steps is not None else w["steps"]
+    warmup = args.warmup
 
-    def timed(opt, clocks=None):
+    def timed(opt, sweeps, clocks=None):
         # execute_sweeps: the first sweep runs step by step, later ones replay
         # one captured sweep (a CUDA graph); the capture happens in the warm-up.
         if clocks:
             clocks.start()
-        opt.execute_sweeps(args.warmup, J)
+        opt.execute_sweeps(warmup, J)
         torch.cuda.synchronize()
         l0 = lib.exafac_kernel_launches()
         barrier(ws)
@@ -304,31 +378,99 @@ def run_gpu(args, w):
         if clocks:
             clocks.begin()
         e0.record()
-        opt.execute_sweeps(args.steps, J)
+        opt.execute_sweeps(sweeps, J)
         e1.record()
         torch.cuda.synchronize()
         if clocks:
             clocks.end()
         barrier(ws)
         el = max_over_ranks(e0.elapsed_time(e1) * 1e-3, ws)
+        opt.step_info()  # raises if a kernel reported a device-side error
         return el, lib.exafac_kernel_launches() - l0, opt.compute_exact_fit()
 
-    # ---- the FP64 form (the reference's arithmetic) -----------------------
-    ref_form = None
-    if args.precision != "fp64" and not args.no_fp64_form:
-        opt64, _, _ = build_optimizer(w, dims, idx, vals, J, "fp64")
-        el64, _, fit64 = timed(opt64)
-        opt64.deinitialize()
-        del opt64
+    def e2e_run(opt, lr, sweeps):
+        """The same metric through the public API with host buffers: every
+        sweep's uniforms come from pinned host memory and its sigma goes back
+        to pinned host memory, inside the timed region.  The copy of sweep
+        s+1's uniforms runs on a copy stream into a staging buffer while sweep
+        s computes; a device copy moves it into the buffer the captured sweep
+        reads.  The host reads sweep s-1's sigma (and checks it) once sweep s
+        is queued, so at most two sweeps are in flight."""
+        per = uniforms_per_step(N, J, w["sampler"])
+        nbuf = min(sweeps, 4)  # distinct pinned input blocks, used in turn
+        host_uni = torch.empty((nbuf, N * per), dtype=torch.float64, pin_memory=True)
+        host_uni.copy_(torch.rand((nbuf, N * per), dtype=torch.float64))
+        dev_uni = torch.empty(N * per, dtype=torch.float64, device="cuda")
+        stage = [torch.empty_like(dev_uni) for _ in range(2)]
+        sig_host = torch.empty((sweeps, R), dtype=torch.float64, pin_memory=True)
+        main_st = torch.cuda.current_stream()
+        copy_st = torch.cuda.Stream()
+        ev_staged = [torch.cuda.Event() for _ in range(2)]
+        ev_free = [torch.cuda.Event() for _ in range(2)]
+        ev_done = [torch.cuda.Event() for _ in range(sweeps)]
+
+        def stage_in(k):
+            b = k % 2
+            with torch.cuda.stream(copy_st):
+                copy_st.wait_event(ev_free[b])  # the device copy out of this buffer is done
+                stage[b].copy_(host_uni[k % nbuf], non_blocking=True)
+                ev_staged[b].record(copy_st)
+
+        def check_sigma(k):
+            ev_done[k].synchronize()
+            if not bool(torch.isfinite(sig_host[k]).all()):
+                raise RuntimeError(f"sweep {k}: sigma is not finite")
+
+        # one untimed sweep with these buffers: it captures the sweep graph for them
+        dev_uni.copy_(host_uni[0], non_blocking=True)
+        opt.execute_sweeps(1, J, dev_uni)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        stage_in(0)
+        for k in range(sweeps):
+            b = k % 2
+            if k + 1 < sweeps:
+                stage_in(k + 1)
+            main_st.wait_event(ev_staged[b])
+            dev_uni.copy_(stage[b], non_blocking=True)
+            ev_free[b].record(main_st)
+            opt.execute_sweeps(1, J, dev_uni)
+            sig_host[k].copy_(lr.sigma, non_blocking=True)
+            ev_done[k].record(main_st)
+            if k >= 1:
+                check_sigma(k - 1)
+        check_sigma(sweeps - 1)
+        torch.cuda.synchronize()
+        el = max_over_ranks(time.perf_counter() - t0, ws)
+        opt.step_info()  # raises if a kernel reported a device-side error
+        return {"value": ws * sweeps / el, "unit": "sweeps/s", "h2d_bytes_per_step": N * per * 8,
+                "d2h_bytes_per_step": R * 8, "sweeps": sweeps}
+
+    # ---- the FP64 form (the reference's arithmetic), and other mixed forms --
+    forms = {}
+    compare = [] if (precision == "fp64" or args.no_fp64_form) else ["fp64"]
+    compare += [f for f in w.get("other_forms", ()) if f != precision and not args.no_fp64_form]
+    for prec in compare:
+        opt, lr, _ = build_optimizer(w, dims, idx, vals, J, prec)
+        el, _, fit = timed(opt, steps)
+        rec = {"precision": prec, "sweeps_per_s": ws * steps / el, "fit_after": fit,
+               "sweeps": warmup + steps + (1 if w["exact_pre"] else 0)}
+        if prec == "fp64":
+            rec["e2e"] = e2e_run(opt, lr, min(steps, 3))
+        forms[prec] = rec
+        log(f"{prec} form: {rec['sweeps_per_s']:.3f} sweeps/s, fit {fit:.6f}")
+        opt.deinitialize()
+        del opt, lr
         torch.cuda.empty_cache()
-        ref_form = {"precision": "fp64", "sweeps_per_s": ws * args.steps / el64, "fit_after": fit64}
 
     # ---- timed region: K sweeps of the measured form, tensor resident -----
-    opt, lr, st = build_optimizer(w, dims, idx, vals, J, args.precision)
+    opt, lr, st = build_optimizer(w, dims, idx, vals, J, precision)
     clocks = ClockSampler(local)
-    elapsed, launches, fit = timed(opt, clocks)
+    elapsed, launches, fit = timed(opt, steps, clocks)
     clk = clocks.stop()
-    value = ws * args.steps / elapsed
+    value = ws * steps / elapsed
+    log(f"{precision} form: {value:.3f} sweeps/s, fit {fit:.6f}")
 
     # ---- roofline of the sampled MTTKRP (region timers, one sweep) -------
     _lib.call("exafac_als_enable_timing", opt._h, 1)
@@ -336,108 +478,71 @@ def run_gpu(args, w):
     for n in range(N):
         opt.execute_ALS_step(n, J)
         info = opt.step_info()
-        tot_bytes += algorithmic_bytes(N, R, info.unique_samples, info.hits, info.touched_rows)
+        tot_bytes += algorithmic_bytes(N, R, info.unique_samples, info.hits, info.touched_rows,
+                                       design_bytes(precision))
         units.append((info.unique_samples, info.hits, info.touched_rows))
     regions = (ctypes.c_double * 7)()
     _lib.call("exafac_als_region_times", opt._h, regions)
     _lib.call("exafac_als_enable_timing", opt._h, 0)
+    opt.timing = False
     spmm_s = regions[3]
     peak, peak_kind = measured_peaks()
     achieved = tot_bytes / spmm_s / 1e9 if spmm_s > 0 else None
+    region_names = ["leverage_sampling", "row_gather", "design_matrix_prep", "spmm", "dense_reduce",
+                    "postprocessing", "sampler_update"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None,
-                "traffic": REGION_TRAFFIC.get((args.workload, args.precision)),
-                "kernel": "sampled MTTKRP region (lookup, hit sort, scatter + solve), per sweep",
+                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "traffic_note": "ncu DRAM bytes of this region: see the profiles of this workload",
+                "kernel": "sampled MTTKRP region (lookup, hit grouping, segmented reduction + solve), per sweep",
                 "algorithmic_bytes": tot_bytes, "duration_s": spmm_s, "peak_source": peak_kind,
-                "regions_s": {k: v for k, v in zip(["leverage_sampling", "row_gather", "design_matrix_prep",
-                                                    "spmm", "dense_reduce", "postprocessing", "sampler_update"],
-                                                   list(regions))},
+                "design_element_bytes": design_bytes(precision),
+                "regions_s": dict(zip(region_names, list(regions))),
                 "units_per_step": [{"unique_samples": a, "hits": b, "touched_rows": c} for a, b, c in units]}
 
+    # ---- the drop-in round loop (execute_ALS_rounds, region timers on) ----
+    rounds = 2
+    opt.execute_ALS_rounds(rounds, J, rounds)
+    stats = json.loads(opt.get_statistics_json())
+    drop_in = {"sweeps_per_s": rounds / stats["als_total_time"], "rounds": rounds,
+               "note": "ALS_Optimizer.execute_ALS_rounds with its region timers, step by step (no graph replay)"}
+
     # ---- e2e through the public API with host buffers ---------------------
-    # Every sweep's uniforms come from pinned host memory and its sigma goes
-    # back to pinned host memory, inside the timed region.  The copy of sweep
-    # s+1's uniforms runs on a copy stream into a staging buffer while sweep s
-    # computes; a device copy moves it into the buffer the captured sweep
-    # reads.  The host reads sweep s-1's sigma (and checks it) once sweep s is
-    # queued, so at most two sweeps are in flight.
-    nbuf = min(args.steps, 8)  # distinct pinned input blocks, used in turn (16.8 MB each)
-    host_uni = torch.empty((nbuf, N, N, J), dtype=torch.float64, pin_memory=True)
-    host_uni.copy_(torch.rand((nbuf, N, N, J), dtype=torch.float64))
-    dev_uni = torch.empty((N, N, J), dtype=torch.float64, device="cuda")
-    stage = [torch.empty_like(dev_uni) for _ in range(2)]
-    sig_host = torch.empty((args.steps, R), dtype=torch.float64, pin_memory=True)
-    main_st = torch.cuda.current_stream()
-    copy_st = torch.cuda.Stream()
-    ev_staged = [torch.cuda.Event() for _ in range(2)]
-    ev_free = [torch.cuda.Event() for _ in range(2)]
-    ev_done = [torch.cuda.Event() for _ in range(args.steps)]
-
-    def stage_in(s):
-        b = s % 2
-        with torch.cuda.stream(copy_st):
-            copy_st.wait_event(ev_free[b])  # the device copy out of this buffer is done
-            stage[b].copy_(host_uni[s % nbuf], non_blocking=True)
-            ev_staged[b].record(copy_st)
-
-    def check_sigma(s):
-        ev_done[s].synchronize()
-        if not bool(torch.isfinite(sig_host[s]).all()):
-            raise RuntimeError(f"sweep {s}: sigma is not finite")
-
-    # one untimed sweep with these buffers: it captures the sweep graph for them
-    dev_uni.copy_(host_uni[0], non_blocking=True)
-    opt.execute_sweeps(1, J, dev_uni)
-    torch.cuda.synchronize()
-    barrier(ws)
-    t0 = time.perf_counter()
-    stage_in(0)
-    for s in range(args.steps):
-        b = s % 2
-        if s + 1 < args.steps:
-            stage_in(s + 1)
-        main_st.wait_event(ev_staged[b])
-        dev_uni.copy_(stage[b], non_blocking=True)
-        ev_free[b].record(main_st)
-        opt.execute_sweeps(1, J, dev_uni)
-        sig_host[s].copy_(lr.sigma, non_blocking=True)
-        ev_done[s].record(main_st)
-        if s >= 1:
-            check_sigma(s - 1)
-    check_sigma(args.steps - 1)
-    torch.cuda.synchronize()
-    e2e_el = max_over_ranks(time.perf_counter() - t0, ws)
-    opt.step_info()  # raises if a kernel reported an out-of-range index
-    e2e = {"value": ws * args.steps / e2e_el, "unit": "sweeps/s", "h2d_bytes_per_step": N * N * J * 8,
-           "d2h_bytes_per_step": R * 8}
+    e2e = e2e_run(opt, lr, steps)
 
     # ---- CPU baseline (rank 0, one GPU only) ------------------------------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        idx_np = st.indices.cpu().numpy().astype(np.uint32)
-        vals_np = st.values.cpu().numpy()
-        cval, cel, cores, cfit = cpu_port_sweeps(dims, idx_np, vals_np, R, J, 1, 0)
-        cpu = {"value": cval, "unit": "sweeps/s", "cores": cores, "kind": "port",
-               "sample": "one sampled sweep of the full workload (after untimed set-up and one exact sweep); "
-                         "oracle restatement, OpenMP over all host threads"}
+        idx_np, vals_np = host_copy(dims, st.indices, st.values)
+        opt.deinitialize()
+        ora = oracle_start(w, dims, idx_np, vals_np)
+        cval, cel, cores, cfit, sample = cpu_port_sample(w, dims, ora, 1, 0)
+        cpu = {"value": cval, "unit": "sweeps/s", "cores": cores, "kind": "port", "sample": sample}
     opt.deinitialize()
     if rank != 0:
         return 0
-    dtype = "f64" if args.precision == "fp64" else f"{args.precision} design Gram, fp32 row products, fp64 solve/CDF"
-    cfg = {"workload": w["desc"], "nnz": nnz, "R": R, "J": J, "sampler": w["sampler"], "precision": args.precision,
-           "preprocessing": "one exact-ALS sweep, untimed", "parallelism": f"{ws} independent replica(s)",
-           "l2": "inputs larger than L2 (per-mode sorted copies and hash tables, tens of GB)", "fit_after": fit}
-    if ref_form is not None:
-        cfg["fp64_form"] = ref_form
-        cfg["speedup_vs_fp64_form"] = value / ref_form["sweeps_per_s"]
-        cfg["fit_gap_vs_fp64_form"] = abs(fit - ref_form["fit_after"])
-        cfg["equal_fit_1e-3"] = bool(abs(fit - ref_form["fit_after"]) <= 1e-3)
-    line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
+    dtype = {"fp64": "f64", "tf32": "tf32 design Gram; fp32 rows, MTTKRP, solve and tree descents; "
+                                    "fp64 Gram chain, pinv, tree sums, CDF",
+             "bf16": "bf16 design Gram; fp32 rows, MTTKRP, solve and tree descents; "
+                     "fp64 Gram chain, pinv, tree sums, CDF"}[precision]
+    cfg = {"workload": w["desc"], "nnz": nnz, "R": R, "J": J, "sampler": w["sampler"], "precision": precision,
+           "preprocessing": "one exact-ALS sweep, untimed" if w["exact_pre"] else "none (N(0,1) factors)",
+           "parallelism": f"{ws} independent replica(s)",
+           "l2": "inputs larger than L2 (per-mode sorted copies and hash tables)", "fit_after": fit,
+           "sweeps_run": warmup + steps + (1 if w["exact_pre"] else 0), "drop_in_rounds": drop_in}
+    if "fp64" in forms:
+        ref = forms["fp64"]
+        cfg["fp64_form"] = ref
+        cfg["speedup_vs_fp64_form"] = value / ref["sweeps_per_s"]
+        cfg["fit_gap_vs_fp64_form"] = abs(fit - ref["fit_after"])
+        cfg["equal_fit_1e-3"] = bool(abs(fit - ref["fit_after"]) <= 1e-3)
+    for prec, rec in forms.items():
+        if prec != "fp64":
+            cfg[f"{prec}_form"] = rec
+    line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": steps,
+            "warmup": warmup, "ms_per_step": 1000.0 * elapsed / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype,
-            "data": "synthetic (seeded Zipf coordinates, log-normal values; no public dataset)",
-            "config": cfg,
-            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+            "data": "synthetic (seeded; no public dataset is named for these shapes)",
+            "config": cfg, "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -447,20 +552,23 @@ def run_gpu(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=None, help="timed sweeps (default: the workload's count)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="zipf4", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="tf32", choices=["fp64", "tf32", "bf16"],
-                    help="form timed for `value`; a mixed form is also compared with the FP64 form")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default=None, choices=["fp64", "tf32", "bf16"],
+                    help="form timed for `value` (default: the workload's); a mixed form is also compared with "
+                         "the FP64 form")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-sweeps", type=int, default=3)
+    ap.add_argument("--ref-sweeps", type=int, default=1)
     ap.add_argument("--no-fp64-form", action="store_true",
                     help="skip timing the FP64 form beside a mixed form (for kernel profiling runs)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
+        if args.steps is None:
+            args.steps = w["steps"]
         return run_reference(args, w)
     return run_gpu(args, w)
 

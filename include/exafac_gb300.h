@@ -194,10 +194,12 @@ int exafac_als_fit(exafac_als_t s, double* fit, void* stream);
 int exafac_als_set_seed(exafac_als_t s, uint64_t seed);
 
 /* Region timers of ALS_Optimizer (als_optimizer.hpp:19-27).  When enabled,
- * each exafac_als_step records CUDA events at its region borders and waits
- * for them before returning; exafac_als_region_times returns the seconds
- * accumulated since enabling, in the order leverage_sampling, row_gather,
- * design_matrix_prep, spmm, dense_reduce, postprocessing, sampler_update. */
+ * each exafac_als_step records CUDA events at its region borders on its
+ * stream and returns without waiting for them; exafac_als_region_times waits
+ * for the steps recorded so far and returns the seconds accumulated since
+ * enabling, in the order leverage_sampling, row_gather, design_matrix_prep,
+ * spmm, dense_reduce, postprocessing, sampler_update.  At most 512 steps stay
+ * pending; a later step first waits for the oldest. */
 int exafac_als_enable_timing(exafac_als_t s, int32_t enable);
 int exafac_als_region_times(exafac_als_t s, double* out7);
 
@@ -210,6 +212,15 @@ int exafac_als_region_times(exafac_als_t s, double* out7);
  * pointer, and dropped by exafac_als_init / exafac_als_set_seed); results are
  * those of calling exafac_als_step N x count times.  Region timing must be off. */
 int exafac_als_sweeps(exafac_als_t s, int64_t J, int32_t count, const double* uniforms_dev, void* stream);
+
+/* Failure-detection test hook (no counterpart in the reference, which has no
+ * device-side waits).  The row sort of each step waits, per tile, for the
+ * status words of earlier tiles (a decoupled look-back); a wait gives up after
+ * `polls` polls (0 = the default, 2^22, about half a second) and the step then
+ * reports EXAFAC_ERR_TIMEOUT through exafac_als_step_info.device_status, with
+ * no hits processed.  withhold_tile >= 0 makes that tile of the first digit
+ * pass publish no status, so the waits on it run out; -1 turns this off. */
+int exafac_als_set_wait_limit(exafac_als_t s, uint32_t polls, int64_t withhold_tile);
 
 /* Copies the last step's counters to the host (synchronises). */
 int exafac_als_step_info(exafac_als_t s, exafac_step_info* out, void* stream);

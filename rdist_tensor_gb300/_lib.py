@@ -72,6 +72,7 @@ SIGNATURES = {
     "exafac_als_enable_timing": (ctypes.c_int, [_P, _I32]),
     "exafac_als_region_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "exafac_als_step_info": (ctypes.c_int, [_P, ctypes.POINTER(StepInfo), _P]),
+    "exafac_als_set_wait_limit": (ctypes.c_int, [_P, ctypes.c_uint32, _I64]),
     "exafac_als_last_dedup": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                                              ctypes.POINTER(_P)]),
     "exafac_cp_sampled_model": (ctypes.c_int, [_I32, _I32, _P, _I64, _P, _P, _P, _I32, _P, _P]),

@@ -159,22 +159,30 @@ class SparseTensor:
         else:
             idx, vals = _block_tensor(int(a), int(b), int(c), seed)
             self.preprocessing = "none"
-        dev = _device()
+        # Host-side validation first (shape, coordinate range, value count,
+        # preprocessing name), before anything reaches the device.
         idx_t = torch.as_tensor(np.ascontiguousarray(idx).astype(np.int64, copy=False) if not torch.is_tensor(idx)
                                 else idx)
         if idx_t.dim() != 2 or idx_t.shape[1] != self.dim:
             raise ValueError("indices must be nnz x N")
         self.nnz = int(idx_t.shape[0])
         dims = torch.as_tensor(tensor_grid.tensor_dims, dtype=torch.int64)
+        if bool((dims < 1).any()) or bool((dims > 0xffffffff).any()):
+            raise ValueError("mode sizes must be in [1, 2^32)")
         if self.nnz and (idx_t.min() < 0 or bool((idx_t.max(dim=0).values >= dims.to(idx_t.device)).any())):
             raise ValueError("coordinate out of range for the tensor grid")
-        self.indices = idx_t.to(device=dev, dtype=torch.int64).to(torch.int32).contiguous()
         v = torch.as_tensor(vals) if not torch.is_tensor(vals) else vals
-        self.values = v.to(device=dev, dtype=torch.float64).contiguous().reshape(-1)
-        if self.values.numel() != self.nnz:
+        if v.numel() != self.nnz:
             raise ValueError("values must have one entry per nonzero")
         if self.preprocessing not in _lib.PREPROCESSING:
             raise ValueError(f"unknown preprocessing {self.preprocessing}")
+        dev = _device()
+        # The engine reads coordinates as uint32 words; they are held in an
+        # int32 tensor, where a coordinate in [2^31, 2^32) keeps its bit
+        # pattern (two's-complement wrap of the validated int64 value).
+        idx64 = idx_t.to(device=dev, dtype=torch.int64)
+        self.indices = torch.where(idx64 >= 2 ** 31, idx64 - 2 ** 32, idx64).to(torch.int32).contiguous()
+        self.values = v.to(device=dev, dtype=torch.float64).contiguous().reshape(-1)
 
 
 def _block_tensor(I: int, N: int, Q: int, seed: int):
@@ -262,6 +270,11 @@ class ALS_Optimizer:
 
     def _create(self, J_max: int):
         self.deinitialize()
+        for k, f in enumerate(self.low_rank_tensor.factors):
+            if not bool(torch.isfinite(f.data).all()):
+                raise ValueError(f"factor matrix {k} has a non-finite entry")
+        if not bool(torch.isfinite(self.low_rank_tensor.sigma).all()):
+            raise ValueError("sigma has a non-finite entry")
         cfg = self._config(J_max)
         pers, setup = ctypes.c_size_t(), ctypes.c_size_t()
         _lib.call("exafac_als_workspace_size", ctypes.byref(cfg), ctypes.byref(pers), ctypes.byref(setup))
@@ -397,7 +410,9 @@ class ALS_Optimizer:
         out = _lib.StepInfo()
         _lib.call("exafac_als_step_info", self._h, ctypes.byref(out), _stream())
         if out.device_status != 0:
-            raise _lib.ExafacError("device", out.device_status, "a kernel reported an out-of-range index")
+            what = {4: "a bounded device-side wait ran out; re-initialise the optimizer"}
+            raise _lib.ExafacError("device", out.device_status,
+                                   what.get(out.device_status, "a kernel reported an out-of-range index"))
         return out
 
     def draw(self, mode: int, J: int, uniforms: torch.Tensor | None = None, perms: torch.Tensor | None = None):

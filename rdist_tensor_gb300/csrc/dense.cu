@@ -108,15 +108,20 @@ __device__ void jacobi_block(int R, const double* __restrict__ A, double* a, dou
     }
 }
 
-// Ascending order of the diagonal: rank[i] = #{j : d_j < d_i or (d_j == d_i and j < i)}.
+// Ascending order of the diagonal: rank[i] = #{j : d_j before d_i}, with
+// "before" a strict total order (value, then index; NaNs after every number),
+// so the ranks are a permutation of 0..R-1 whatever the values: the order[]
+// built from them has no unwritten slot even when a NaN reached the matrix.
+__device__ __forceinline__ bool diag_before(double dj, int j, double di, int i) {
+    const bool nj = isnan(dj), ni = isnan(di);
+    if (nj || ni) return nj == ni ? j < i : ni;
+    return dj < di || (dj == di && j < i);
+}
 __device__ void ascending_ranks(int R, const double* a, int Re, int* rank) {
     for (int i = threadIdx.x; i < R; i += blockDim.x) {
-        double di = a[i * Re + i];
+        const double di = a[i * Re + i];
         int r = 0;
-        for (int j = 0; j < R; j++) {
-            double dj = a[j * Re + j];
-            r += (dj < di) || (dj == di && j < i);
-        }
+        for (int j = 0; j < R; j++) r += diag_before(a[j * Re + j], j, di, i);
         rank[i] = r;
     }
 }

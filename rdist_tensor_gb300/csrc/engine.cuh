@@ -25,6 +25,9 @@ constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a p
 constexpr int kExpandChunk = 256;  // hits per warp chunk in the hit expansion
 constexpr int kSortEpochSlot = 14;  // counters[] slot of the row sort's look-back epoch
 constexpr int kRngSlot = 15;              // counters[] slot of the session's Philox counter
+// Polls of a look-back status word before the wait is declared failed
+// (EXAFAC_ERR_TIMEOUT); each poll after the 32nd sleeps ~64 ns.
+constexpr uint32_t kSpinLimit = 1u << 22;
 
 struct Slot1 {
     unsigned long long key;
@@ -83,6 +86,13 @@ struct Session {
     double* Phi = nullptr;     // R x R (full)
     double* PhiP = nullptr;    // packed
     double* vt = nullptr;      // Jacobi scratch, N+1 matrices
+    // FP32 copies the mixed forms' STS-CP descents read (rounded from the FP64
+    // arrays after every change): row trees, factors, eigen trees, E, Phi
+    float* treeF[kMaxModes] = {nullptr};
+    float* Uf[kMaxModes] = {nullptr};
+    float* eigF = nullptr;
+    float* EmatF = nullptr;
+    float* PhiPF = nullptr;
 
     // nonzero-row tracking per factor (rows outside the list are zero)
     bool dense[kMaxModes] = {false};
@@ -140,11 +150,15 @@ struct Session {
     uint32_t* carry_seg = nullptr;  // chunks: that row's touched-row index (compact Mc)
     uint32_t* chunk_seg = nullptr;  // chunks of kSegChunkF32 sorted hits: run index of the first hit
     uint32_t* expand_first = nullptr;  // ceil(nnz / kExpandChunk) + 1: sample owning each expansion chunk's first hit
-    float* Uc = nullptr;            // Imax x 32, mixed forms: solved rows by touched-row index
+    float* Uc = nullptr;            // Imax x f32_row_stride(R), mixed forms: solved rows by touched-row index
     uint32_t* rowbits = nullptr;    // ceil(Imax / 32): rows touched by the current step
-    float* Df = nullptr;          // Jmax x R design rows (mixed forms)
+    float* Df = nullptr;          // Jmax x f32_row_stride(R) design rows (mixed forms)
 
     uint64_t seed = 0x5eed;  // Philox key; the stream counter is counters[kRngSlot] on the device
+    // Look-back waits of the row sort: poll limit, and (test hook, -1 = off)
+    // a tile of the first digit pass that publishes no status.
+    uint32_t wait_polls = kSpinLimit;
+    int64_t withhold_tile = -1;
 };
 
 // ---- sampler kernels (sampler_kernels.cu)
@@ -154,6 +168,8 @@ int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStre
 int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* perms, cudaStream_t st);
 int sts_compute_M(Session& s, int n, cudaStream_t st);
 int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
+// FP32 copies of factor k and its row tree (mixed STS-CP sessions; else a no-op).
+int sts_refresh_f32(Session& s, int k, cudaStream_t st);
 
 // ---- step kernels (step_kernels.cu)
 int dedup(Session& s, int n, int64_t J, cudaStream_t st);
@@ -186,6 +202,10 @@ int nonzeros_by_row(Session& s, int n, cudaStream_t st);
 int mttkrp_solve_balanced(Session& s, int n, cudaStream_t st);
 int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st);
 int mttkrp_scatter_out(Session& s, double* out, cudaStream_t st);
+// 32 < R <= 128 (wide_kernels.cu): MTTKRP + solve + Gram, and renormalisation,
+// in FP64 (FP64 form) or FP32 (mixed forms).
+int mttkrp_solve_wide(Session& s, int n, cudaStream_t st);
+int normalize_wide(Session& s, int n, bool arls, cudaStream_t st);
 int spmm_solve(Session& s, int n, cudaStream_t st);
 int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStream_t st);
 int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st);

@@ -36,7 +36,6 @@ constexpr int kHistGrid = 152 * 2;          // os_hist
 constexpr uint32_t kStatAgg = 1u << 30;     // look-back status: the tile's own count
 constexpr uint32_t kStatPrefix = 2u << 30;  // look-back status: the inclusive prefix
 constexpr uint32_t kStatValue = (1u << 30) - 1;
-constexpr uint32_t kSpinLimit = 1u << 22;   // look-back polls before a wait is declared failed
 constexpr uint32_t kNoItem = 0xffffffffu;
 
 __device__ __forceinline__ int64_t hit_count(const int64_t* counters, int64_t cap) { return min(counters[1], cap); }
@@ -235,7 +234,8 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
                                                                   uint32_t* __restrict__ aux,
                                                                   uint64_t* __restrict__ status,
                                                                   uint32_t* __restrict__ kout,
-                                                                  PT* __restrict__ pout, DeviceStatus* err) {
+                                                                  PT* __restrict__ pout, DeviceStatus* err,
+                                                                  uint32_t spin_limit, int64_t withhold) {
     extern __shared__ __align__(16) unsigned char hs_dyn[];  // payloads, then keys, of one tile
     constexpr int kTile = kHsThreads * ITEMS;
     PT* spay = reinterpret_cast<PT*>(hs_dyn);
@@ -302,10 +302,11 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
             // publish this tile's count, then look back for the prefix
             uint64_t* my = status + t * 256 + d;
             uint32_t excl = 0;
+            const bool publish = t != withhold;  // withhold >= 0 only under the wait-limit test hook
             if (t == 0) {
-                os_store(my, epoch | kStatPrefix | run);
+                if (publish) os_store(my, epoch | kStatPrefix | run);
             } else {
-                os_store(my, epoch | kStatAgg | run);
+                if (publish) os_store(my, epoch | kStatAgg | run);
                 // windows of kLook predecessors: their status words are loaded
                 // together, then taken in order back to the first prefix
                 constexpr int kLook = 4;
@@ -320,9 +321,9 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
                         const uint64_t* src = status + (top - q) * 256 + d;
                         uint64_t x = v[q];
                         for (uint32_t it = 0; (x & 0xffffffff00000000ull) != epoch; it++) {
-                            // give up after kSpinLimit polls, or at once when another wait already did
-                            if (it >= kSpinLimit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
-                                report(err, EXAFAC_ERR_DEVICE, 9, top - q, t);
+                            // give up after spin_limit polls, or at once when another wait already did
+                            if (it >= spin_limit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
+                                report(err, EXAFAC_ERR_TIMEOUT, 9, top - q, t);
                                 x = epoch | kStatPrefix;
                                 break;
                             }
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(kHsThreads) os_downsweep_kernel(const int64_t*
                         done = ((uint32_t)x & kStatPrefix) != 0;
                     }
                 }
-                os_store(my, epoch | kStatPrefix | (excl + run));
+                if (publish) os_store(my, epoch | kStatPrefix | (excl + run));
             }
             const uint32_t ts = block256_exclusive(run, wsum);
             tstart[d] = ts;
@@ -387,7 +388,8 @@ __global__ void __launch_bounds__(kHsThreads) hs_runs_kernel(const int64_t* __re
                                                              int64_t* __restrict__ seg_start,
                                                              uint32_t* __restrict__ chunk_seg,
                                                              uint32_t* __restrict__ rowbits,
-                                                             int64_t* __restrict__ touched_count, DeviceStatus* err) {
+                                                             int64_t* __restrict__ touched_count, DeviceStatus* err,
+                                                             uint32_t spin_limit) {
     __shared__ uint32_t wsum[kHsWarps];
     __shared__ int64_t tile_sh;
     __shared__ int first_sh;
@@ -396,7 +398,14 @@ __global__ void __launch_bounds__(kHsThreads) hs_runs_kernel(const int64_t* __re
     pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const int64_t H = hit_count(counters, cap);
+    // A digit pass whose look-back ran out (reported) leaves an unsorted key
+    // array whose unwritten positions hold stale rows, possibly of another
+    // mode: the step then has no runs, so no later kernel indexes by them.
+    const bool sort_failed = *(volatile int*)&err->code == EXAFAC_ERR_TIMEOUT;
+    const int64_t H = sort_failed ? 0 : hit_count(counters, cap);
+    // and the kernels after this one see no hits either (every block has read
+    // the count above through sort_failed, not from counters[1])
+    if (sort_failed && blockIdx.x == 0 && threadIdx.x == 0) const_cast<int64_t*>(counters)[1] = 0;
     const int64_t ntiles = (H + kHsTile - 1) / kHsTile;
     const uint64_t epoch = (uint64_t)(uint32_t)(counters[kSortEpochSlot] + 4) << 32;
     if (ntiles == 0) {
@@ -446,9 +455,9 @@ __global__ void __launch_bounds__(kHsThreads) hs_runs_kernel(const int64_t* __re
                     const uint64_t* src = status + src_t * 256;
                     x = os_load(src);
                     for (uint32_t it = 0; (x & 0xffffffff00000000ull) != epoch; it++) {
-                        // give up after kSpinLimit polls, or at once when another wait already did
-                        if (it >= kSpinLimit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
-                            report(err, EXAFAC_ERR_DEVICE, 12, src_t, t);
+                        // give up after spin_limit polls, or at once when another wait already did
+                        if (it >= spin_limit || ((it & 1023u) == 1023u && *(volatile int*)&err->code != 0)) {
+                            report(err, EXAFAC_ERR_TIMEOUT, 12, src_t, t);
                             x = epoch | kStatPrefix;
                             break;
                         }
@@ -546,12 +555,14 @@ static int sort_keys(Session& s, int n, bool packed, cudaStream_t st) {
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             EXAFAC_CUDA_TRY(launch_dependent(os_downsweep_kernel<uint64_t, IT>, kHsDownGridPacked, kHsThreads, smem, st,
                                              s.counters, cap, s.hit_key[src], s.pay64[src], p, s.os_aux, s.os_status,
-                                             s.hit_key[dst], s.pay64[dst], s.status));
+                                             s.hit_key[dst], s.pay64[dst], s.status, s.wait_polls,
+                                             p == 0 ? s.withhold_tile : (int64_t)-1));
         } else {
             const size_t smem = (sizeof(uint32_t) + sizeof(uint32_t)) * kHsTile;
             EXAFAC_CUDA_TRY(launch_dependent(os_downsweep_kernel<uint32_t, kHsItems>, kHsDownGrid, kHsThreads, smem, st,
                                              s.counters, cap, s.hit_key[src], p == 0 ? nullptr : s.hit_pay[src], p,
-                                             s.os_aux, s.os_status, s.hit_key[dst], s.hit_pay[dst], s.status));
+                                             s.os_aux, s.os_status, s.hit_key[dst], s.hit_pay[dst], s.status,
+                                             s.wait_polls, p == 0 ? s.withhold_tile : (int64_t)-1));
         }
         count_launch();
         EXAFAC_CHECK_LAUNCH();
@@ -586,7 +597,7 @@ int hits_by_row(Session& s, int n, bool packed, cudaStream_t st) {
     EXAFAC_TRY(sort_keys(s, n, packed, st));
     EXAFAC_CUDA_TRY(launch_dependent(hs_runs_kernel, kHsGrid, kHsThreads, 0, st, s.counters, cap, s.key_sorted,
                                      s.os_aux, s.os_status, s.touched, s.seg_start, s.chunk_seg, s.rowbits,
-                                     s.counters + 2, s.status));
+                                     s.counters + 2, s.status, s.wait_polls));
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;

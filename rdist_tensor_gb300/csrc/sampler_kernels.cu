@@ -284,6 +284,20 @@ int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* p
 // STS-CP
 // ---------------------------------------------------------------------------
 
+// FP32 copies (round to nearest even, in integer arithmetic) of FP64 arrays.
+__global__ void narrow_copy_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = narrow_f64(in[i]);
+}
+
+static int narrow_copy(const double* in, float* out, int64_t n, cudaStream_t st) {
+    if (n <= 0) return EXAFAC_OK;
+    narrow_copy_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 16), 256, 0, st>>>(in, out, n);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
 // STS_CP::computeM part 1 (sts_cp.hpp:81-102): suffix Hadamard products of
 // the factor Grams over the modes != n; chain[n] is cleared.
 __global__ void sts_chain_kernel(int N, int n, int R, const double* __restrict__ gram, double* __restrict__ chain) {
@@ -415,83 +429,98 @@ int sts_compute_M(Session& s, int n, cudaStream_t st) {
     EXAFAC_CHECK_LAUNCH();
     sts_eigen_tree_kernel<<<N, 256, 0, st>>>(N, n, R, s.etree, s.Emat, s.gram, s.eigG); count_launch();
     EXAFAC_CHECK_LAUNCH();
+    if (s.cfg.precision != EXAFAC_PREC_FP64) {  // the mixed forms descend on FP32 copies
+        EXAFAC_TRY(narrow_copy(s.eigG, s.eigF, (int64_t)N * s.etree.node_count * s.P, st));
+        EXAFAC_TRY(narrow_copy(s.Emat, s.EmatF, (int64_t)(N + 1) * R2, st));
+        EXAFAC_TRY(narrow_copy(s.PhiP, s.PhiPF, s.P, st));
+    }
     return EXAFAC_OK;
 }
 
+template <typename T>
 struct StsModes {
-    const double* treeG[kMaxModes];
-    const double* U[kMaxModes];
+    const T* treeG[kMaxModes];
+    const T* U[kMaxModes];
     TreeShape rt[kMaxModes];
     int next[kMaxModes];
 };
 
-// STS_CP::KRPDrawSamples (sts_cp.hpp:203-300) at one rank, warp per sample:
-// for each sampled mode k, an eigen-tree descent driven by h picks v and sets
-// scaled_h = h * E[next(k)][v]; a row-tree descent driven by scaled_h picks
-// the row and sets h *= U_k[row] (exact_leverage_tree.hpp:293-496 with no
-// distributed levels).  Weight = R / (J h^T Phi h).
-__global__ void sts_draw_kernel(int N, int n, int R, int64_t J, StsModes m, TreeShape et,
-                                const double* __restrict__ eigG, const double* __restrict__ E,
-                                const double* __restrict__ PhiP, const double* __restrict__ uni,
-                                uint32_t* __restrict__ samples, double* __restrict__ weights,
-                                DeviceStatus* status) {
-    extern __shared__ unsigned char smraw[];
+// STS_CP::KRPDrawSamples (sts_cp.hpp:203-300) at one rank, one sample per
+// group of G warps: for each sampled mode k, an eigen-tree descent driven by h
+// picks v and sets scaled_h = h * E[next(k)][v]; a row-tree descent driven by
+// scaled_h picks the row and sets h *= U_k[row]
+// (exact_leverage_tree.hpp:293-496 with no distributed levels).  Weight =
+// R / (J h^T Phi h).  T = double: the reference's arithmetic on the FP64
+// trees and factors; T = float (mixed forms): the same descents on FP32
+// copies of the trees (summed in FP64, rounded once), factors, eigenvector
+// rows and Phi.
+template <typename T>
+__global__ void sts_draw_kernel(int N, int n, int R, int G, int S, int64_t J, StsModes<T> m, TreeShape et,
+                                const T* __restrict__ eigG, const T* __restrict__ E, const T* __restrict__ PhiP,
+                                const double* __restrict__ uni, uint32_t* __restrict__ samples,
+                                double* __restrict__ weights, DeviceStatus* status) {
+    extern __shared__ __align__(16) unsigned char stsdyn[];
     const int P = packed_size(R);
-    const int warps = blockDim.x >> 5;
-    unsigned short* pa = reinterpret_cast<unsigned short*>(smraw);
-    unsigned short* pb = pa + P;
-    double* base = reinterpret_cast<double*>(smraw + align_up(2 * P * sizeof(unsigned short), 16));
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* h = base + (size_t)w * (P + 3 * R);
-    double* sh = h + R;
-    double* q = sh + R;
-    double* z = q + R;
-    block_build_pairs(R, pa, pb);
-    __syncthreads();
-    for (int64_t i = (int64_t)blockIdx.x * warps + w; i < J; i += (int64_t)gridDim.x * warps) {
-        for (int r = lane; r < R; r += 32) h[r] = 1.0;
-        __syncwarp();
+    T *h, *sh, *q;
+    int gi;
+    const SampleGroup<T> grp = sample_group<T>(stsdyn, R, G, h, sh, q, gi);
+    const int tg = grp.tg, nth = grp.nthreads();
+    for (int64_t i = (int64_t)blockIdx.x * S + gi; i < J; i += (int64_t)gridDim.x * S) {
+        for (int r = tg; r < R; r += nth) h[r] = T(1);
+        bool empty = false;  // a descent ended in a leaf of zero mass: weight 0
+        grp.sync();
         for (int k = 0; k < N; k++) {
             if (k == n) continue;
-            for (int r = lane; r < R; r += 32) sh[r] = h[r];
-            __syncwarp();
             // Eigen tree: descent by h, leaf v, scaled_h = h * E_next[v].
-            const double* Ek = E + (int64_t)m.next[k] * R * R;
-            warp_build_z(R, h, pa, pb, z);
-            int64_t v = warp_descend(et, R, eigG + (int64_t)k * et.node_count * P, Ek, z, h, q,
-                                     uni[((int64_t)k * 2 + 0) * J + i]);
+            const T* Ek = E + (int64_t)m.next[k] * R * R;
+            grp.build_z(R, h);
+            int64_t v = descend<T>(grp, et, R, eigG + (int64_t)k * et.node_count * P, Ek, h, q,
+                                   (T)uni[((int64_t)k * 2 + 0) * J + i]);
             if (v >= R) {
                 report(status, EXAFAC_ERR_DEVICE, 1, v, R);
                 v = R - 1;
             }
-            if (lane == 0) samples[i * N + n] = (uint32_t)v;
-            for (int r = lane; r < R; r += 32) sh[r] *= Ek[v * R + r];
-            __syncwarp();
+            if (tg == 0) samples[i * N + n] = (uint32_t)v;
+            for (int r = tg; r < R; r += nth) sh[r] = h[r] * Ek[v * R + r];
+            grp.sync();
             // Row tree: descent by scaled_h, row, h *= U_k[row].
-            warp_build_z(R, sh, pa, pb, z);
-            int64_t row = warp_descend(m.rt[k], R, m.treeG[k], m.U[k], z, sh, q, uni[((int64_t)k * 2 + 1) * J + i]);
+            grp.build_z(R, sh);
+            int64_t row = descend<T>(grp, m.rt[k], R, m.treeG[k], m.U[k], sh, q,
+                                     (T)uni[((int64_t)k * 2 + 1) * J + i], &empty);
             if (row >= m.rt[k].n) {
                 report(status, EXAFAC_ERR_DEVICE, 2, row, m.rt[k].n);
                 row = m.rt[k].n - 1;
             }
-            if (lane == 0) samples[i * N + k] = (uint32_t)row;
-            for (int r = lane; r < R; r += 32) h[r] *= m.U[k][row * R + r];
-            __syncwarp();
+            if (tg == 0) samples[i * N + k] = (uint32_t)row;
+            for (int r = tg; r < R; r += nth) h[r] *= m.U[k][row * R + r];
+            grp.sync();
         }
-        warp_build_z(R, h, pa, pb, z);
-        double hq = warp_quad(R, z, PhiP);
-        if (lane == 0) weights[i] = (double)R / (hq * (double)J);
-        __syncwarp();
+        grp.build_z(R, h);
+        const T hq = grp.quad(P, PhiP);
+        // h^T Phi h > 0 for every sample the descents can reach in exact
+        // arithmetic; a rounded zero or negative value (or an empty leaf)
+        // gives the sample no weight instead of an infinite or NaN one.
+        const bool ok = !empty && hq > T(0);
+        if (tg == 0) weights[i] = ok ? (double)R / ((double)hq * (double)J) : 0.0;
+        grp.sync();
     }
 }
 
-int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
-    const int N = s.N, R = s.R, P = s.P;
-    StsModes m;
+int sts_refresh_f32(Session& s, int k, cudaStream_t st) {
+    if (s.cfg.sampler != EXAFAC_SAMPLER_STS_CP || s.cfg.precision == EXAFAC_PREC_FP64) return EXAFAC_OK;
+    EXAFAC_TRY(narrow_copy(s.F.U[k], s.Uf[k], s.dims[k] * s.R, st));
+    return narrow_copy(s.treeG[k], s.treeF[k], s.rtree[k].node_count * s.P, st);
+}
+
+template <typename T>
+static int sts_draw_launch(Session& s, int n, int64_t J, const double* uni, const T* const* treeG, const T* const* U,
+                           const T* eigG, const T* E, const T* PhiP, cudaStream_t st) {
+    const int N = s.N;
+    StsModes<T> m;
     for (int k = 0; k < kMaxModes; k++) {
         if (k < N) {
-            m.treeG[k] = s.treeG[k];
-            m.U[k] = s.F.U[k];
+            m.treeG[k] = treeG[k];
+            m.U[k] = U[k];
             m.rt[k] = s.rtree[k];
             int nx = k + 1;
             if (nx == n) nx++;
@@ -503,19 +532,36 @@ int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
             m.next[k] = 0;
         }
     }
-    int warps = 8;
-    size_t smem = align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * (P + 3 * R);
-    while (smem > 200 * 1024 && warps > 1) {
-        warps /= 2;
-        smem = align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * (P + 3 * R);
-    }
+    int G, S;
+    sample_group_shape(s.R, sizeof(T), G, S);
+    const size_t smem = (size_t)S * sample_group_bytes(s.R, sizeof(T));
     if (smem > 48 * 1024)
-        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(sts_draw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int64_t blocks = std::min<int64_t>(ceil_div(J, warps), 152 * 16);
-    sts_draw_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), warps * 32, smem, st>>>(
-        N, n, R, J, m, s.etree, s.eigG, s.Emat, s.PhiP, uni, s.samples, s.weights, s.status); count_launch();
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(sts_draw_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t blocks = std::max<int64_t>(std::min<int64_t>(ceil_div(J, S), 152 * 32), 1);
+    sts_draw_kernel<T><<<(unsigned)blocks, S * G * 32, smem, st>>>(N, n, s.R, G, S, J, m, s.etree, eigG, E, PhiP, uni,
+                                                                   s.samples, s.weights, s.status);
+    count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
+}
+
+int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
+    if (s.cfg.precision == EXAFAC_PREC_FP64) {
+        const double* treeG[kMaxModes];
+        const double* U[kMaxModes];
+        for (int k = 0; k < kMaxModes; k++) {
+            treeG[k] = k < s.N ? s.treeG[k] : nullptr;
+            U[k] = k < s.N ? s.F.U[k] : nullptr;
+        }
+        return sts_draw_launch<double>(s, n, J, uni, treeG, U, s.eigG, s.Emat, s.PhiP, st);
+    }
+    const float* treeG[kMaxModes];
+    const float* U[kMaxModes];
+    for (int k = 0; k < kMaxModes; k++) {
+        treeG[k] = k < s.N ? s.treeF[k] : nullptr;
+        U[k] = k < s.N ? s.Uf[k] : nullptr;
+    }
+    return sts_draw_launch<float>(s, n, J, uni, treeG, U, s.eigF, s.EmatF, s.PhiPF, st);
 }
 
 }  // namespace exafac

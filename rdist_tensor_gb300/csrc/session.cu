@@ -8,7 +8,9 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <deque>
 #include <new>
+#include <vector>
 
 #include "dense.cuh"
 #include "engine.cuh"
@@ -54,6 +56,15 @@ static void carve(Session& s) {
     } else {
         for (int k = 0; k < N; k++) s.treeG[k] = a.take<double>(s.rtree[k].node_count * P);
         s.eigG = a.take<double>((int64_t)N * s.etree.node_count * P);
+        if (s.cfg.precision != EXAFAC_PREC_FP64) {
+            for (int k = 0; k < N; k++) {
+                s.treeF[k] = a.take<float>(s.rtree[k].node_count * P);
+                s.Uf[k] = a.take<float>(s.dims[k] * R);
+            }
+            s.eigF = a.take<float>((int64_t)N * s.etree.node_count * P);
+            s.EmatF = a.take<float>((int64_t)(N + 1) * R2);
+            s.PhiPF = a.take<float>(P);
+        }
     }
     s.cdf_total = a.take<double>(N);
     s.gram = a.take<double>((int64_t)N * R2);
@@ -107,9 +118,10 @@ static void carve(Session& s) {
     s.os_aux = a.take<uint32_t>(4 + 4 * 256 + 1);
     s.Mc = a.take<double>(I * std::max(R, 16));  // FP64 rows of R, or FP32 rows padded to a multiple of 4
     const int64_t chunks = ceil_div(nnz, kSegChunkF32) + 1;
-    // carries: FP32 chunks of 32 hits x 32 columns, or FP64 chunks of 128 x
-    // up to 128 columns (the exact MTTKRP at R > 32)
-    const int64_t carry = std::max(chunks * kCarryStride,
+    // carries (doubles): chunks of 64 hits x 32 columns (R <= 32), of 64 hits
+    // x 32 ceil(R / 32) columns (R > 32, FP64 or FP32), or of 128 hits x
+    // 32 ceil(R / 32) columns (the exact MTTKRP)
+    const int64_t carry = std::max(chunks * (int64_t)(32 * ceil_div(R, 32)),
                                    (ceil_div(nnz, kSegChunkHits) + 1) * (int64_t)(32 * ceil_div(R, 32)));
     s.carry_first = a.take<double>(carry);
     s.carry_last = a.take<double>(carry);
@@ -117,9 +129,10 @@ static void carve(Session& s) {
     s.carry_seg = a.take<uint32_t>(chunks);
     s.chunk_seg = a.take<uint32_t>(chunks);
     s.expand_first = a.take<uint32_t>(ceil_div(nnz, kExpandChunk) + 1);
-    if (s.cfg.precision != EXAFAC_PREC_FP64) s.Uc = a.take<float>(I * 32);
+    const int64_t rs = std::max(32, f32_row_stride(R));  // FP32 rows padded to a multiple of 4 floats
+    if (s.cfg.precision != EXAFAC_PREC_FP64) s.Uc = a.take<float>(I * rs);
     s.rowbits = a.take<uint32_t>(ceil_div(I, 32));
-    s.Df = a.take<float>(J * 32);  // rows padded to a multiple of 4 floats
+    s.Df = a.take<float>(J * rs);
 }
 
 static int plan(const exafac_als_config* cfg, Session& s) {
@@ -187,6 +200,7 @@ static int refresh_sampler(Session& s, int k, bool all_rows, cudaStream_t st) {
         EXAFAC_TRY(arls_build_cdf(s, k, nullptr, nullptr, st));
     } else {
         EXAFAC_TRY(launch_tree_build(s.rtree[k], R, s.F.U[k], s.treeG[k], st));
+        EXAFAC_TRY(sts_refresh_f32(s, k, st));
     }
     return EXAFAC_OK;
 }
@@ -221,8 +235,18 @@ struct exafac_als_s {
     Session s;
     // Region timing (als_optimizer.hpp:19-27): events at the region borders
     // of each step, read back at the end of the step when enabled.
+    // Each timed step takes a set of six events from a pool and records its
+    // region borders into it; nothing waits for them until the times are read
+    // (exafac_als_region_times), or until more than kMaxPendingSteps steps are
+    // pending, when the oldest are drained.
+    static constexpr size_t kMaxPendingSteps = 512;
+    struct EventSet {
+        cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    };
     bool timing = false;
-    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::vector<EventSet> free_sets;
+    std::deque<EventSet> pending;
+    EventSet* cur = nullptr;
     double region[7] = {0, 0, 0, 0, 0, 0, 0};
     // Side stream for the design rows, their Gram and its pseudo-inverse,
     // which run beside the fiber lookup and the hit sort (fork / join events
@@ -243,8 +267,13 @@ struct exafac_als_s {
     const double* sweep_uni = nullptr;
     long long sweep_launches = 0;
     ~exafac_als_s() {
-        for (auto& e : ev)
-            if (e) cudaEventDestroy(e);
+        for (auto* list : {&free_sets})
+            for (auto& set : *list)
+                for (auto& e : set.ev)
+                    if (e) cudaEventDestroy(e);
+        for (auto& set : pending)
+            for (auto& e : set.ev)
+                if (e) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         if (fork2) cudaEventDestroy(fork2);
@@ -277,16 +306,58 @@ static int fork_design(exafac_als_s* h, int n, int64_t J, cudaStream_t st) {
     return EXAFAC_OK;
 }
 
+// Adds the region times of the oldest pending step (waits for its last event).
+static int drain_one(exafac_als_s* h) {
+    exafac_als_s::EventSet set = h->pending.front();
+    h->pending.pop_front();
+    h->free_sets.push_back(set);
+    EXAFAC_CUDA_TRY(cudaEventSynchronize(set.ev[5]));
+    const int map[5] = {0, 2, 3, 5, 6};  // R1, R3, R4, R6, R7
+    float ms[5];
+    for (int i = 0; i < 5; i++) {
+        // A step that returned an error part way left later borders
+        // unrecorded: it adds nothing.
+        if (cudaEventElapsedTime(&ms[i], set.ev[i], set.ev[i + 1]) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return EXAFAC_OK;
+        }
+    }
+    for (int i = 0; i < 5; i++) h->region[map[i]] += ms[i] * 1e-3;
+    return EXAFAC_OK;
+}
+
+static int drain_all(exafac_als_s* h) {
+    while (!h->pending.empty()) EXAFAC_TRY(drain_one(h));
+    return EXAFAC_OK;
+}
+
+// Region border i of the current step (0 opens the step, 5 closes it).
 static int mark(exafac_als_s* h, int i, cudaStream_t st) {
-    if (h->timing) EXAFAC_CUDA_TRY(cudaEventRecord(h->ev[i], st));
+    if (!h->timing) return EXAFAC_OK;
+    if (i == 0) {
+        if (h->pending.size() >= exafac_als_s::kMaxPendingSteps) EXAFAC_TRY(drain_one(h));
+        exafac_als_s::EventSet set;
+        if (!h->free_sets.empty()) {
+            set = h->free_sets.back();
+            h->free_sets.pop_back();
+        } else {
+            for (auto& e : set.ev) EXAFAC_CUDA_TRY(cudaEventCreate(&e));
+        }
+        h->pending.push_back(set);
+        h->cur = &h->pending.back();
+    }
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->cur->ev[i], st));
     return EXAFAC_OK;
 }
 
 extern "C" int exafac_als_enable_timing(exafac_als_t h, int32_t enable) {
     EXAFAC_ARG(h != nullptr, "null session");
-    if (enable && !h->ev[0]) {
-        for (auto& e : h->ev) EXAFAC_CUDA_TRY(cudaEventCreate(&e));
+    // steps timed before this call no longer count
+    while (!h->pending.empty()) {
+        h->free_sets.push_back(h->pending.front());
+        h->pending.pop_front();
     }
+    h->cur = nullptr;
     h->timing = enable != 0;
     for (double& r : h->region) r = 0.0;
     return EXAFAC_OK;
@@ -294,6 +365,7 @@ extern "C" int exafac_als_enable_timing(exafac_als_t h, int32_t enable) {
 
 extern "C" int exafac_als_region_times(exafac_als_t h, double* out7) {
     EXAFAC_ARG(h != nullptr && out7 != nullptr, "null argument");
+    EXAFAC_TRY(drain_all(h));
     for (int i = 0; i < 7; i++) out7[i] = h->region[i];
     return EXAFAC_OK;
 }
@@ -428,51 +500,34 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     // U = MTTKRP * Phi on the touched rows (the other rows are zero).
     const bool arls = s.cfg.sampler == EXAFAC_SAMPLER_CP_ARLS_LEV;
     const bool tiled = s.R <= 32;
-    EXAFAC_TRY(lookup_hits(s, n, J, tiled && s.cfg.precision != EXAFAC_PREC_FP64, st));
+    EXAFAC_TRY(lookup_hits(s, n, J, s.cfg.precision != EXAFAC_PREC_FP64, st));
     // rowbits is set: the old rows are cleared on the side stream
     EXAFAC_CUDA_TRY(cudaEventRecord(h->fork2, st));
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork2, 0));
     EXAFAC_TRY(zero_old_rows(s, n, h->side));
     EXAFAC_CUDA_TRY(cudaEventRecord(h->join2, h->side));
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join, 0));
-    if (tiled) {
-        EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
-    } else {
-        EXAFAC_TRY(clear_dense_factor(s, n, st));
-        EXAFAC_TRY(spmm_solve(s, n, st));
-    }
+    if (tiled) EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
+    else EXAFAC_TRY(mttkrp_solve_wide(s, n, st));
     // the old rows are cleared (the renormalisation may rescale every row)
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join2, 0));
     EXAFAC_TRY(mark(h, 3, st));
     // R5 (dense reduce) is empty at one rank.  R6: renormalise (and, for
     // CP-ARLS-LEV, the new leverage scores of the touched rows).
-    if (tiled) {
-        EXAFAC_TRY(normalize_balanced(s, n, arls, st));
-    } else {
-        EXAFAC_TRY(normalize_factor(s, n, false, st));
-        if (arls) {
-            EXAFAC_TRY(launch_pinv(s.R, s.ngram, s.upinv, 1e-11, s.vt, st));
-            EXAFAC_TRY(arls_leverage(s, n, false, s.upinv, st));
-        }
-    }
+    if (tiled) EXAFAC_TRY(normalize_balanced(s, n, arls, st));
+    else EXAFAC_TRY(normalize_wide(s, n, arls, st));
     EXAFAC_TRY(mark(h, 4, st));
     // R7: sampler update (CDF of the new scores, or the row tree).
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.gram + (int64_t)n * s.R * s.R, s.ngram, sizeof(double) * s.R * s.R,
                                     cudaMemcpyDeviceToDevice, st));
     if (arls) EXAFAC_TRY(arls_build_cdf(s, n, s.touched, s.counters + 2, st));
-    else EXAFAC_TRY(launch_tree_build(s.rtree[n], s.R, s.F.U[n], s.treeG[n], st));
+    else {
+        EXAFAC_TRY(launch_tree_build(s.rtree[n], s.R, s.F.U[n], s.treeG[n], st));
+        EXAFAC_TRY(sts_refresh_f32(s, n, st));
+    }
     EXAFAC_TRY(keep_touched(s, n, st));
     s.dense[n] = false;
     EXAFAC_TRY(mark(h, 5, st));
-    if (h->timing) {
-        EXAFAC_CUDA_TRY(cudaEventSynchronize(h->ev[5]));
-        const int map[5] = {0, 2, 3, 5, 6};  // R1, R3, R4, R6, R7
-        for (int i = 0; i < 5; i++) {
-            float ms = 0.f;
-            EXAFAC_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]));
-            h->region[map[i]] += ms * 1e-3;
-        }
-    }
     return EXAFAC_OK;
 }
 
@@ -528,7 +583,7 @@ extern "C" int exafac_als_sweeps(exafac_als_t h, int64_t J, int32_t count, const
     Session& s = h->s;
     EXAFAC_ARG(J >= 1 && J <= s.Jmax, "J out of range");
     EXAFAC_ARG(count >= 0, "count must be >= 0");
-    EXAFAC_ARG(!h->timing, "exafac_als_sweeps: region timing is on (it reads events after every step)");
+    EXAFAC_ARG(!h->timing, "exafac_als_sweeps: region timing is on (region borders are recorded by exafac_als_step)");
     cudaStream_t st = (cudaStream_t)stream;
     int done = 0;
     // A factor that no sampled step has updated yet is cleared whole by its
@@ -607,6 +662,18 @@ extern "C" int exafac_als_fit(exafac_als_t h, double* fit, void* stream) {
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(v, s.scal + 1, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     EXAFAC_TRY(check_status(s, st));
     *fit = 1.0 - std::sqrt(v[0] + v[1]) / s.tensor_norm;
+    return EXAFAC_OK;
+}
+
+extern "C" int exafac_als_set_wait_limit(exafac_als_t h, uint32_t polls, int64_t withhold_tile) {
+    EXAFAC_ARG(h != nullptr, "null session");
+    EXAFAC_ARG(withhold_tile >= -1, "withhold_tile must be -1 (off) or a tile index");
+    h->s.wait_polls = polls == 0 ? kSpinLimit : polls;
+    h->s.withhold_tile = withhold_tile;
+    if (h->sweep_exec) {  // the captured sweep holds the old limits
+        cudaGraphExecDestroy(h->sweep_exec);
+        h->sweep_exec = nullptr;
+    }
     return EXAFAC_OK;
 }
 

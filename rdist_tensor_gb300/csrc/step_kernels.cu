@@ -448,8 +448,8 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_kernel(int N, in
 }
 
 // R > 32 (padded to RP = 64 or 128): the block's 8 warps share one 32-row
-// tile (warp w builds rows 4w..4w+3, FP64 row products, D' = d w in FP64 for
-// the FP64 MTTKRP), and split the lower-triangle 16 x 8 MMA blocks of the
+// tile (warp w builds rows 4w..4w+3, FP64 row products, D' = d w rounded to
+// FP32 for the FP32 MTTKRP), and split the lower-triangle 16 x 8 MMA blocks of the
 // RP x RP Gram between them; each Gram entry has one owner, so the block sum
 // needs no ordering.
 template <int kRound, int RP>
@@ -457,9 +457,10 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_wide_kernel(int 
                                                                             const int64_t* __restrict__ ju_dev,
                                                                             const uint32_t* __restrict__ sd,
                                                                             const double* __restrict__ wd,
-                                                                            FactorPtrs f, double* __restrict__ D,
+                                                                            FactorPtrs f, float* __restrict__ Df,
                                                                             double* __restrict__ part) {
     constexpr int kStride = RP + 8;  // row stride mod 32 == 8: conflict-free fragment loads
+    const int ldf = f32_row_stride(R);  // FP32 design rows for the FP32 MTTKRP
     constexpr int kMT = RP / 16;
     constexpr int kPairs = kMT * (kMT + 1);  // m-tile mt pairs with n-tiles 0 .. 2 mt + 1
     constexpr int kPerWarp = (kPairs + kDesignWarps - 1) / kDesignWarps;
@@ -518,7 +519,7 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_wide_kernel(int 
                 float v = 0.0f;
                 if (r < nrow && c < R) {
                     const double x = d[cb] * sw;
-                    D[j * R + c] = x * sw;
+                    Df[j * ldf + c] = (float)(x * sw);
                     v = kRound == 1 ? round_tf32((float)x) : round_bf16((float)x);
                 }
                 t[r][c] = v;
@@ -570,7 +571,7 @@ static int launch_design_wide(Session& s, int n, cudaStream_t st) {
         EXAFAC_CUDA_TRY(cudaFuncSetAttribute(design_mma_wide_kernel<kRound, RP>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     design_mma_wide_kernel<kRound, RP><<<kDesignBlocks, kDesignWarps * 32, smem, st>>>(
-        s.N, n, s.R, s.counters + 0, s.sd, s.wd, factor_ptrs(s), s.D, s.part);
+        s.N, n, s.R, s.counters + 0, s.sd, s.wd, factor_ptrs(s), s.Df, s.part);
     count_launch();
     return EXAFAC_OK;
 }
@@ -580,7 +581,7 @@ int design_gram(Session& s, int n, int64_t J, cudaStream_t st) {
     int64_t nblk = std::max<int64_t>(1, ceil_div(J, kGramRows));
     if (s.cfg.precision != EXAFAC_PREC_FP64) {
         const bool tf32 = s.cfg.precision == EXAFAC_PREC_TF32;
-        if (R > 32) {  // FP64 design rows for the FP64 MTTKRP, tensor-core Gram
+        if (R > 32) {  // FP32 design rows for the FP32 MTTKRP, tensor-core Gram
             int rc;
             if (R <= 64) rc = tf32 ? launch_design_wide<1, 64>(s, n, st) : launch_design_wide<2, 64>(s, n, st);
             else rc = tf32 ? launch_design_wide<1, 128>(s, n, st) : launch_design_wide<2, 128>(s, n, st);

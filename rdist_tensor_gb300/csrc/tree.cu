@@ -62,32 +62,23 @@ __global__ void tree_hadamard_kernel(int64_t nodes, int R, double* __restrict__ 
     }
 }
 
-__global__ void tree_sample_kernel(TreeShape t, int R, const double* __restrict__ G, const double* __restrict__ U,
-                                   int64_t J, const double* __restrict__ x, double* __restrict__ hmul,
-                                   const double* __restrict__ draws, uint32_t* __restrict__ out, int64_t out_stride) {
-    extern __shared__ unsigned char smraw[];
-    const int P = packed_size(R);
-    const int warps = blockDim.x / 32;
-    unsigned short* pa = reinterpret_cast<unsigned short*>(smraw);
-    unsigned short* pb = pa + P;
-    double* base = reinterpret_cast<double*>(smraw + align_up(2 * P * sizeof(unsigned short), 16));
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = P + R + (int)t.F;
-    double* z_sm = base + (size_t)w * per_warp;
-    double* x_sm = z_sm + P;
-    double* q_sm = x_sm + R;
-    block_build_pairs(R, pa, pb);
-    __syncthreads();
-    for (int64_t i = (int64_t)blockIdx.x * warps + w; i < J; i += (int64_t)gridDim.x * warps) {
-        for (int r = lane; r < R; r += 32) x_sm[r] = x[i * R + r];
-        __syncwarp();
-        warp_build_z(R, x_sm, pa, pb, z_sm);
-        int64_t row = warp_descend(t, R, G, U, z_sm, x_sm, q_sm, draws[i]);
-        if (lane == 0) out[i * out_stride] = (uint32_t)row;
-        if (row < t.n) {
-            for (int r = lane; r < R; r += 32) hmul[i * R + r] *= U[row * R + r];
-        }
-        __syncwarp();
+// PTSample for J samples (FP64), one sample per group of G warps.
+__global__ void tree_sample_kernel(TreeShape t, int R, int G, int S, const double* __restrict__ Gt,
+                                   const double* __restrict__ U, int64_t J, const double* __restrict__ x,
+                                   double* __restrict__ hmul, const double* __restrict__ draws,
+                                   uint32_t* __restrict__ out, int64_t out_stride) {
+    extern __shared__ __align__(16) unsigned char tsdyn[];
+    double *xs, *unused, *q;
+    int gi;
+    const SampleGroup<double> grp = sample_group<double>(tsdyn, R, G, xs, unused, q, gi);
+    for (int64_t i = (int64_t)blockIdx.x * S + gi; i < J; i += (int64_t)gridDim.x * S) {
+        for (int r = grp.tg; r < R; r += grp.nthreads()) xs[r] = x[i * R + r];
+        grp.sync();
+        grp.build_z(R, xs);
+        const int64_t row = descend<double>(grp, t, R, Gt, U, xs, q, draws[i]);
+        if (grp.tg == 0) out[i * out_stride] = (uint32_t)row;
+        for (int r = grp.tg; r < R; r += grp.nthreads()) hmul[i * R + r] *= U[row * R + r];
+        grp.sync();
     }
 }
 
@@ -128,27 +119,19 @@ int launch_tree_hadamard(const TreeShape& t, int R, double* G, const double* M, 
     return EXAFAC_OK;
 }
 
-size_t tree_sample_smem(int R, int64_t F, int warps) {
-    const int P = packed_size(R);
-    return align_up(2 * P * sizeof(unsigned short), 16) + sizeof(double) * warps * (P + R + F);
-}
-
 int launch_tree_sample(const TreeShape& t, int R, const double* G, const double* U, int64_t J, const double* x,
                        double* hmul, const double* draws, uint32_t* out, int64_t out_stride, cudaStream_t stream) {
-    int warps = 8;
-    size_t smem = tree_sample_smem(R, t.F, warps);
-    while (smem > 200 * 1024 && warps > 1) {
-        warps /= 2;
-        smem = tree_sample_smem(R, t.F, warps);
-    }
-    if (smem > 48 * 1024) {
-        EXAFAC_CUDA_TRY(
-            cudaFuncSetAttribute(tree_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
-    int64_t blocks = (J + warps - 1) / warps;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    int Gw, S;
+    sample_group_shape(R, sizeof(double), Gw, S);
+    const size_t smem = (size_t)S * sample_group_bytes(R, sizeof(double));
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(tree_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t blocks = (J + S - 1) / S;
+    if (blocks > 152 * 32) blocks = 152 * 32;
     if (blocks < 1) blocks = 1;
-    tree_sample_kernel<<<(int)blocks, warps * 32, smem, stream>>>(t, R, G, U, J, x, hmul, draws, out, out_stride); count_launch();
+    tree_sample_kernel<<<(int)blocks, S * Gw * 32, smem, stream>>>(t, R, Gw, S, G, U, J, x, hmul, draws, out,
+                                                                   out_stride);
+    count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
@@ -172,6 +155,10 @@ extern "C" int exafac_tree_sample(int64_t n, int32_t F, int32_t R, const double*
                                   const double* x, double* hmul, const double* draws, uint32_t* rows_out,
                                   int64_t rows_stride, void* stream) {
     EXAFAC_ARG(n >= 1 && F >= 1 && R >= 1 && R <= kMaxRank && J >= 0, "exafac_tree_sample: bad shape");
+    if (F > kMaxLeafRows) {
+        set_error("exafac_tree_sample: leaves of more than 128 rows are not supported");
+        return EXAFAC_ERR_UNSUPPORTED;
+    }
     EXAFAC_ARG(G && U && x && hmul && draws && rows_out, "exafac_tree_sample: null pointer");
     if (J == 0) return EXAFAC_OK;
     return launch_tree_sample(make_tree_shape(n, F), R, G, U, J, x, hmul, draws, rows_out, rows_stride,

@@ -3,6 +3,8 @@
 // triangle of its Gram, P = R(R+1)/2 doubles, row-major packed
 // (entry (a, b), a <= b, at a*R - a*(a-1)/2 + (b - a)).
 #pragma once
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace exafac {
@@ -52,30 +54,21 @@ int launch_tree_sample(const TreeShape& t, int R, const double* G, const double*
                        double* hmul, const double* draws, uint32_t* out, int64_t out_stride, cudaStream_t stream);
 
 // ---------------------------------------------------------------------------
-// Device pieces shared with the fused STS-CP sampler.
+// Device pieces shared by PTSample and the fused STS-CP sampler, in FP64
+// (T = double, the reference's arithmetic) or FP32 (the mixed forms, over
+// FP32 copies of the trees and factors).  A group of G warps (32 G threads,
+// G in {1, 2, 4}) draws one sample at a time.  Per descent the group forms
+// z_e = w_e x_a x_b in shared memory (packed order, w = 1 on the diagonal and
+// 2 above it), so that x^T G x = sum_e z_e G_e for every packed node G: each
+// level is then one coalesced pass over the node, P / (32 G) multiply-adds
+// per thread, and a group sum in a fixed order.  G > 1 splits one sample's
+// levels over several warps at large R, where a warp's share of shared memory
+// (z holds P = R (R + 1) / 2 values) would otherwise leave few warps per SM.
+// With G > 1 the block is the group (barriers are __syncthreads()).
 // ---------------------------------------------------------------------------
 
-// Per-warp precomputation of z_e = w_e x_a x_b (w = 1 on the diagonal, 2 off
-// it) so that x^T G x = sum_e z_e G_e for every packed node G.
-__device__ __forceinline__ void warp_build_z(int R, const double* x_sm, const unsigned short* pa,
-                                             const unsigned short* pb, double* z_sm) {
-    const int P = packed_size(R);
-    const int lane = threadIdx.x & 31;
-    for (int e = lane; e < P; e += 32) {
-        int a = pa[e], b = pb[e];
-        double v = x_sm[a] * x_sm[b];
-        z_sm[e] = (a == b) ? v : 2.0 * v;
-    }
-    __syncwarp();
-}
-
-__device__ __forceinline__ double warp_quad(int R, const double* z_sm, const double* __restrict__ g) {
-    const int P = packed_size(R);
-    const int lane = threadIdx.x & 31;
-    double acc = 0.0;
-    for (int e = lane; e < P; e += 32) acc = fma(z_sm[e], __ldg(g + e), acc);
-    return warp_sum(acc);
-}
+__device__ __forceinline__ double fmat(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmat(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 // Fills pa/pb (P entries each) with the (row, col) of each packed index.
 __device__ __forceinline__ void block_build_pairs(int R, unsigned short* pa, unsigned short* pb) {
@@ -88,21 +81,80 @@ __device__ __forceinline__ void block_build_pairs(int R, unsigned short* pa, uns
     }
 }
 
-// One descent of PTSample (partition_tree.hpp:226-380) by the calling warp.
-// z_sm: the sample's z (see warp_build_z); x_sm: the descent vector x (R);
-// q_sm: F doubles of scratch.  Returns the chosen row (< n unless the
-// uniform hits the upper edge of a partial leaf, see the reference).
-__device__ __forceinline__ int64_t warp_descend(const TreeShape& t, int R, const double* __restrict__ G,
-                                                const double* __restrict__ U, const double* z_sm, const double* x_sm,
-                                                double* q_sm, double d) {
+template <typename T>
+struct SampleGroup {
+    int G;     // warps per sample
+    int tg;    // thread index within the group
+    T* z;      // P
+    T* red;    // G partial sums
+    __device__ __forceinline__ int nthreads() const { return 32 * G; }
+    __device__ __forceinline__ void sync() const {
+        if (G == 1) __syncwarp();
+        else __syncthreads();
+    }
+    // The group's sum of v (every thread gets it); partial sums of the warps
+    // added in warp order.
+    __device__ __forceinline__ T sum(T v) const {
+        v = warp_sum(v);
+        if (G == 1) return v;
+        if ((tg & 31) == 0) red[tg >> 5] = v;
+        __syncthreads();
+        T s = red[0];
+        for (int w = 1; w < G; w++) s += red[w];
+        __syncthreads();
+        return s;
+    }
+    // z = packed w_ab x_a x_b (rows split over the group's threads).
+    __device__ __forceinline__ void build_z(int R, const T* x) const {
+        for (int a = tg; a < R; a += nthreads()) {
+            const T xa = x[a];
+            const T xa2 = xa + xa;
+            T* zr = z + packed_index(R, a, a) - a;
+            zr[a] = xa * xa;
+            for (int b = a + 1; b < R; b++) zr[b] = xa2 * x[b];
+        }
+        sync();
+    }
+    // x^T G x = sum_e z_e G_e for one packed node.
+    __device__ __forceinline__ T quad(int P, const T* __restrict__ g) const {
+        T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+        const int step = nthreads();
+        int e = tg;
+        for (; e + 3 * step < P; e += 4 * step) {
+            a0 = fmat(z[e], __ldg(g + e), a0);
+            a1 = fmat(z[e + step], __ldg(g + e + step), a1);
+            a2 = fmat(z[e + 2 * step], __ldg(g + e + 2 * step), a2);
+            a3 = fmat(z[e + 3 * step], __ldg(g + e + 3 * step), a3);
+        }
+        for (; e < P; e += step) a0 = fmat(z[e], __ldg(g + e), a0);
+        return sum((a0 + a1) + (a2 + a3));
+    }
+};
+
+// One descent of PTSample (partition_tree.hpp:204-380) by the group, with
+// the uniform d and z built from the descent vector x: root mass, one
+// left-child quadratic form per level (cutoff = low + m_L / m), the tail
+// level, then, for F > 1, the leaf's rows by the prefix of their squared dots
+// U_j . x (thread per row; the prefix a warp scan in row order): the first
+// row j < F - 1 with frac < prefix_j / total, else the leaf's last row.
+// q: F values of group scratch.  Returns the chosen row (< n).
+//
+// A leaf whose rows all have zero dot with x (possible only through rounding
+// of the cutoffs, in practice in FP32: the descent stepped into a child of
+// zero mass) sets *empty and returns its first row; the caller gives the
+// sample weight 0.  The reference's loop would pick the leaf's last slot
+// there (0 / 0 comparisons), possibly past the tensor.
+template <typename T>
+__device__ __forceinline__ int64_t descend(const SampleGroup<T>& grp, const TreeShape& t, int R,
+                                           const T* __restrict__ G, const T* __restrict__ U, const T* x, T* q, T d,
+                                           bool* empty = nullptr) {
     const int P = packed_size(R);
-    const int lane = threadIdx.x & 31;
     int64_t c = 0;
-    double low = 0.0, high = 1.0;
-    const double m = warp_quad(R, z_sm, G);
+    T low = T(0), high = T(1);
+    const T m = grp.quad(P, G);
     for (int64_t lvl = 0; lvl < t.lfill_level; lvl++) {
-        double mL = warp_quad(R, z_sm, G + (2 * c + 1) * P);
-        double cutoff = low + mL / m;
+        const T mL = grp.quad(P, G + (2 * c + 1) * P);
+        const T cutoff = low + mL / m;
         if (d <= cutoff) {
             c = 2 * c + 1;
             high = cutoff;
@@ -112,8 +164,8 @@ __device__ __forceinline__ int64_t warp_descend(const TreeShape& t, int R, const
         }
     }
     if (t.node_count > t.nodes_before_lfill && !tree_is_leaf(t, c)) {
-        double mL = warp_quad(R, z_sm, G + (2 * c + 1) * P);
-        double cutoff = low + mL / m;
+        const T mL = grp.quad(P, G + (2 * c + 1) * P);
+        const T cutoff = low + mL / m;
         if (d <= cutoff) {
             c = 2 * c + 1;
             high = cutoff;
@@ -123,46 +175,116 @@ __device__ __forceinline__ int64_t warp_descend(const TreeShape& t, int R, const
         }
     }
     const int64_t leaf = tree_leaf_idx(t, c);
-    int64_t res = 0;
-    if (t.F > 1) {
-        const double frac = (d - low) / (high - low);
-        const int64_t F = t.F;
-        const int64_t rows = (t.n - leaf * F) < F ? (t.n - leaf * F) : F;
-        for (int64_t j = lane; j < F; j += 32) {
-            double v = 0.0;
-            if (j < rows) {
-                const double* u = U + (leaf * F + j) * R;
-                for (int r = 0; r < R; r++) v = fma(__ldg(u + r), x_sm[r], v);
-            }
-            q_sm[j] = v * v;
+    if (t.F <= 1) return leaf * t.F;
+    const T frac = (d - low) / (high - low);
+    const int64_t F = t.F;
+    const int64_t rows = (t.n - leaf * F) < F ? (t.n - leaf * F) : F;
+    const T* Ub = U + leaf * F * R;
+    for (int64_t j = grp.tg; j < F; j += grp.nthreads()) {
+        T v = T(0);
+        if (j < rows) {
+            const T* u = Ub + j * R;
+            for (int r = 0; r < R; r++) v = fmat(__ldg(u + r), x[r], v);
         }
-        __syncwarp();
-        // Sequential exclusive prefix of q^2 in row order, as the reference
-        // accumulates it; q_sm[j] becomes the prefix through row j.
-        double total = 0.0;
-        if (lane == 0) {
-            double run = 0.0;
-            for (int64_t j = 0; j < F; j++) {
-                run += q_sm[j];
-                q_sm[j] = run;
-            }
-            total = run;
-        }
-        total = __shfl_sync(0xffffffffu, total, 0);
-        __syncwarp();
-        res = F - 1;
-        for (int64_t base = 0; base < F - 1; base += 32) {
-            int64_t j = base + lane;
-            bool hit = (j < F - 1) && (frac < q_sm[j] / total);
-            unsigned mask = __ballot_sync(0xffffffffu, hit);
-            if (mask) {
-                res = base + __ffs(mask) - 1;
-                break;
-            }
-        }
-        __syncwarp();
+        q[j] = v * v;
     }
-    return res + leaf * t.F;
+    grp.sync();
+    // warp 0: inclusive prefix in row order (F <= 128), then the first row
+    // with frac < prefix / total
+    int64_t res = 0;
+    bool is_empty = false;
+    if (grp.tg < 32) {
+        const int lane = grp.tg;
+        T incl[4];
+        T carry = T(0);
+#pragma unroll
+        for (int blk = 0; blk < 4; blk++) {
+            const int64_t j = 32 * blk + lane;
+            T v = j < F ? q[j] : T(0);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const T u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            incl[blk] = carry + v;
+            carry += __shfl_sync(0xffffffffu, v, 31);
+        }
+        const T total = carry;
+        if (!(total > T(0))) {
+            is_empty = true;
+        } else {
+            res = F - 1;
+#pragma unroll
+            for (int blk = 0; blk < 4; blk++) {
+                const int64_t j = 32 * blk + lane;
+                const bool hit = (j < F - 1) && (frac < incl[blk] / total);
+                const unsigned mask = __ballot_sync(0xffffffffu, hit);
+                if (mask) {
+                    res = 32 * blk + __ffs(mask) - 1;
+                    break;
+                }
+            }
+            // frac >= 1 (the uniform equal to the leaf's upper cutoff) leaves
+            // the last slot, which a partial leaf does not hold
+            if (res >= rows) res = rows - 1;
+        }
+    }
+    if (grp.G > 1) {  // broadcast warp 0's choice to the other warps (through q, read by now)
+        // (a 32-bit slot: q is only 4-byte aligned in the FP32 layout; res < 128)
+        __syncthreads();
+        if (grp.tg == 0) reinterpret_cast<int*>(q)[0] = is_empty ? -1 : (int)res;
+        __syncthreads();
+        const int v = reinterpret_cast<const int*>(q)[0];
+        is_empty = v < 0;
+        res = is_empty ? 0 : (int64_t)v;
+        __syncthreads();
+    }
+    if (is_empty) {
+        if (empty) *empty = true;
+        return leaf * F;
+    }
+    return res + leaf * F;
+}
+
+// Leaves of at most this many rows (PTSample's F); the STS-CP row trees use
+// F = R <= 128.
+constexpr int kMaxLeafRows = 128;
+
+// Shared memory of one sample's group: z (P), h and sh (R each), q (128),
+// red (8), in elements of esz bytes, rounded to 16 bytes.
+__host__ __device__ inline size_t sample_group_bytes(int R, int esz) {
+    return ((size_t)esz * (packed_size(R) + 2 * R + kMaxLeafRows + 8) + 15) / 16 * 16;
+}
+
+// Warps per sample (G) and samples per block (S) for rank R and element size
+// esz: G = 4 above P = 4096 (R > 90), 2 above P = 1024 (R > 44), else 1; with
+// G = 1 up to 8 samples (warps) per block, fewer when their shared memory
+// would pass 64 KB.
+inline void sample_group_shape(int R, int esz, int& G, int& S) {
+    const int P = packed_size(R);
+    G = P > 4096 ? 4 : (P > 1024 ? 2 : 1);
+    S = 1;
+    if (G == 1) S = (int)std::max<size_t>(1, std::min<size_t>(8, (64 * 1024) / sample_group_bytes(R, esz)));
+}
+
+// The calling thread's group, and its h / sh / q buffers, in dynamic shared
+// memory laid out group after group.
+template <typename T>
+__device__ __forceinline__ SampleGroup<T> sample_group(unsigned char* dyn, int R, int G, T*& h, T*& sh, T*& q,
+                                                       int& gi) {
+    const size_t bytes = sample_group_bytes(R, sizeof(T));
+    gi = (threadIdx.x >> 5) / G;
+    T* base = reinterpret_cast<T*>(dyn + gi * bytes);
+    const int P = packed_size(R);
+    h = base + P;
+    sh = h + R;
+    q = sh + R;
+    SampleGroup<T> grp;
+    grp.G = G;
+    grp.tg = threadIdx.x - gi * 32 * G;
+    grp.z = base;
+    grp.red = q + kMaxLeafRows;
+    return grp;
 }
 
 }  // namespace exafac

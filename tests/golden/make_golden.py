@@ -16,6 +16,13 @@ Fixtures:
                  updated factors, sigma, hit counts, fits.
   workload1.npz  the 2000^3 / 2e6-nonzero planted tensor, R=25, J=65536,
                  STS-CP, one sweep (tensor and uniforms regenerated from seeds).
+  keys128.npz    a 5-mode tensor whose packed off-mode keys need 64 to 73 bits,
+                 one sweep per sampler.
+  sweeps20.npz, sweeps20_dense.npz
+                 20 sweeps of STS-CP (the 2000^3 workload; a 150^3 tensor with
+                 30 % observed): fit after every sweep, sigma after every step.
+  exact.npz      ExactALS, two sweeps on a 3- and a 4-mode tensor.
+  stats_*.json   the statistics JSON of execute_ALS_rounds.
 """
 import json
 import os
@@ -163,8 +170,157 @@ def workload1():
     np.savez_compressed(os.path.join(HERE, "workload1.npz"), **out)
 
 
+def support_tensor(dims, support, nnz, R, seed):
+    """A tensor whose nonzeros sit on a small grid of coordinates spread over
+    large modes (the highest coordinate of every mode included, so every bit of
+    the packed keys is exercised), and factors that are nonzero only on those
+    rows: sampled fibres then hold nonzeros, as they do after the exact-ALS
+    preprocessing of a sparse tensor."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for d, s in zip(dims, support):
+        r = np.sort(rng.choice(d - 1, size=s - 1, replace=False))
+        rows.append(np.concatenate([r, [d - 1]]).astype(np.uint32))
+    cells = int(np.prod(support))
+    lin = rng.choice(cells, size=nnz, replace=False)
+    local = np.stack(np.unravel_index(lin, tuple(support)), axis=1)
+    idx = np.stack([rows[k][local[:, k]] for k in range(len(dims))], axis=1).astype(np.uint32)
+    vals = rng.random(nnz) + 0.5
+    fvals = []
+    for k, d in enumerate(dims):
+        v = rng.standard_normal((len(rows[k]), R))
+        v /= np.sqrt((v * v).sum(axis=0))[None, :]
+        fvals.append(v)
+    return np.ascontiguousarray(idx), vals, rows, fvals
+
+
+def dense_factors(dims, rows, fvals):
+    out = []
+    for d, r, v in zip(dims, rows, fvals):
+        U = np.zeros((int(d), v.shape[1]))
+        U[r] = v
+        out.append(U)
+    return out
+
+
+def keys128():
+    """5-mode tensor whose packed off-mode coordinates need more than 64 bits
+    for modes 1-4 (65, 65, 65, 73 bits) and exactly 64 for mode 0; one full
+    sweep per sampler.  Factor rows are stored on the support only (the other
+    rows are zero before and after every step)."""
+    dims = (300_000, 250_000, 200_000, 150_000, 900)
+    support = (12, 10, 9, 8, 6)
+    R, J, nnz = 6, 1500, 4000
+    idx, vals, rows, fvals = support_tensor(dims, support, nnz, R, seed=21)
+    factors = dense_factors(dims, rows, fvals)
+    out = {"dims": np.array(dims, dtype=np.int64), "R": np.int64(R), "J": np.int64(J), "idx": idx, "vals": vals}
+    for k in range(len(dims)):
+        out[f"rows{k}"] = rows[k]
+        out[f"fvals{k}"] = fvals[k]
+    for sampler in ("cp_arls_lev", "sts_cp"):
+        rec = run_sweep(dims, idx, vals, R, factors, sampler, J, (31, 32), steps=len(dims))
+        for t in range(len(dims)):
+            U = rec.pop(f"s{t}_factor")
+            n = t % len(dims)
+            assert not np.any(np.delete(U, rows[n], axis=0)), "factor rows outside the support"
+            rec[f"s{t}_factor_rows"] = U[rows[n]]
+            rec[f"s{t}_spmm_out_rows"] = rec.pop(f"s{t}_spmm_out")[rows[n]]
+        for k, v in rec.items():
+            out[f"{sampler}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "keys128.npz"), **out)
+
+
+def sweeps20(dense=False):
+    """20 full sweeps of STS-CP by the reference with its local stream
+    reseeded: the fit after every sweep and sigma after every step.  Default:
+    the 2000^3 / 2e6-nonzero planted tensor, R=25, J=65536 (its fit stays near
+    zero: 2.5e-4 of the entries are observed).  dense=True: a 150^3 planted
+    rank-8 tensor with 30 % of its entries observed, R=8, J=16384, whose fit
+    converges to a clearly positive value."""
+    if dense:
+        dims, idx, vals = synthetic.planted_uniform(dims=(150, 150, 150), nnz=1_012_500, rank=8, seed=5,
+                                                    nonneg=False)
+        R, J, sweeps = 8, 16384, 20
+        factors = synthetic.gaussian_factors(dims, R, seed=6)
+        seeds = (5353, 5454)
+        name = "sweeps20_dense.npz"
+    else:
+        dims, idx, vals = synthetic.planted_uniform(seed=0)
+        R, J, sweeps = 25, 65536, 20
+        factors = synthetic.gaussian_factors(dims, R, seed=1)
+        seeds = (5151, 5252)
+        name = "sweeps20.npz"
+    keep, st, lr, s, opt = make_problem(dims, idx, vals, R, factors, "sts_cp", seeds)
+    N = len(dims)
+    fits = [opt.compute_exact_fit()]
+    sigmas = []
+    for _ in range(sweeps):
+        for n in range(N):
+            opt.execute_ALS_step(n, J)
+            sigmas.append(lr.get_sigma()[0])
+        fits.append(opt.compute_exact_fit())
+        print(f"sweep {len(fits) - 1}: fit {fits[-1]:.8f}", flush=True)
+    out = {"seeds": np.array(seeds, dtype=np.int64), "R": np.int64(R), "J": np.int64(J), "sweeps": np.int64(sweeps),
+           "fits": np.array(fits), "sigmas": np.array(sigmas),
+           "final_factor0_head": lr.get_factor(0)[:64]}
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
+def sweeps20_dense():
+    sweeps20(dense=True)
+
+
+def exact():
+    """ExactALS (exact_als.hpp:90-143): two sweeps from given factors on a
+    3-mode and a 4-mode tensor; factors and sigma after every step, fits."""
+    out = {}
+    for name, (d, nnz, R, seed) in {"e3": ((40, 35, 30), 2500, 5, 41), "e4": ((15, 12, 10, 9), 900, 4, 42)}.items():
+        dims, idx, vals = synthetic.random_sparse(d, nnz, seed=seed)
+        factors = synthetic.gaussian_factors(dims, R, seed=seed + 1)
+        dims32 = np.asarray(dims, dtype=np.int32)
+        g = REF.Grid(np.ones(len(dims), dtype=np.int32))
+        tg = REF.TensorGrid(dims32, g)
+        st = REF.SparseTensor(tg, np.ascontiguousarray(idx, dtype=np.uint32), np.asarray(vals, dtype=np.float64),
+                              "none")
+        st.set_indices(np.ascontiguousarray(idx, dtype=np.uint32))
+        lr = REF.LowRankTensor(R, tg)
+        for k, U in enumerate(factors):
+            lr.set_factor(k, U)
+        lr.set_sigma(np.ones(R))
+        opt = REF.ExactALS(st, lr)
+        opt.initialize_ground_truth_for_als()
+        out[f"{name}_fit0"] = opt.compute_exact_fit()
+        N = len(dims)
+        for t in range(2 * N):
+            opt.execute_ALS_step(t % N, 0)
+            out[f"{name}_s{t}_factor"] = lr.get_factor(t % N)
+            out[f"{name}_s{t}_sigma"] = lr.get_sigma()[0]
+        out[f"{name}_fit1"] = opt.compute_exact_fit()
+        out[f"{name}_idx"], out[f"{name}_vals"] = idx, vals
+        out[f"{name}_dims"] = np.asarray(dims, dtype=np.int64)
+        for k, U in enumerate(factors):
+            out[f"{name}_U{k}"] = U
+    np.savez_compressed(os.path.join(HERE, "exact.npz"), **out)
+
+
+def stats_schema():
+    """The statistics JSON of ALS_Optimizer::execute_ALS_rounds
+    (als_optimizer.hpp:40-124, compute_dstat common.h:613-675) at one rank:
+    two rounds on a small tensor, fit every round.  Timings vary run to run;
+    the tests compare keys, nesting and the non-timing values."""
+    dims, idx, vals = synthetic.random_sparse((30, 25, 20), 2000, seed=61)
+    factors = synthetic.gaussian_factors(dims, 4, seed=62)
+    for sampler in ("sts_cp", "cp_arls_lev"):
+        keep, st, lr, s, opt = make_problem(dims, idx, vals, 4, factors, sampler, (71, 72))
+        opt.execute_ALS_rounds(2, 500, 1)
+        text = opt.get_statistics_json()
+        with open(os.path.join(HERE, f"stats_{sampler}.json"), "w") as f:
+            f.write(text + "\n")
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["units", "steps", "workload1"]
+    which = sys.argv[1:] or ["units", "steps", "workload1", "keys128", "sweeps20", "sweeps20_dense", "exact",
+                             "stats_schema"]
     for w in which:
         globals()[w]()
         print("wrote", w)
