@@ -6,7 +6,8 @@
 
 Inputs: the reference's named tensors (HDF5 files, need h5py), ``random``
 (the reference's block tensor), or ``synthetic:<planted|zipf4|zipf4_small|zipf5>``.
-Extra flags: --seed, --precision {fp64,tf32,bf16}.  One process, one GPU.
+Extra flags: --seed, --precision {fp64,tf32,bf16}, --factor-file PATH (write the
+factors at the end), --init-factors PATH (resume from them).  One process, one GPU.
 """
 import argparse
 import json
@@ -40,6 +41,8 @@ def decompose(args, output_filename, trial_num):
 
     low_rank_tensor = LowRankTensor(args.trank, sparse_tensor.tensor_grid)
     low_rank_tensor.initialize_factors_gaussian_random(seed=args.seed)
+    if args.init_factors is not None:  # resume from FACTOR_MODE_i written by --factor-file
+        low_rank_tensor.read_from_file(args.init_factors)
 
     sample_count = 0
     kw = dict(precision=args.precision, seed=args.seed)
@@ -102,6 +105,8 @@ def decompose(args, output_filename, trial_num):
     }
     print(json.dumps(output_dict, indent=4))
     print(f"Final Fit: {final_fit}")
+    if args.factor_file is not None:
+        print(f"Factors written to {low_rank_tensor.write_to_file(args.factor_file)}")
     if output_filename is not None:
         with open(os.path.join(args.output_folder, output_filename), "w") as f:
             f.write(json.dumps(output_dict, indent=4))
@@ -129,6 +134,10 @@ def parse_args(argv=None):
                         required=False, type=str)
     parser.add_argument("--seed", type=int, default=0, help="seed of the factor init and the sampling stream")
     parser.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16"])
+    parser.add_argument("--factor-file", dest="factor_file", default=None,
+                        help="write the factors (FACTOR_MODE_i, SIGMA) here at the end (HDF5 with h5py, else .npz)")
+    parser.add_argument("--init-factors", dest="init_factors", default=None,
+                        help="start from the factors of a --factor-file (resume)")
     return parser.parse_args(argv)
 
 

@@ -100,7 +100,11 @@ size_t exafac_dense_workspace_bytes(int32_t R);
  * reference.  Scratch is a static 128 KiB device array shared by all calls
  * on a device: R must be <= 128; calls that overlap on the GPU race on it.
  * The first call on each device looks up the array's address
- * (cudaGetSymbolAddress), so make it before any stream capture. */
+ * (cudaGetSymbolAddress), so make it before any stream capture.  The address
+ * is kept for the life of the process: after a device reset
+ * (cudaDeviceReset, or a reset of the primary context) the module is loaded
+ * again and the kept address is stale, so do not call this entry point on a
+ * device that has been reset since its first call. */
 int exafac_pinv_square_static(int32_t R, const double* A_dev, double* out_dev, double tol, void* stream);
 
 /* ---------------------------------------------------------------------------
@@ -189,6 +193,19 @@ int exafac_als_exact_step(exafac_als_t s, int32_t mode, void* stream);
 /* ALS_Optimizer::compute_exact_fit -> SparseTensor::compute_exact_fit
  * (sparse_tensor.hpp:288-356).  Synchronises; *fit is a host double. */
 int exafac_als_fit(exafac_als_t s, double* fit, void* stream);
+
+/* Fit estimate with zero sampling (the reference's legacy
+ * DistLowRank.compute_estimated_fit, exafac/low_rank_tensor.py:110-184):
+ * 1 - sqrt(sum over nonzeros of (x - m)^2 + (prod dims - nnz) * mean of m^2
+ * over the zero samples kept) / ||X||, m the model value.  Z coordinates are
+ * drawn uniformly over the index space (zero_idx_dev, Z x N uint32, or NULL
+ * for Philox4x32-10 keyed by seed); those that are nonzeros of the tensor are
+ * dropped, found exactly through the session's mode-0 fibre hash table (the
+ * reference used a Bloom filter, bloom_filter.cpp:198-252).  The reference
+ * takes Z = (1 / alpha - 1) nnz with alpha = 0.5.  Writes *fit and the number
+ * of zero samples kept (*kept, may be NULL); synchronises. */
+int exafac_als_estimated_fit(exafac_als_t s, int64_t Z, const uint32_t* zero_idx_dev, uint64_t seed, double* fit,
+                             int64_t* kept, void* stream);
 
 /* Seeds the session's Philox stream used when uniforms_dev is NULL. */
 int exafac_als_set_seed(exafac_als_t s, uint64_t seed);

@@ -473,3 +473,25 @@ def exact_als_sweep(ora: "OracleALS", sweeps: int = 1):
             grams[n] = gram(U)
     for n in range(N):
         ora.update_sampler(n)
+
+
+def estimated_fit(ora: "OracleALS", zero_coords: np.ndarray):
+    """DistLowRank.compute_estimated_fit (exafac/low_rank_tensor.py:110-184)
+    with the zero samples given and an exact membership test: the squared
+    error over every nonzero plus the mean squared model value over the zero
+    samples that are not nonzeros, scaled by (prod dims - nnz).  Returns
+    (estimated fit, zero samples kept)."""
+    def model(coords):
+        p = np.tile(ora.sigma, (len(coords), 1))
+        for k, U in enumerate(ora.factors):
+            p = p * U[coords[:, k].astype(np.int64)]
+        return p.sum(axis=1)
+
+    nonzero_loss = float(np.sum((ora.val - model(ora.idx)) ** 2))
+    present = {tuple(int(x) for x in row) for row in ora.idx}
+    keep = np.array([tuple(int(x) for x in row) not in present for row in zero_coords], dtype=bool)
+    z = model(np.asarray(zero_coords)[keep])
+    kept = int(keep.sum())
+    dense = float(np.prod(np.array(ora.dims, dtype=np.float64)))
+    zero_loss = float(np.sum(z * z)) * (dense - ora.idx.shape[0]) / kept if kept else 0.0
+    return 1.0 - math.sqrt(nonzero_loss + zero_loss) / ora.tensor_norm, kept

@@ -68,6 +68,8 @@ SIGNATURES = {
     "exafac_als_sweeps": (ctypes.c_int, [_P, _I64, _I32, _P, _P]),
     "exafac_als_sampled_mttkrp": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P]),
     "exafac_als_fit": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
+    "exafac_als_estimated_fit": (ctypes.c_int, [_P, _I64, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(_I64), _P]),
     "exafac_als_set_seed": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "exafac_als_enable_timing": (ctypes.c_int, [_P, _I32]),
     "exafac_als_region_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),

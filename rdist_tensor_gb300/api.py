@@ -132,6 +132,28 @@ class LowRankTensor:
         else:
             self.sigma.fill_(1.0)
 
+    def write_to_file(self, filename: str, fmt: str | None = None) -> str:
+        """LowRankTensor.write_to_file (exafac/low_rank_tensor.py:186-192):
+        FACTOR_MODE_i datasets (HDF5 when h5py is importable, else .npz),
+        plus SIGMA.  Returns the path written."""
+        from . import checkpoint
+
+        return checkpoint.write_factors(filename, [f.data.cpu().numpy() for f in self.factors],
+                                        self.sigma.cpu().numpy(), fmt)
+
+    def read_from_file(self, filename: str):
+        """Loads factors (and sigma, when the file holds it) written by
+        write_to_file, to resume a decomposition."""
+        from . import checkpoint
+
+        mats, sigma = checkpoint.read_factors(filename)
+        if len(mats) != len(self.factors):
+            raise ValueError(f"{filename} holds {len(mats)} factors, the tensor has {len(self.factors)} modes")
+        for f, m in zip(self.factors, mats):
+            if tuple(m.shape) != tuple(f.data.shape):
+                raise ValueError(f"factor shape {m.shape} does not match {tuple(f.data.shape)}")
+        self.set_factors(mats, sigma)
+
     def test_gram_matrix_computation(self):
         """low_rank_tensor.hpp:44-54: prints the Grams of the deterministic factors."""
         for i, f in enumerate(self.factors):
@@ -232,13 +254,18 @@ class ALS_Optimizer:
     """Round loop, fit and statistics (als_optimizer.hpp:10-218)."""
 
     def __init__(self, ground_truth: SparseTensor, low_rank_tensor: LowRankTensor, sampler: Sampler | None,
-                 max_samples: int = 1 << 19, precision: str = "fp64", seed: int = 0x5eed):
+                 max_samples: int = 1 << 19, precision: str = "fp64", seed: int = 0x5eed,
+                 workspace_fill: int | None = None):
+        """workspace_fill: a byte value written over the session's device
+        workspace before it is used (a test aid: results must not depend on
+        what the workspace held; 0xFF makes every float and double a NaN)."""
         self.ground_truth = ground_truth
         self.low_rank_tensor = low_rank_tensor
         self.sampler = sampler
         self.max_samples = int(max_samples)
         self.precision = precision
         self.seed = int(seed)
+        self.workspace_fill = workspace_fill
         self.stats = {}
         self._h = None
         self._ws = None
@@ -281,6 +308,9 @@ class ALS_Optimizer:
         dev = _device()
         self._ws = torch.empty(pers.value, dtype=torch.uint8, device=dev)
         setup_ws = torch.empty(setup.value, dtype=torch.uint8, device=dev)
+        if self.workspace_fill is not None:
+            self._ws.fill_(int(self.workspace_fill))
+            setup_ws.fill_(int(self.workspace_fill))
         h = ctypes.c_void_p()
         _lib.call("exafac_als_create", ctypes.byref(cfg), _ptr(self._ws), ctypes.c_size_t(pers.value),
                   ctypes.byref(h))
@@ -323,6 +353,34 @@ class ALS_Optimizer:
         out = ctypes.c_double()
         _lib.call("exafac_als_fit", self._h, ctypes.byref(out), _stream())
         return out.value
+
+    def compute_estimated_fit(self, alpha: float = 0.5, seed: int = 0, zero_coords=None):
+        """The reference's legacy zero-sampling fit estimate
+        (exafac/low_rank_tensor.py:110-184): the error over every nonzero plus
+        (1 / alpha - 1) nnz uniform zero samples (coordinates that are
+        nonzeros are found exactly and dropped).  zero_coords: optional
+        Z x N coordinates to use instead of the Philox draws.  Returns
+        (estimated fit, zero samples kept)."""
+        self._require()
+        fit, kept = ctypes.c_double(), ctypes.c_int64()
+        if zero_coords is not None:
+            z = torch.as_tensor(np.asarray(zero_coords, dtype=np.int64) if not torch.is_tensor(zero_coords)
+                                else zero_coords)
+            if z.dim() != 2 or z.shape[1] != self.ground_truth.dim:
+                raise ValueError("zero_coords must be Z x N")
+            dims = torch.as_tensor(self.ground_truth.tensor_grid.tensor_dims, dtype=torch.int64)
+            if z.numel() and (z.min() < 0 or bool((z.max(dim=0).values >= dims.to(z.device)).any())):
+                raise ValueError("zero coordinate out of range")
+            z64 = z.to(device=_device(), dtype=torch.int64)
+            zd = torch.where(z64 >= 2 ** 31, z64 - 2 ** 32, z64).to(torch.int32).contiguous()
+            Z = int(zd.shape[0])
+            ptr = _ptr(zd)
+        else:
+            Z = max(1, int(round((1.0 / float(alpha) - 1.0) * self.ground_truth.nnz)))
+            ptr = None
+        _lib.call("exafac_als_estimated_fit", self._h, Z, ptr, ctypes.c_uint64(int(seed)), ctypes.byref(fit),
+                  ctypes.byref(kept), _stream())
+        return fit.value, kept.value
 
     def execute_ALS_step(self, mode: int, J: int, uniforms: torch.Tensor | None = None,
                          perms: torch.Tensor | None = None):

@@ -548,11 +548,110 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
     pinv_small_block(R, ngram, out, tol, vt_scratch, 2);
 }
 
+// Larger ranks (R > 92, where three full R x R matrices pass the shared
+// memory cap): the same Cholesky inverse with L and L^{-1} held as packed
+// lower triangles ((i, j), j <= i, at i (i + 1) / 2 + j; two times 66 KB at
+// R = 128), the same acceptance test and Jacobi fallback; the Newton step,
+// when asked for, runs in global scratch (2 R^2 doubles of vt_scratch: the
+// sessions' scratch holds (N + 1) R^2).
+__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+__device__ void newton_refine_global(int R, const double* __restrict__ A, double* __restrict__ out,
+                                     double* __restrict__ scratch) {
+    double* X = scratch;
+    double* T = scratch + (size_t)R * R;
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) X[e] = out[e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {  // T = A X
+        const int i = e / R, j = e % R;
+        double acc = 0.0;
+        for (int k = 0; k < R; k++) acc = fma(i <= k ? A[i * R + k] : A[k * R + i], X[k * R + j], acc);
+        T[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {  // out = 2X - X T
+        const int i = e / R, j = e % R;
+        double acc = 0.0;
+        for (int k = 0; k < R; k++) acc = fma(X[i * R + k], T[k * R + j], acc);
+        out[e] = 2.0 * X[e] - acc;
+    }
+    __syncthreads();
+}
+
+__global__ void spd_pinv_packed_kernel(int R, const double* __restrict__ A, double* __restrict__ out, double tol,
+                                       double* vt_scratch, int refine) {
+    extern __shared__ double smem[];
+    __shared__ int fail;
+    __shared__ double fro_w[32];  // per-warp parts, summed in warp order
+    const int P = R * (R + 1) / 2;
+    double* L = smem;
+    double* Li = smem + P;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < R; i += nt)
+        for (int j = 0; j <= i; j++) {
+            L[tri(i, j)] = A[j * R + i];  // upper triangle of A
+            Li[tri(i, j)] = 0.0;
+        }
+    if (tid == 0) fail = 0;
+    __syncthreads();
+    for (int k = 0; k < R; k++) {
+        if (tid == 0) {
+            const double d = L[tri(k, k)];
+            if (!(d > 0.0) || !isfinite(d)) fail = 1;
+            else L[tri(k, k)] = sqrt(d);
+        }
+        __syncthreads();
+        if (fail) break;
+        const double lkk = L[tri(k, k)];
+        for (int i = k + 1 + tid; i < R; i += nt) L[tri(i, k)] /= lkk;
+        __syncthreads();
+        const int m = R - k - 1;
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = k + 1 + e / m, j = k + 1 + e % m;
+            if (j <= i) L[tri(i, j)] -= L[tri(i, k)] * L[tri(j, k)];
+        }
+        __syncthreads();
+    }
+    if (!fail) {
+        for (int c = tid; c < R; c += nt) {
+            for (int i = c; i < R; i++) {
+                double sacc = (i == c) ? 1.0 : 0.0;
+                for (int t = c; t < i; t++) sacc -= L[tri(i, t)] * Li[tri(t, c)];
+                Li[tri(i, c)] = sacc / L[tri(i, i)];
+            }
+        }
+        __syncthreads();
+        double part = 0.0;
+        for (int e = tid; e < R * R; e += nt) {
+            const int a = e / R, b = e % R;
+            const int k0 = a > b ? a : b;
+            double acc = 0.0;
+            for (int k = k0; k < R; k++) acc = fma(Li[tri(k, a)], Li[tri(k, b)], acc);
+            out[e] = acc;
+            part += acc * acc;
+        }
+        part = warp_sum(part);
+        if ((tid & 31) == 0) fro_w[tid >> 5] = part;
+        __syncthreads();
+        double fro = 0.0;
+        for (int q = 0; q < (nt + 31) / 32; q++) fro += fro_w[q];
+        const double bound = 1.0 / sqrt(fro);
+        if (isfinite(fro) && bound > 10.0 * tol) {  // the same in every thread
+            if (refine) newton_refine_global(R, A, out, vt_scratch);
+            return;
+        }
+        __syncthreads();
+    }
+    syev_block(R, A, nullptr, nullptr, out, tol, vt_scratch, smem);
+    if (refine) newton_refine_global(R, A, out, vt_scratch);
+}
+
 // Shared memory of the Cholesky path (L, L^{-1}, and the Newton step's
-// third matrix).  The Cholesky path is used when its buffers fit under
-// kPinvSmemCap (R <= 92); larger ranks go straight to Jacobi, unrefined
-// (refinement is only requested by the mixed forms, which need R <= 32).
+// third matrix).  The Cholesky path in full matrices is used when its buffers
+// fit under kPinvSmemCap (R <= 92); larger ranks take the packed kernel.
 static size_t chol_smem_bytes(int R) { return sizeof(double) * 3 * (size_t)R * R; }
+static size_t chol_packed_smem_bytes(int R) { return sizeof(double) * 2 * (size_t)(R * (R + 1) / 2); }
 constexpr size_t kPinvSmemCap = 200 * 1024;
 
 size_t pinv_smem_bytes(int R) {
@@ -571,6 +670,15 @@ static int launch_pinv_impl(int R, const double* A, double* out, double tol, dou
         return EXAFAC_OK;
     }
     const int fast = chol_smem_bytes(R) <= kPinvSmemCap;
+    if (!fast) {
+        const size_t smem = std::max(chol_packed_smem_bytes(R), syev_smem_bytes(R));
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(spd_pinv_packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        spd_pinv_packed_kernel<<<1, 512, smem, stream>>>(R, A, out, tol, vt_scratch, refine);
+        count_launch();
+        EXAFAC_CHECK_LAUNCH();
+        return EXAFAC_OK;
+    }
     size_t smem = pinv_smem_bytes(R);
     if (smem > 48 * 1024)
         EXAFAC_CUDA_TRY(cudaFuncSetAttribute(spd_pinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -18,7 +18,8 @@ int launch_syev(int R, const double* A, int64_t a_stride, int batch, double* V, 
 int launch_pinv(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
 
 // The same followed by one Newton step X <- 2X - X A X (the refinement the
-// mixed forms apply to the solve).
+// mixed forms apply to the solve).  For R > 92 the step runs in vt_scratch,
+// which must then hold 2 R^2 doubles.
 int launch_pinv_refined(int R, const double* A, double* out, double tol, double* vt_scratch, cudaStream_t stream);
 // The leverage-score pseudo-inverse of the mixed forms (unit-diagonal Gram):
 // the sweep in FP32 when its error bound allows, else the FP64 path.

@@ -170,6 +170,9 @@ int sts_compute_M(Session& s, int n, cudaStream_t st);
 int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
 // FP32 copies of factor k and its row tree (mixed STS-CP sessions; else a no-op).
 int sts_refresh_f32(Session& s, int k, cudaStream_t st);
+// Row tree of mode k after a sampled update: FP64 build (FP64 form), or the
+// FP32-copy build with FP64 internal sums and the FP32 copies (mixed forms).
+int sts_rebuild_tree(Session& s, int k, cudaStream_t st);
 
 // ---- step kernels (step_kernels.cu)
 int dedup(Session& s, int n, int64_t J, cudaStream_t st);
@@ -212,6 +215,9 @@ int normalize_factor(Session& s, int n, bool all_rows, cudaStream_t st);
 int clear_dense_factor(Session& s, int n, cudaStream_t st);
 int zero_old_rows(Session& s, int n, cudaStream_t st);
 int fit_residual(Session& s, double* out_dev, cudaStream_t st);
+// Zero-sampling fit estimate (estfit.cu); synchronises.
+int estimated_fit(Session& s, int64_t Z, const uint32_t* zero_idx, uint64_t seed, double* fit, int64_t* kept,
+                  cudaStream_t st);
 int exact_mttkrp(Session& s, int n, double* M, cudaStream_t st);
 int matmul_rows_sym(Session& s, const double* M, const double* Phi, double* U, int64_t rows, cudaStream_t st);
 int chain_gram(Session& s, int skip, double* out, cudaStream_t st);

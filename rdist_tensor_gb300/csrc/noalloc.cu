@@ -18,7 +18,10 @@
 // name denotes a host-side stand-in, not a device address.  The first call on
 // each device looks up the device address with cudaGetSymbolAddress (with
 // that device current) and caches it; make that first call before any stream
-// capture starts.
+// capture starts.  The cache lasts as long as the process: a device reset
+// (cudaDeviceReset, or a reset of the primary context) reloads the module at
+// another address, so the entry point must not be used on a device reset
+// after its first call there.
 #include <mutex>
 
 #include "dense.cuh"

@@ -298,6 +298,28 @@ static int narrow_copy(const double* in, float* out, int64_t n, cudaStream_t st)
     return EXAFAC_OK;
 }
 
+// FP32 copies of packed nodes (P doubles each) at the padded FP32 node stride
+// Pf, the padding zeroed.
+__global__ void narrow_nodes_kernel(const double* __restrict__ in, int P, float* __restrict__ out, int Pf,
+                                    int64_t nodes) {
+    const int64_t total = nodes * Pf;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = i / Pf;
+        const int e = (int)(i - c * Pf);
+        out[i] = e < P ? narrow_f64(in[c * P + e]) : 0.0f;
+    }
+}
+
+static int narrow_nodes(const double* in, float* out, int R, int64_t nodes, cudaStream_t st) {
+    const int P = packed_size(R), Pf = packed_stride_f32(R);
+    if (nodes <= 0) return EXAFAC_OK;
+    narrow_nodes_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nodes * Pf, 256), 152 * 16), 256, 0, st>>>(in, P, out,
+                                                                                                         Pf, nodes);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
 // STS_CP::computeM part 1 (sts_cp.hpp:81-102): suffix Hadamard products of
 // the factor Grams over the modes != n; chain[n] is cleared.
 __global__ void sts_chain_kernel(int N, int n, int R, const double* __restrict__ gram, double* __restrict__ chain) {
@@ -362,52 +384,94 @@ __global__ void sts_emat_kernel(int N, int n, int R, const double* __restrict__ 
 
 // Eigen tree of each sampled mode k (sts_cp.hpp:179-187): PartitionTree over
 // the rows of E[next(k)] with one row per leaf, then every node times the
-// Gram of U_k.  One CTA per mode.
-__global__ void sts_eigen_tree_kernel(int N, int n, int R, TreeShape t, const double* __restrict__ E,
-                                      const double* __restrict__ gram, double* __restrict__ eigG) {
-    const int k = blockIdx.x;
-    if (k == n || k >= N) return;
+// Gram of U_k; the same operations in the same order as the reference (leaf
+// outer products, pairwise sums bottom-up, then the Hadamard product), spread
+// over the GPU: one launch for the leaves of every sampled mode, one per
+// level for the sums, one for the products.
+
+// Row a of packed index e (R x R upper triangle, rows in order).
+__device__ __forceinline__ int packed_row(int R, int e) {
+    const double b = 2.0 * R + 1.0;
+    int a = (int)((b - sqrt(b * b - 8.0 * e)) * 0.5);
+    if (a < 0) a = 0;
+    if (a > R - 1) a = R - 1;
+    while (a > 0 && packed_index(R, a, a) > e) a--;
+    while (a + 1 < R && packed_index(R, a + 1, a + 1) <= e) a++;
+    return a;
+}
+
+__device__ __forceinline__ int eigen_next(int N, int n, int k) {
     int nxt = k + 1;
     if (nxt == n) nxt++;
-    if (nxt > N) nxt = N;
+    return nxt > N ? N : nxt;
+}
+
+__global__ void eigen_leaves_kernel(int N, int n, int R, TreeShape t, const double* __restrict__ E,
+                                    double* __restrict__ eigG) {
     const int P = packed_size(R);
-    const double* Ek = E + (int64_t)nxt * R * R;
-    double* G = eigG + (int64_t)k * t.node_count * P;
     const int64_t first_leaf = t.node_count - t.leaf_count;
-    for (int64_t i = threadIdx.x; i < t.leaf_count * P; i += blockDim.x) {
-        int64_t li = i / P;
-        int e = (int)(i % P);
-        int a = 0, rem = e;
-        while (rem >= R - a) {
-            rem -= R - a;
-            a++;
-        }
-        int b = a + rem;
-        int64_t v = tree_leaf_idx(t, first_leaf + li);
-        G[(first_leaf + li) * P + e] = Ek[v * R + a] * Ek[v * R + b];
+    const int64_t per_mode = t.leaf_count * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)N * per_mode;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(i / per_mode);
+        if (k == n) continue;
+        const int64_t li = (i % per_mode) / P;
+        const int e = (int)(i % P);
+        const int a = packed_row(R, e), b = a + (e - packed_index(R, a, a));
+        const double* Ek = E + (int64_t)eigen_next(N, n, k) * R * R;
+        const int64_t v = tree_leaf_idx(t, first_leaf + li);
+        eigG[((int64_t)k * t.node_count + first_leaf + li) * P + e] = Ek[v * R + a] * Ek[v * R + b];
     }
-    __syncthreads();
-    int64_t start = t.nodes_before_lfill, end = first_leaf;
+}
+
+// Internal nodes [start, end) of every sampled mode's tree: G[c] = G[2c+1] + G[2c+2].
+__global__ void eigen_level_kernel(int N, int n, int P, TreeShape t, int64_t start, int64_t end,
+                                   double* __restrict__ eigG) {
+    const int64_t per_mode = (end - start) * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)N * per_mode;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(i / per_mode);
+        if (k == n) continue;
+        const int64_t c = start + (i % per_mode) / P;
+        const int e = (int)(i % P);
+        double* G = eigG + (int64_t)k * t.node_count * P;
+        G[c * P + e] = G[(2 * c + 1) * P + e] + G[(2 * c + 2) * P + e];
+    }
+}
+
+__global__ void eigen_hadamard_kernel(int N, int n, int R, TreeShape t, const double* __restrict__ gram,
+                                      double* __restrict__ eigG) {
+    const int P = packed_size(R);
+    const int64_t per_mode = t.node_count * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)N * per_mode;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(i / per_mode);
+        if (k == n) continue;
+        const int e = (int)(i % P);
+        const int a = packed_row(R, e), b = a + (e - packed_index(R, a, a));
+        eigG[i] *= gram[(int64_t)k * R * R + a * R + b];
+    }
+}
+
+static int build_eigen_trees(Session& s, int n, cudaStream_t st) {
+    const int N = s.N, R = s.R, P = s.P;
+    const TreeShape& t = s.etree;
+    auto grid = [](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(work, 256), 152 * 16)); };
+    eigen_leaves_kernel<<<grid((int64_t)N * t.leaf_count * P), 256, 0, st>>>(N, n, R, t, s.Emat, s.eigG);
+    count_launch();
+    int64_t start = t.nodes_before_lfill, end = t.node_count - t.leaf_count;
     for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
-        for (int64_t i = threadIdx.x; i < (end - start) * P; i += blockDim.x) {
-            int64_t c = start + i / P;
-            int e = (int)(i % P);
-            G[c * P + e] = G[(2 * c + 1) * P + e] + G[(2 * c + 2) * P + e];
+        if (end > start) {
+            eigen_level_kernel<<<grid((int64_t)N * (end - start) * P), 256, 0, st>>>(N, n, P, t, start, end, s.eigG);
+            count_launch();
         }
-        __syncthreads();
         end = start;
         start = ((start + 1) / 2) - 1;
     }
-    const double* Gk = gram + (int64_t)k * R * R;
-    for (int64_t i = threadIdx.x; i < t.node_count * P; i += blockDim.x) {
-        int e = (int)(i % P);
-        int a = 0, rem = e;
-        while (rem >= R - a) {
-            rem -= R - a;
-            a++;
-        }
-        G[i] *= Gk[a * R + a + rem];
-    }
+    eigen_hadamard_kernel<<<grid((int64_t)N * t.node_count * P), 256, 0, st>>>(N, n, R, t, s.gram, s.eigG);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
 }
 
 int sts_compute_M(Session& s, int n, cudaStream_t st) {
@@ -427,12 +491,11 @@ int sts_compute_M(Session& s, int n, cudaStream_t st) {
     }
     sts_emat_kernel<<<1, 256, 0, st>>>(N, n, R, s.eigV, s.eigL, s.Emat); count_launch();
     EXAFAC_CHECK_LAUNCH();
-    sts_eigen_tree_kernel<<<N, 256, 0, st>>>(N, n, R, s.etree, s.Emat, s.gram, s.eigG); count_launch();
-    EXAFAC_CHECK_LAUNCH();
+    EXAFAC_TRY(build_eigen_trees(s, n, st));
     if (s.cfg.precision != EXAFAC_PREC_FP64) {  // the mixed forms descend on FP32 copies
-        EXAFAC_TRY(narrow_copy(s.eigG, s.eigF, (int64_t)N * s.etree.node_count * s.P, st));
+        EXAFAC_TRY(narrow_nodes(s.eigG, s.eigF, R, (int64_t)N * s.etree.node_count, st));
         EXAFAC_TRY(narrow_copy(s.Emat, s.EmatF, (int64_t)(N + 1) * R2, st));
-        EXAFAC_TRY(narrow_copy(s.PhiP, s.PhiPF, s.P, st));
+        EXAFAC_TRY(narrow_nodes(s.PhiP, s.PhiPF, R, 1, st));
     }
     return EXAFAC_OK;
 }
@@ -460,7 +523,7 @@ __global__ void sts_draw_kernel(int N, int n, int R, int G, int S, int64_t J, St
                                 const double* __restrict__ uni, uint32_t* __restrict__ samples,
                                 double* __restrict__ weights, DeviceStatus* status) {
     extern __shared__ __align__(16) unsigned char stsdyn[];
-    const int P = packed_size(R);
+    const int P = node_stride<T>(R);  // node stride of the trees and of PhiP
     T *h, *sh, *q;
     int gi;
     const SampleGroup<T> grp = sample_group<T>(stsdyn, R, G, h, sh, q, gi);
@@ -509,7 +572,14 @@ __global__ void sts_draw_kernel(int N, int n, int R, int G, int S, int64_t J, St
 int sts_refresh_f32(Session& s, int k, cudaStream_t st) {
     if (s.cfg.sampler != EXAFAC_SAMPLER_STS_CP || s.cfg.precision == EXAFAC_PREC_FP64) return EXAFAC_OK;
     EXAFAC_TRY(narrow_copy(s.F.U[k], s.Uf[k], s.dims[k] * s.R, st));
-    return narrow_copy(s.treeG[k], s.treeF[k], s.rtree[k].node_count * s.P, st);
+    return narrow_nodes(s.treeG[k], s.treeF[k], s.R, s.rtree[k].node_count, st);
+}
+
+int sts_rebuild_tree(Session& s, int k, cudaStream_t st) {
+    if (s.cfg.precision == EXAFAC_PREC_FP64) return launch_tree_build(s.rtree[k], s.R, s.F.U[k], s.treeG[k], st);
+    EXAFAC_TRY(narrow_copy(s.F.U[k], s.Uf[k], s.dims[k] * s.R, st));
+    EXAFAC_TRY(launch_tree_build_f32(s.rtree[k], s.R, s.Uf[k], s.treeG[k], st));
+    return narrow_nodes(s.treeG[k], s.treeF[k], s.R, s.rtree[k].node_count, st);
 }
 
 template <typename T>

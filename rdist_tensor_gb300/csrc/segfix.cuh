@@ -51,10 +51,17 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
                 if (bal != full) break;
             }
         }
+        // Columns R .. ldm - 1 of a padded FP32 row are written as zeros: the
+        // solve reads whole rows, and the row's memory holds whatever the
+        // workspace held before (a NaN there would survive the product with
+        // Phi's zero padding).
         if (c1 - c0 <= 32) {  // short span: column per lane, chunks in order
             for (int cb = 0; cb < CB; cb++) {
                 const int col = 32 * cb + lane;
-                if (col >= R) continue;
+                if (col >= R) {
+                    if (col < ldm) Mc[out * ldm + col] = TA(0);
+                    continue;
+                }
                 TA v = carry_last[c0 * (32 * CB) + col];
 #pragma unroll 4
                 for (int64_t m = c0 + 1; m <= c1; m++) v += carry_first[m * (32 * CB) + col];
@@ -83,6 +90,7 @@ __global__ void __launch_bounds__(256) segfix_kernel(int R, int ldm, const int64
             }
             const int col = 32 * cb + lane;
             if (col < R) Mc[out * ldm + col] = carry_last[c0 * (32 * CB) + col] + acc[0];
+            else if (col < ldm) Mc[out * ldm + col] = TA(0);
         }
     }
 }

@@ -57,13 +57,14 @@ static void carve(Session& s) {
         for (int k = 0; k < N; k++) s.treeG[k] = a.take<double>(s.rtree[k].node_count * P);
         s.eigG = a.take<double>((int64_t)N * s.etree.node_count * P);
         if (s.cfg.precision != EXAFAC_PREC_FP64) {
+            const int Pf = packed_stride_f32(R);
             for (int k = 0; k < N; k++) {
-                s.treeF[k] = a.take<float>(s.rtree[k].node_count * P);
+                s.treeF[k] = a.take<float>(s.rtree[k].node_count * Pf);
                 s.Uf[k] = a.take<float>(s.dims[k] * R);
             }
-            s.eigF = a.take<float>((int64_t)N * s.etree.node_count * P);
+            s.eigF = a.take<float>((int64_t)N * s.etree.node_count * Pf);
             s.EmatF = a.take<float>((int64_t)(N + 1) * R2);
-            s.PhiPF = a.take<float>(P);
+            s.PhiPF = a.take<float>(Pf);
         }
     }
     s.cdf_total = a.take<double>(N);
@@ -101,7 +102,7 @@ static void carve(Session& s) {
     s.ugram = a.take<double>(R2);
     s.ngram = a.take<double>(R2);
     s.upinv = a.take<double>(R2);
-    s.fitpart = a.take<double>(152 * 8);
+    s.fitpart = a.take<double>(2 * 152 * 8);
     s.status = a.take<DeviceStatus>(1);
     s.scan_sc = a.take<char>((int64_t)scan_scratch_bytes(std::max(std::max(J, I), nnz)));
     s.dims_dev = a.take<int64_t>(kMaxModes);
@@ -521,10 +522,7 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     EXAFAC_CUDA_TRY(cudaMemcpyAsync(s.gram + (int64_t)n * s.R * s.R, s.ngram, sizeof(double) * s.R * s.R,
                                     cudaMemcpyDeviceToDevice, st));
     if (arls) EXAFAC_TRY(arls_build_cdf(s, n, s.touched, s.counters + 2, st));
-    else {
-        EXAFAC_TRY(launch_tree_build(s.rtree[n], s.R, s.F.U[n], s.treeG[n], st));
-        EXAFAC_TRY(sts_refresh_f32(s, n, st));
-    }
+    else EXAFAC_TRY(sts_rebuild_tree(s, n, st));
     EXAFAC_TRY(keep_touched(s, n, st));
     s.dense[n] = false;
     EXAFAC_TRY(mark(h, 5, st));
@@ -675,6 +673,15 @@ extern "C" int exafac_als_set_wait_limit(exafac_als_t h, uint32_t polls, int64_t
         h->sweep_exec = nullptr;
     }
     return EXAFAC_OK;
+}
+
+extern "C" int exafac_als_estimated_fit(exafac_als_t h, int64_t Z, const uint32_t* zero_idx, uint64_t seed,
+                                        double* fit, int64_t* kept, void* stream) {
+    EXAFAC_ARG(h && h->s.initialized, "session not initialised");
+    Session& s = h->s;
+    cudaStream_t st = (cudaStream_t)stream;
+    EXAFAC_TRY(estimated_fit(s, Z, zero_idx, seed, fit, kept, st));
+    return check_status(s, st);
 }
 
 extern "C" int exafac_als_step_info(exafac_als_t h, exafac_step_info* out, void* stream) {

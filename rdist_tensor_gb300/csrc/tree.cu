@@ -35,6 +35,43 @@ __global__ void tree_leaf_gram_kernel(TreeShape t, int R, const double* __restri
     }
 }
 
+// Leaf Grams of the mixed forms, from the FP32 copy of the factor: a block
+// per leaf (its rows staged in shared memory), a thread per packed entry
+// (a, b).  Each product u_a u_b is split exactly into its FP32 rounding p and
+// error fma(u_a, u_b, -p), and both are added into a compensated (hi, lo)
+// FP32 sum (Knuth's two-sum), so the leaf sum carries about 48 bits on the
+// FP32 pipe; it is widened to FP64 for the tree, whose internal sums are
+// FP64.
+__global__ void tree_leaf_gram_f32_kernel(TreeShape t, int R, const float* __restrict__ U, double* __restrict__ G) {
+    extern __shared__ __align__(16) float lsm[];  // F x R
+    const int P = packed_size(R);
+    const int64_t first_leaf = t.node_count - t.leaf_count;
+    for (int64_t li = blockIdx.x; li < t.leaf_count; li += gridDim.x) {
+        const int64_t c = first_leaf + li;
+        const int64_t leaf = tree_leaf_idx(t, c);
+        const int64_t rows = (t.n - leaf * t.F) < t.F ? (t.n - leaf * t.F) : t.F;
+        __syncthreads();
+        for (int64_t e = threadIdx.x; e < rows * R; e += blockDim.x) lsm[e] = U[leaf * t.F * R + e];
+        __syncthreads();
+        double* g = G + c * P;
+        for (int a = 0, base = 0; a < R; base += R - a, a++) {
+            for (int b = a + threadIdx.x; b < R; b += blockDim.x) {
+                float hi = 0.0f, lo = 0.0f;
+                for (int64_t r = 0; r < rows; r++) {
+                    const float x = lsm[r * R + a], y = lsm[r * R + b];
+                    const float p = x * y;
+                    const float err = __fmaf_rn(x, y, -p);
+                    const float sum = hi + p;
+                    const float bp = sum - hi;
+                    lo += (hi - (sum - bp)) + (p - bp) + err;
+                    hi = sum;
+                }
+                g[base + (b - a)] = (double)hi + (double)lo;
+            }
+        }
+    }
+}
+
 // One level of internal nodes: G[c] = G[2c+1] + G[2c+2] (the reference adds
 // both children to a zeroed node: 0 + (l + r) == l + r).
 __global__ void tree_level_kernel(int64_t start, int64_t end, int P, double* __restrict__ G) {
@@ -105,6 +142,29 @@ int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cud
     for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
         if (end > start) {
             tree_level_kernel<<<grid_for((end - start) * P, 256), 256, 0, stream>>>(start, end, P, G); count_launch();
+            EXAFAC_CHECK_LAUNCH();
+        }
+        end = start;
+        start = ((start + 1) / 2) - 1;
+    }
+    return EXAFAC_OK;
+}
+
+int launch_tree_build_f32(const TreeShape& t, int R, const float* U, double* G, cudaStream_t stream) {
+    const int P = packed_size(R);
+    const size_t smem = sizeof(float) * t.F * R;
+    if (smem > 48 * 1024)
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(tree_leaf_gram_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int blocks = (int)std::min<int64_t>(t.leaf_count, 152 * 4);
+    tree_leaf_gram_f32_kernel<<<blocks, 128, smem, stream>>>(t, R, U, G);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    int64_t start = t.nodes_before_lfill, end = t.node_count - t.leaf_count;
+    for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
+        if (end > start) {
+            tree_level_kernel<<<grid_for((end - start) * P, 256), 256, 0, stream>>>(start, end, P, G);
+            count_launch();
             EXAFAC_CHECK_LAUNCH();
         }
         end = start;

@@ -40,10 +40,17 @@ __host__ __device__ __forceinline__ int64_t tree_leaf_idx(const TreeShape& t, in
 }
 __host__ __device__ __forceinline__ bool tree_is_leaf(const TreeShape& t, int64_t c) { return 2 * c + 1 >= t.node_count; }
 __host__ __device__ __forceinline__ int packed_size(int R) { return R * (R + 1) / 2; }
+// Node stride of the FP32 tree copies the mixed forms descend on: the packed
+// size rounded up to a multiple of 4 floats (zero padded), so that every node
+// starts on a 16-byte boundary and is read with 16-byte loads.
+__host__ __device__ __forceinline__ int packed_stride_f32(int R) { return (packed_size(R) + 3) & ~3; }
 __host__ __device__ __forceinline__ int packed_index(int R, int a, int b) { return a * R - a * (a - 1) / 2 + (b - a); }
 
 // Builds the tree over U (n x R, row-major).  G: node_count * P doubles.
 int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cudaStream_t stream);
+// The same from an FP32 copy of U: leaf Grams as compensated FP32 sums of
+// exactly split products (about 48 bits), internal sums in FP64.
+int launch_tree_build_f32(const TreeShape& t, int R, const float* U, double* G, cudaStream_t stream);
 
 // Multiplies every node elementwise by the symmetric matrix M (R x R full)
 // (multiply_matrices_against_provided, partition_tree.hpp:176-187).
@@ -81,11 +88,20 @@ __device__ __forceinline__ void block_build_pairs(int R, unsigned short* pa, uns
     }
 }
 
+// Node stride of the trees a descent in T reads: packed (the reference's
+// layout) in FP64, padded to 16 bytes in FP32.
+template <typename T>
+__host__ __device__ __forceinline__ int node_stride(int R);
+template <>
+__host__ __device__ __forceinline__ int node_stride<double>(int R) { return packed_size(R); }
+template <>
+__host__ __device__ __forceinline__ int node_stride<float>(int R) { return packed_stride_f32(R); }
+
 template <typename T>
 struct SampleGroup {
     int G;     // warps per sample
     int tg;    // thread index within the group
-    T* z;      // P
+    T* z;      // node_stride<T>(R) values (zero past P)
     T* red;    // G partial sums
     __device__ __forceinline__ int nthreads() const { return 32 * G; }
     __device__ __forceinline__ void sync() const {
@@ -115,21 +131,61 @@ struct SampleGroup {
         }
         sync();
     }
-    // x^T G x = sum_e z_e G_e for one packed node.
-    __device__ __forceinline__ T quad(int P, const T* __restrict__ g) const {
-        T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-        const int step = nthreads();
-        int e = tg;
-        for (; e + 3 * step < P; e += 4 * step) {
-            a0 = fmat(z[e], __ldg(g + e), a0);
-            a1 = fmat(z[e + step], __ldg(g + e + step), a1);
-            a2 = fmat(z[e + 2 * step], __ldg(g + e + 2 * step), a2);
-            a3 = fmat(z[e + 3 * step], __ldg(g + e + 3 * step), a3);
-        }
-        for (; e < P; e += step) a0 = fmat(z[e], __ldg(g + e), a0);
-        return sum((a0 + a1) + (a2 + a3));
-    }
+    // x^T G x = sum_e z_e G_e for one node (ps = node_stride<T>(R) values).
+    __device__ __forceinline__ T quad(int ps, const T* __restrict__ g) const;
 };
+
+// FP64: scalar loads, eight in flight per thread.
+template <>
+__device__ __forceinline__ double SampleGroup<double>::quad(int ps, const double* __restrict__ g) const {
+    double a[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) a[i] = 0.0;
+    const int step = nthreads();
+    int e = tg;
+    for (; e + 7 * step < ps; e += 8 * step) {
+        double gv[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) gv[i] = __ldg(g + e + i * step);
+#pragma unroll
+        for (int i = 0; i < 8; i++) a[i] = fmat(z[e + i * step], gv[i], a[i]);
+    }
+    for (; e < ps; e += step) a[0] = fmat(z[e], __ldg(g + e), a[0]);
+    return sum(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])));
+}
+
+// FP32: 16-byte loads of the node and of z (both padded with zeros to
+// a multiple of 4), four in flight per thread.
+template <>
+__device__ __forceinline__ float SampleGroup<float>::quad(int ps, const float* __restrict__ g) const {
+    const float4* g4 = reinterpret_cast<const float4*>(g);
+    const float4* z4 = reinterpret_cast<const float4*>(z);
+    const int n4 = ps >> 2;
+    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int step = nthreads();
+    int e = tg;
+    for (; e + 3 * step < n4; e += 4 * step) {
+        float4 gv[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) gv[i] = __ldg(g4 + e + i * step);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const float4 zv = z4[e + i * step];
+            a[i] = fmat(zv.x, gv[i].x, a[i]);
+            a[i] = fmat(zv.y, gv[i].y, a[i]);
+            a[i] = fmat(zv.z, gv[i].z, a[i]);
+            a[i] = fmat(zv.w, gv[i].w, a[i]);
+        }
+    }
+    for (; e < n4; e += step) {
+        const float4 gv = __ldg(g4 + e), zv = z4[e];
+        a[0] = fmat(zv.x, gv.x, a[0]);
+        a[0] = fmat(zv.y, gv.y, a[0]);
+        a[0] = fmat(zv.z, gv.z, a[0]);
+        a[0] = fmat(zv.w, gv.w, a[0]);
+    }
+    return sum((a[0] + a[1]) + (a[2] + a[3]));
+}
 
 // One descent of PTSample (partition_tree.hpp:204-380) by the group, with
 // the uniform d and z built from the descent vector x: root mass, one
@@ -148,7 +204,7 @@ template <typename T>
 __device__ __forceinline__ int64_t descend(const SampleGroup<T>& grp, const TreeShape& t, int R,
                                            const T* __restrict__ G, const T* __restrict__ U, const T* x, T* q, T d,
                                            bool* empty = nullptr) {
-    const int P = packed_size(R);
+    const int P = node_stride<T>(R);  // node stride of G
     int64_t c = 0;
     T low = T(0), high = T(1);
     const T m = grp.quad(P, G);
@@ -250,10 +306,12 @@ __device__ __forceinline__ int64_t descend(const SampleGroup<T>& grp, const Tree
 // F = R <= 128.
 constexpr int kMaxLeafRows = 128;
 
-// Shared memory of one sample's group: z (P), h and sh (R each), q (128),
-// red (8), in elements of esz bytes, rounded to 16 bytes.
+// Shared memory of one sample's group: z (the node stride: P in FP64, P
+// rounded up to 4 in FP32), h and sh (R each), q (128), red (8), in elements
+// of esz bytes, rounded to 16 bytes.
 __host__ __device__ inline size_t sample_group_bytes(int R, int esz) {
-    return ((size_t)esz * (packed_size(R) + 2 * R + kMaxLeafRows + 8) + 15) / 16 * 16;
+    const int ps = esz == 4 ? packed_stride_f32(R) : packed_size(R);
+    return ((size_t)esz * (ps + 2 * R + kMaxLeafRows + 8) + 15) / 16 * 16;
 }
 
 // Warps per sample (G) and samples per block (S) for rank R and element size
@@ -275,7 +333,7 @@ __device__ __forceinline__ SampleGroup<T> sample_group(unsigned char* dyn, int R
     const size_t bytes = sample_group_bytes(R, sizeof(T));
     gi = (threadIdx.x >> 5) / G;
     T* base = reinterpret_cast<T*>(dyn + gi * bytes);
-    const int P = packed_size(R);
+    const int P = node_stride<T>(R);
     h = base + P;
     sh = h + R;
     q = sh + R;
@@ -284,6 +342,8 @@ __device__ __forceinline__ SampleGroup<T> sample_group(unsigned char* dyn, int R
     grp.tg = threadIdx.x - gi * 32 * G;
     grp.z = base;
     grp.red = q + kMaxLeafRows;
+    // z past the packed entries stays zero (build_z writes entries < P only)
+    for (int e = packed_size(R) + grp.tg; e < P; e += grp.nthreads()) base[e] = T(0);
     return grp;
 }
 
