@@ -1,0 +1,435 @@
+// STS-CP draws of the mixed forms, breadth first (STS_CP::KRPDrawSamples,
+// sts_cp.hpp:203-300, and PartitionTree::PTSample, partition_tree.hpp:
+// 204-380, at one rank), in FP32 over the FP32 copies of the trees, factors,
+// eigenvector rows and Phi.
+//
+// A depth-first descent reads one R x R node per level per sample from L2 or
+// HBM (P = R (R + 1) / 2 values, 33 KB at R = 128): about 6 TB per sweep of
+// the 5-mode, R = 128, J = 2^19 workload.  Here all J samples of a tree move
+// one level at a time.  The sample slots are kept ordered by their current
+// node (a stable partition after every level, lefts before rights within a
+// parent), so a block that takes 64 consecutive slots meets a few runs of
+// equal node; it stages each run's node once in shared memory as a full
+// symmetric matrix and every warp evaluates x^T A x for its samples of the
+// run (y = A x with lanes over columns, 16-byte loads of A's rows).  A level
+// then reads each sample's R-vector once and each node once per run.  The
+// leaf stage stages the leaf's F x R rows of U (transposed) the same way and
+// picks the row by the prefix of its squared dots, in row order.
+//
+// Per level: the quadratic forms and the branch decisions (one kernel), an
+// exclusive scan of the decisions, the children's slot ranges, and the
+// scatter of the slots.  The quantities and comparisons are those of the
+// depth-first form (cutoff = low + m_L / m); the sums run in a fixed order,
+// so the draws repeat run to run.
+#include "engine.cuh"
+#include "prims.cuh"
+
+namespace exafac {
+
+constexpr int kBfsTile = 64;   // slots per block in the level and leaf kernels
+constexpr int kBfsWarps = 8;
+constexpr int kBfsBlocks = 152 * 3;
+
+__host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
+
+// MODE 0: the mass x^T G_0 x of the node G (one node) into mroot[j].
+// MODE 1: a level of the descent: the left child's mass m_L, the branch
+//         (d <= low + m_L / m goes left), node, (low, high), flag[slot].
+// MODE 2: the tail level: as MODE 1 for samples at internal nodes; samples
+//         already at a leaf stay (flag 1).
+template <int MODE>
+__global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf, const float* __restrict__ G,
+                                                                   const float* __restrict__ X, int64_t J,
+                                                                   const int32_t* __restrict__ order,
+                                                                   int64_t* __restrict__ node,
+                                                                   float2* __restrict__ lh, float* __restrict__ mroot,
+                                                                   const double* __restrict__ dv,
+                                                                   uint32_t* __restrict__ flag, TreeShape t) {
+    extern __shared__ __align__(16) float bfs_sm[];
+    const int AS = round4(R);
+    float* A = bfs_sm;        // R x AS: the run's node, full symmetric
+    float* xs = A + R * AS;   // per warp: the sample's vector
+    __shared__ int64_t cs[kBfsTile];
+    __shared__ int32_t js[kBfsTile];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* xw = xs + w * AS;
+    const int b0 = 4 * lane;
+    const int64_t ntiles = (J + kBfsTile - 1) / kBfsTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t s0 = tile * kBfsTile;
+        const int n = (int)min((int64_t)kBfsTile, J - s0);
+        __syncthreads();  // the previous tile is done with cs / js
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int32_t j = order[s0 + i];
+            js[i] = j;
+            cs[i] = MODE == 0 ? 0 : node[j];
+        }
+        __syncthreads();
+        for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
+            const int64_t c = cs[i0];
+            int i1 = i0 + 1;
+            while (i1 < n && cs[i1] == c) i1++;
+            const bool stay = MODE == 2 && tree_is_leaf(t, c);
+            if (stay) {
+                for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) flag[s0 + i] = 1u;
+                i0 = i1;
+                continue;
+            }
+            const int64_t g = MODE == 0 ? 0 : 2 * c + 1;
+            const float* Gn = G + g * Pf;
+            for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+                const int a = e / R, b = e - a * R;
+                A[a * AS + b] = __ldg(Gn + (a <= b ? packed_index(R, a, b) : packed_index(R, b, a)));
+            }
+            __syncthreads();
+            for (int i = i0 + w; i < i1; i += kBfsWarps) {
+                const int32_t j = js[i];
+                for (int r = lane; r < R; r += 32) xw[r] = X[(int64_t)j * R + r];
+                __syncwarp();
+                float part = 0.0f;
+                if (b0 < R) {
+                    float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+                    for (int a = 0; a < R; a++) {
+                        const float xa = xw[a];
+                        const float4 av = *reinterpret_cast<const float4*>(A + a * AS + b0);
+                        y.x = __fmaf_rn(av.x, xa, y.x);
+                        y.y = __fmaf_rn(av.y, xa, y.y);
+                        y.z = __fmaf_rn(av.z, xa, y.z);
+                        y.w = __fmaf_rn(av.w, xa, y.w);
+                    }
+                    part = y.x * xw[b0];  // columns past R are not added
+                    if (b0 + 1 < R) part = __fmaf_rn(y.y, xw[b0 + 1], part);
+                    if (b0 + 2 < R) part = __fmaf_rn(y.z, xw[b0 + 2], part);
+                    if (b0 + 3 < R) part = __fmaf_rn(y.w, xw[b0 + 3], part);
+                }
+                const float q = warp_sum(part);
+                if (lane == 0) {
+                    if (MODE == 0) {
+                        mroot[j] = q;
+                    } else {
+                        const float2 bnd = lh[j];
+                        const float cutoff = bnd.x + q / mroot[j];
+                        const bool left = (float)dv[j] <= cutoff;
+                        node[j] = left ? 2 * c + 1 : 2 * c + 2;
+                        lh[j] = left ? make_float2(bnd.x, cutoff) : make_float2(cutoff, bnd.y);
+                        flag[s0 + i] = left ? 1u : 0u;
+                    }
+                }
+                __syncwarp();
+            }
+            __syncthreads();  // before the next run restages A
+            i0 = i1;
+        }
+    }
+}
+
+// Slot ranges of the next level's nodes from the parents' (nl of them,
+// ranges off[0..nl]) and the exclusive scan SL of the flags (SL[J] = total):
+// the left child takes the parent's first nleft slots.
+__global__ void bfs_offsets_kernel(int64_t nl, int64_t J, const int64_t* __restrict__ off,
+                                   const int64_t* __restrict__ SL, int64_t* __restrict__ coff) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t start = off[i], end = off[i + 1];
+        coff[2 * i] = start;
+        coff[2 * i + 1] = start + (SL[end] - SL[start]);
+        if (i == 0) coff[2 * nl] = J;
+    }
+}
+
+// The stable partition: within its parent's range, a slot whose flag is set
+// (went left, or stayed at a leaf on the tail level) keeps its order among
+// those, before the others.  lb: the parents' first node index.
+__global__ void bfs_scatter_kernel(int64_t J, int64_t lb, int64_t nl, const int32_t* __restrict__ order,
+                                   const int64_t* __restrict__ node, const int64_t* __restrict__ off,
+                                   const int64_t* __restrict__ SL, const uint32_t* __restrict__ flag,
+                                   int32_t* __restrict__ order2) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < J; s += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t j = order[s];
+        const int64_t c = node[j];
+        const int64_t parent = c >= lb + nl ? (c - 1) / 2 : c;
+        const int64_t i = parent - lb;
+        const int64_t start = off[i], end = off[i + 1];
+        const int64_t before = SL[s] - SL[start];
+        const int64_t nleft = SL[end] - SL[start];
+        const int64_t pos = flag[s] ? start + before : start + nleft + ((s - start) - before);
+        order2[pos] = j;
+    }
+}
+
+// Every sample at the root: node 0, (low, high) = (0, 1); the root's range
+// is all slots.
+__global__ void bfs_reset_kernel(int64_t J, int64_t* __restrict__ node, float2* __restrict__ lh,
+                                 int32_t* __restrict__ order, int64_t* __restrict__ off, int first) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < J; s += (int64_t)gridDim.x * blockDim.x) {
+        node[s] = 0;
+        lh[s] = make_float2(0.0f, 1.0f);
+        if (first) order[s] = (int32_t)s;
+        if (s == 0) {
+            off[0] = 0;
+            off[1] = J;
+        }
+    }
+}
+
+// Leaf stage, F > 1: runs of equal leaf; the leaf's rows of U staged
+// transposed (UT[a][r], rows past the tensor zero); per sample the squared
+// dots q_r^2 = (U_r . x)^2 (lanes over rows, four each), their inclusive
+// prefix in row order, and the first row r < F - 1 with frac < prefix_r /
+// total, else the last row the leaf holds.  A leaf of zero total marks the
+// sample empty (weight 0) and takes its first row.
+__global__ void __launch_bounds__(kBfsWarps * 32) bfs_leaf_kernel(int R, TreeShape t, const float* __restrict__ U,
+                                                                  const float* __restrict__ X, int64_t J,
+                                                                  const int32_t* __restrict__ order,
+                                                                  const int64_t* __restrict__ node,
+                                                                  const float2* __restrict__ lh,
+                                                                  const double* __restrict__ dv, int N, int col,
+                                                                  uint32_t* __restrict__ samples,
+                                                                  int32_t* __restrict__ empty) {
+    extern __shared__ __align__(16) float bfs_sm[];
+    const int F = (int)t.F;
+    const int FS = round4(F) + 4;  // UT row stride
+    const int AS = round4(R);
+    float* UT = bfs_sm;          // R x FS
+    float* xs = UT + R * FS;     // per warp
+    __shared__ int64_t cs[kBfsTile];
+    __shared__ int32_t js[kBfsTile];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* xw = xs + w * AS;
+    const int r0 = 4 * lane;
+    const int64_t ntiles = (J + kBfsTile - 1) / kBfsTile;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t s0 = tile * kBfsTile;
+        const int n = (int)min((int64_t)kBfsTile, J - s0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int32_t j = order[s0 + i];
+            js[i] = j;
+            cs[i] = node[j];
+        }
+        __syncthreads();
+        for (int i0 = 0; i0 < n;) {
+            const int64_t c = cs[i0];
+            int i1 = i0 + 1;
+            while (i1 < n && cs[i1] == c) i1++;
+            const int64_t leaf = tree_leaf_idx(t, c);
+            const int rows = (int)min((int64_t)F, t.n - leaf * F);
+            const float* Ub = U + leaf * F * R;
+            for (int e = threadIdx.x; e < F * R; e += blockDim.x) {
+                const int r = e / R, a = e - r * R;
+                UT[a * FS + r] = r < rows ? __ldg(Ub + (int64_t)r * R + a) : 0.0f;
+            }
+            __syncthreads();
+            for (int i = i0 + w; i < i1; i += kBfsWarps) {
+                const int32_t j = js[i];
+                for (int r = lane; r < R; r += 32) xw[r] = X[(int64_t)j * R + r];
+                __syncwarp();
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (r0 < F) {
+#pragma unroll 4
+                    for (int a = 0; a < R; a++) {
+                        const float xa = xw[a];
+                        const float4 uv = *reinterpret_cast<const float4*>(UT + a * FS + r0);
+                        q.x = __fmaf_rn(uv.x, xa, q.x);
+                        q.y = __fmaf_rn(uv.y, xa, q.y);
+                        q.z = __fmaf_rn(uv.z, xa, q.z);
+                        q.w = __fmaf_rn(uv.w, xa, q.w);
+                    }
+                }
+                // squared dots of this lane's rows (rows past F add nothing)
+                float p0 = r0 < F ? q.x * q.x : 0.0f;
+                float p1 = r0 + 1 < F ? q.y * q.y : 0.0f;
+                float p2 = r0 + 2 < F ? q.z * q.z : 0.0f;
+                float p3 = r0 + 3 < F ? q.w * q.w : 0.0f;
+                p1 += p0;
+                p2 += p1;
+                p3 += p2;
+                float inc = p3;  // inclusive scan of the lanes' totals
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float u = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += u;
+                }
+                const float before = inc - p3;
+                const float total = __shfl_sync(0xffffffffu, inc, 31);
+                int res;
+                bool is_empty = false;
+                if (!(total > 0.0f)) {
+                    is_empty = true;
+                    res = 0;
+                } else {
+                    const float2 bnd = lh[j];
+                    const float frac = ((float)dv[j] - bnd.x) / (bnd.y - bnd.x);
+                    int mine = 128;  // this lane's first hit among its rows r < F - 1
+                    if (r0 < F - 1 && frac < (before + p0) / total) mine = r0;
+                    else if (r0 + 1 < F - 1 && frac < (before + p1) / total) mine = r0 + 1;
+                    else if (r0 + 2 < F - 1 && frac < (before + p2) / total) mine = r0 + 2;
+                    else if (r0 + 3 < F - 1 && frac < (before + p3) / total) mine = r0 + 3;
+                    const unsigned mask = __ballot_sync(0xffffffffu, mine < 128);
+                    res = mask ? __shfl_sync(0xffffffffu, mine, __ffs(mask) - 1) : F - 1;
+                    if (res >= rows) res = rows - 1;  // frac >= 1 in a partial leaf
+                }
+                if (lane == 0) {
+                    samples[(int64_t)j * N + col] = (uint32_t)(leaf * F + res);
+                    if (is_empty) empty[j] = 1;
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+            i0 = i1;
+        }
+    }
+}
+
+// Leaf stage, F = 1 (eigen trees): the leaf index.
+__global__ void bfs_leaf1_kernel(TreeShape t, int64_t J, const int64_t* __restrict__ node, int N, int col,
+                                 uint32_t* __restrict__ samples, int32_t* __restrict__ v_out) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < J; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = tree_leaf_idx(t, node[j]);
+        samples[j * N + col] = (uint32_t)v;
+        v_out[j] = (int32_t)v;
+    }
+}
+
+// sh = h * E_next[v] and h = h * U_k[row] (row-wise products), h = 1.
+__global__ void bfs_scale_kernel(int R, int64_t J, const float* __restrict__ h, const float* __restrict__ Ek,
+                                 const int32_t* __restrict__ v, float* __restrict__ sh) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < J * R; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / R;
+        const int r = (int)(e - j * R);
+        sh[e] = h[e] * Ek[(int64_t)v[j] * R + r];
+    }
+}
+
+__global__ void bfs_row_update_kernel(int R, int64_t J, const float* __restrict__ Uk, const uint32_t* __restrict__ samples,
+                                      int N, int col, float* __restrict__ h) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < J * R; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / R;
+        const int r = (int)(e - j * R);
+        h[e] *= Uk[(int64_t)samples[j * N + col] * R + r];
+    }
+}
+
+__global__ void bfs_init_kernel(int R, int64_t J, float* __restrict__ h, int32_t* __restrict__ empty) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < J * R; e += (int64_t)gridDim.x * blockDim.x) {
+        h[e] = 1.0f;
+        if (e < J) empty[e] = 0;
+    }
+}
+
+// Weight = R / (J h^T Phi h); zero for a sample whose descent ended in an
+// empty leaf or whose quadratic form rounded to zero or below.
+__global__ void bfs_weight_kernel(int R, int64_t J, const float* __restrict__ hq, const int32_t* __restrict__ empty,
+                                  double* __restrict__ weights) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < J; j += (int64_t)gridDim.x * blockDim.x) {
+        const float q = hq[j];
+        weights[j] = (!empty[j] && q > 0.0f) ? (double)R / ((double)q * (double)J) : 0.0;
+    }
+}
+
+static unsigned grid_for_elems(int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 152 * 16));
+}
+
+size_t bfs_level_smem(int R) { return sizeof(float) * ((size_t)R * round4(R) + (size_t)kBfsWarps * round4(R)); }
+size_t bfs_leaf_smem(int R, int F) {
+    return sizeof(float) * ((size_t)R * (round4(F) + 4) + (size_t)kBfsWarps * round4(R));
+}
+
+// One descent of every sample through tree t (node array G, stride Pf;
+// leaf rows U for F > 1), driven by x (J x R) and the uniforms dv[j]; the
+// chosen rows go to samples[j * N + col] (and v_out for F = 1).
+static int bfs_descend(Session& s, const TreeShape& t, const float* G, const float* U, const float* X,
+                       const double* dv, int64_t J, int col, int32_t* v_out, cudaStream_t st) {
+    const int R = s.R, Pf = packed_stride_f32(R);
+    BfsState& b = s.bfs;
+    const size_t lsm = bfs_level_smem(R);
+    // every descent starts from the identity order (a permutation of 0..J-1
+    // whatever the earlier calls left)
+    bfs_reset_kernel<<<grid_for_elems(J), 256, 0, st>>>(J, b.node, b.lh, b.order[b.cur], b.off[0], 1);
+    count_launch();
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
+    bfs_level_kernel<0><<<blocks, kBfsWarps * 32, lsm, st>>>(R, Pf, G, X, J, b.order[b.cur], b.node, b.lh, b.m,
+                                                             dv, b.flag, t);
+    count_launch();
+    int oi = 0;                  // off[oi]: the current level's slot ranges
+    int64_t lb = 0, nl = 1;      // the level's first node and node count
+    const int64_t levels = t.lfill_level;
+    const bool tail = t.node_count > t.nodes_before_lfill;
+    for (int64_t lvl = 0; lvl <= levels; lvl++) {
+        const bool is_tail = lvl == levels;
+        if (is_tail && !tail) break;
+        if (is_tail)
+            bfs_level_kernel<2><<<blocks, kBfsWarps * 32, lsm, st>>>(R, Pf, G, X, J, b.order[b.cur], b.node, b.lh,
+                                                                     b.m, dv, b.flag, t);
+        else
+            bfs_level_kernel<1><<<blocks, kBfsWarps * 32, lsm, st>>>(R, Pf, G, X, J, b.order[b.cur], b.node, b.lh,
+                                                                     b.m, dv, b.flag, t);
+        count_launch();
+        EXAFAC_TRY(scan_exclusive_u32_to_i64(b.flag, b.SL, J, b.SL + J, s.scan_sc, st));
+        if (!is_tail) {
+            bfs_offsets_kernel<<<grid_for_elems(nl), 256, 0, st>>>(nl, J, b.off[oi], b.SL, b.off[oi ^ 1]);
+            count_launch();
+        }
+        bfs_scatter_kernel<<<grid_for_elems(J), 256, 0, st>>>(J, lb, nl, b.order[b.cur], b.node, b.off[oi], b.SL,
+                                                             b.flag, b.order[b.cur ^ 1]);
+        count_launch();
+        b.cur ^= 1;
+        oi ^= 1;
+        lb = 2 * lb + 1;
+        nl *= 2;
+    }
+    if (t.F > 1) {
+        const size_t fsm = bfs_leaf_smem(R, (int)t.F);
+        bfs_leaf_kernel<<<blocks, kBfsWarps * 32, fsm, st>>>(R, t, U, X, J, b.order[b.cur], b.node, b.lh, dv, s.N, col,
+                                                            s.samples, b.empty);
+    } else {
+        bfs_leaf1_kernel<<<grid_for_elems(J), 256, 0, st>>>(t, J, b.node, s.N, col, s.samples, v_out);
+    }
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
+    const int N = s.N, R = s.R, Pf = packed_stride_f32(R);
+    BfsState& b = s.bfs;
+    {  // the kernels' shared-memory limits (for the largest rank)
+        const int lsm = (int)bfs_level_smem(kMaxRank), fsm = (int)bfs_leaf_smem(kMaxRank, kMaxRank);
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_level_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm));
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_level_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm));
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_level_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm));
+        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    }
+    bfs_init_kernel<<<grid_for_elems(J * R), 256, 0, st>>>(R, J, b.h, b.empty);
+    count_launch();
+    for (int k = 0; k < N; k++) {
+        if (k == n) continue;
+        int nx = k + 1;
+        if (nx == n) nx++;
+        if (nx > N) nx = N;
+        const float* Ek = s.EmatF + (int64_t)nx * R * R;
+        // eigen tree of mode k, driven by h: v, then sh = h * E_next[v]
+        EXAFAC_TRY(bfs_descend(s, s.etree, s.eigF + (int64_t)k * s.etree.node_count * Pf, nullptr, b.h,
+                               uni + ((int64_t)k * 2 + 0) * J, J, n, b.v, st));
+        bfs_scale_kernel<<<grid_for_elems(J * R), 256, 0, st>>>(R, J, b.h, Ek, b.v, b.sh);
+        count_launch();
+        // row tree of mode k, driven by sh: the row, then h *= U_k[row]
+        EXAFAC_TRY(bfs_descend(s, s.rtree[k], s.treeF[k], s.Uf[k], b.sh, uni + ((int64_t)k * 2 + 1) * J, J, k,
+                               nullptr, st));
+        bfs_row_update_kernel<<<grid_for_elems(J * R), 256, 0, st>>>(R, J, s.Uf[k], s.samples, N, k, b.h);
+        count_launch();
+    }
+    // h^T Phi h (one node: Phi), then the weights
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
+    bfs_level_kernel<0><<<blocks, kBfsWarps * 32, bfs_level_smem(R), st>>>(R, Pf, s.PhiPF, b.h, J, b.order[b.cur],
+                                                                          b.node, b.lh, b.m, nullptr, b.flag,
+                                                                          s.etree);
+    count_launch();
+    bfs_weight_kernel<<<grid_for_elems(J), 256, 0, st>>>(R, J, b.m, b.empty, s.weights);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+}  // namespace exafac

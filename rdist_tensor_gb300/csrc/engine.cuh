@@ -52,6 +52,23 @@ struct FactorPtrs {  // factor matrices passed by value to kernels
     const double* U[kMaxModes];
 };
 
+// Sample state of the breadth-first STS-CP draws of the mixed forms
+// (bfs_sampler.cu), J_max entries each unless stated.
+struct BfsState {
+    float* h = nullptr;       // J x R: product of the chosen rows
+    float* sh = nullptr;      // J x R: h scaled by the chosen eigenvector row
+    float* m = nullptr;       // root mass of the current descent (then h^T Phi h)
+    float2* lh = nullptr;     // (low, high) of the current descent
+    int64_t* node = nullptr;  // current node
+    int32_t* order[2] = {nullptr, nullptr};  // slot -> sample, ordered by node (ping-pong)
+    int cur = 0;
+    uint32_t* flag = nullptr;  // by slot: went left (or stayed at a leaf)
+    int64_t* SL = nullptr;     // J + 1: exclusive scan of flag
+    int64_t* off[2] = {nullptr, nullptr};  // slot ranges of a level's nodes (ping-pong)
+    int32_t* v = nullptr;      // eigen-tree leaf of each sample
+    int32_t* empty = nullptr;  // a descent ended in a leaf of zero mass
+};
+
 struct Session {
     exafac_als_config cfg;
     int N = 0, R = 0, P = 0;
@@ -93,6 +110,7 @@ struct Session {
     float* eigF = nullptr;
     float* EmatF = nullptr;
     float* PhiPF = nullptr;
+    BfsState bfs;
 
     // nonzero-row tracking per factor (rows outside the list are zero)
     bool dense[kMaxModes] = {false};
@@ -168,6 +186,8 @@ int arls_leverage(Session& s, int k, bool all_rows, const double* pinv, cudaStre
 int arls_draw(Session& s, int n, int64_t J, const double* uni, const uint32_t* perms, cudaStream_t st);
 int sts_compute_M(Session& s, int n, cudaStream_t st);
 int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
+// The mixed forms' STS-CP draws, breadth first (bfs_sampler.cu).
+int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
 // FP32 copies of factor k and its row tree (mixed STS-CP sessions; else a no-op).
 int sts_refresh_f32(Session& s, int k, cudaStream_t st);
 // Row tree of mode k after a sampled update: FP64 build (FP64 form), or the

@@ -625,13 +625,7 @@ int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
         }
         return sts_draw_launch<double>(s, n, J, uni, treeG, U, s.eigG, s.Emat, s.PhiP, st);
     }
-    const float* treeG[kMaxModes];
-    const float* U[kMaxModes];
-    for (int k = 0; k < kMaxModes; k++) {
-        treeG[k] = k < s.N ? s.treeF[k] : nullptr;
-        U[k] = k < s.N ? s.Uf[k] : nullptr;
-    }
-    return sts_draw_launch<float>(s, n, J, uni, treeG, U, s.eigF, s.EmatF, s.PhiPF, st);
+    return sts_draw_bfs(s, n, J, uni, st);
 }
 
 }  // namespace exafac

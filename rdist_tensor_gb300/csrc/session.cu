@@ -65,6 +65,22 @@ static void carve(Session& s) {
             s.eigF = a.take<float>((int64_t)N * s.etree.node_count * Pf);
             s.EmatF = a.take<float>((int64_t)(N + 1) * R2);
             s.PhiPF = a.take<float>(Pf);
+            BfsState& b = s.bfs;
+            b.h = a.take<float>(J * R);
+            b.sh = a.take<float>(J * R);
+            b.m = a.take<float>(J);
+            b.lh = a.take<float2>(J);
+            b.node = a.take<int64_t>(J);
+            b.order[0] = a.take<int32_t>(J);
+            b.order[1] = a.take<int32_t>(J);
+            b.flag = a.take<uint32_t>(J);
+            b.SL = a.take<int64_t>(J + 1);
+            int64_t widest = std::max<int64_t>(s.etree.leaf_count, 1);  // nodes of the widest level
+            for (int k = 0; k < N; k++) widest = std::max<int64_t>(widest, s.rtree[k].leaf_count);
+            b.off[0] = a.take<int64_t>(2 * widest + 2);
+            b.off[1] = a.take<int64_t>(2 * widest + 2);
+            b.v = a.take<int32_t>(J);
+            b.empty = a.take<int32_t>(J);
         }
     }
     s.cdf_total = a.take<double>(N);
