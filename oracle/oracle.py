@@ -387,8 +387,11 @@ class OracleALS:
         else:
             self.sts.update(n, self.factors[n])
 
-    def step(self, n: int, J: int, uniforms, perms=None) -> dict:
-        samples, weights = self.draw(n, J, uniforms, perms)
+    def step(self, n: int, J: int, uniforms, perms=None, draws=None) -> dict:
+        """One AccumulatorStationary step.  draws: optional (samples, weights)
+        to use in place of the oracle's own draw (to check the solve of a
+        form whose draws may differ in a few near-tie samples)."""
+        samples, weights = self.draw(n, J, uniforms, perms) if draws is None else draws
         sd, wd = deduplicate(samples, weights, n)
         D, G, Phi = design_matrix(self.factors, sd, wd, n)
         M, hits = self.lookups[n].sampled_mttkrp(sd, D, self.dims[n])

@@ -734,6 +734,268 @@ int launch_syev(int R, const double* A, int64_t a_stride, int batch, double* V, 
     return EXAFAC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// STS-CP computeM of the mixed forms (sts_cp.hpp:80-188 with Cholesky factors
+// in place of the two eigendecompositions).
+//
+// The draws use, per sampled mode, rows e_v with sum_v e_v e_v^T = M (the
+// eigen tree picks v, then the row tree a row by (U_i . (h * e_v))^2): the
+// row is then drawn with probability proportional to (h * U_i)^T M (h * U_i)
+// whatever factor supplies the rows, so any E with E^T E = M gives the same
+// distribution of rows and weights as the reference's scaled eigenvectors
+// (only the intermediate leaf v differs).  The FP64 form keeps the
+// eigenvectors, which reproduce the reference's draws; the mixed forms take
+// Cholesky factors: about R^3 / 3 FP64 FMAs each, against some ten Jacobi
+// sweeps of about 5 R^3.
+//
+// sts_phi_chol_kernel (one CTA): A = chain[first] (the Hadamard product of
+// every Gram but mode n's) = L L^T, Phi = A^{-1} = L^{-T} L^{-1}, taken when
+// lambda_min >= 1 / ||A^{-1}||_F > 10 tol (as the Cholesky pseudo-inverse
+// above); the rows of L^{-1} are a factor of Phi and become E[N].  Otherwise
+// the CTA computes the Jacobi eigendecomposition and the reference's
+// W = V Lambda^{-1/2} (eigenvalues <= tol dropped).  Then chain[k] *= Phi
+// for k >= 1, k != n.
+//
+// sts_chain_chol_kernel (one CTA per k = 1..N-1, k != n): the pivoted
+// Cholesky P^T chain[k] P = L L^T (largest remaining diagonal first; stops
+// once it is <= R eps times the largest diagonal, the rest of the matrix, a
+// positive semidefinite remainder with entries that small, dropped): E[k]
+// row v = column v of P L.
+// ---------------------------------------------------------------------------
+
+// Right-looking Cholesky of the packed lower triangle L (tri(i, j), j <= i),
+// in place.  piv != nullptr: symmetric pivoting on the largest remaining
+// diagonal (piv[j] = the original index at position j), stopping when it is
+// <= stop; *rank = the number of columns factored.  piv == nullptr: stops at
+// a pivot that is not a positive finite number, *rank = its position.
+// col: R doubles of shared scratch.  Every thread returns the same *rank.
+__device__ void chol_packed_block(int R, double* L, int* piv, double stop, double* col, int* rank) {
+    __shared__ int s_p;
+    __shared__ int s_stop;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (piv)
+        for (int i = tid; i < R; i += nt) piv[i] = i;
+    if (tid == 0) s_stop = R;
+    __syncthreads();
+    for (int k = 0; k < R; k++) {
+        if (piv) {
+            if (tid < 32) {  // warp 0: the largest remaining diagonal (first index on ties)
+                double best = -1.0;
+                int bi = k;
+                for (int i = k + tid; i < R; i += 32) {
+                    const double d = L[tri(i, i)];
+                    if (d > best) {
+                        best = d;
+                        bi = i;
+                    }
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) {
+                        best = ob;
+                        bi = oi;
+                    }
+                }
+                if (tid == 0) {
+                    s_p = bi;
+                    if (!(best > stop)) s_stop = k;
+                }
+            }
+            __syncthreads();
+            if (s_stop == k) break;
+            const int p = s_p;
+            if (p != k) {  // swap rows and columns k and p (disjoint element pairs)
+                for (int j = tid; j < R; j += nt) {
+                    double *x = nullptr, *y = nullptr;
+                    if (j < k) {
+                        x = &L[tri(k, j)];
+                        y = &L[tri(p, j)];
+                    } else if (j == k) {
+                        x = &L[tri(k, k)];
+                        y = &L[tri(p, p)];
+                    } else if (j < p) {
+                        x = &L[tri(j, k)];
+                        y = &L[tri(p, j)];
+                    } else if (j > p) {
+                        x = &L[tri(j, k)];
+                        y = &L[tri(j, p)];
+                    }
+                    if (x) {
+                        const double t = *x;
+                        *x = *y;
+                        *y = t;
+                    }
+                }
+                if (tid == 0) {
+                    const int t = piv[k];
+                    piv[k] = piv[p];
+                    piv[p] = t;
+                }
+            }
+            __syncthreads();
+        } else {
+            const double d = L[tri(k, k)];
+            if (!(d > 0.0) || !isfinite(d)) {  // the same in every thread
+                if (tid == 0) s_stop = k;
+                break;
+            }
+        }
+        const double lkk = sqrt(L[tri(k, k)]);
+        for (int i = k + 1 + tid; i < R; i += nt) col[i] = L[tri(i, k)] / lkk;
+        __syncthreads();
+        if (tid == 0) L[tri(k, k)] = lkk;
+        const int m = R - k - 1;
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = k + 1 + e / m, j = k + 1 + e % m;
+            if (j < i) L[tri(i, j)] -= col[i] * col[j];
+            else if (j == i) {
+                L[tri(i, i)] -= col[i] * col[i];
+                L[tri(i, k)] = col[i];
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    *rank = s_stop;
+}
+
+__global__ void sts_phi_chol_kernel(int N, int n, int R, int first, double tol, double* __restrict__ chain,
+                                    double* __restrict__ E, double* __restrict__ Phi, double* __restrict__ PhiP,
+                                    double* __restrict__ V, double* __restrict__ lam, double* __restrict__ vt) {
+    extern __shared__ double smem[];
+    __shared__ double fro_w[32];
+    __shared__ double col[kMaxRank];
+    const int P = R * (R + 1) / 2, R2 = R * R;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    double* L = smem;
+    double* Li = smem + P;
+    const double* A = chain + (int64_t)first * R2;
+    double* EN = E + (int64_t)N * R2;
+    for (int e = tid; e < P; e += nt) {
+        int i = 0;
+        while (tri(i + 1, 0) <= e) i++;
+        const int j = e - tri(i, 0);
+        L[e] = A[j * R + i];  // upper triangle of A
+        Li[e] = 0.0;
+    }
+    __syncthreads();
+    int rank;
+    chol_packed_block(R, L, nullptr, 0.0, col, &rank);
+    bool ok = rank == R;
+    if (ok) {
+        for (int c = tid; c < R; c += nt) {  // L^{-1}, column c by forward substitution
+            for (int i = c; i < R; i++) {
+                double s = (i == c) ? 1.0 : 0.0;
+                for (int t = c; t < i; t++) s -= L[tri(i, t)] * Li[tri(t, c)];
+                Li[tri(i, c)] = s / L[tri(i, i)];
+            }
+        }
+        __syncthreads();
+        double part = 0.0;
+        for (int e = tid; e < R2; e += nt) {  // Phi = L^{-T} L^{-1}
+            const int a = e / R, b = e % R;
+            const int k0 = a > b ? a : b;
+            double acc = 0.0;
+            for (int k = k0; k < R; k++) acc = fma(Li[tri(k, a)], Li[tri(k, b)], acc);
+            Phi[e] = acc;
+            part += acc * acc;
+        }
+        part = warp_sum(part);
+        if ((tid & 31) == 0) fro_w[tid >> 5] = part;
+        __syncthreads();
+        double fro = 0.0;
+        for (int q = 0; q < (nt + 31) / 32; q++) fro += fro_w[q];
+        ok = isfinite(fro) && 1.0 / sqrt(fro) > 10.0 * tol;  // the same in every thread
+        if (ok)
+            for (int e = tid; e < R2; e += nt) {  // E[N] row v = row v of L^{-1}
+                const int v = e / R, u = e % R;
+                EN[e] = u <= v ? Li[tri(v, u)] : 0.0;
+            }
+    }
+    __syncthreads();
+    if (!ok) {  // Jacobi: W[:, R-1-v] = eigenvector v / sqrt(lambda_v), lambda_v > tol
+        syev_block(R, A, V, lam, nullptr, tol, vt, smem);
+        __syncthreads();
+        for (int e = tid; e < R2; e += nt) {
+            const int a = e / R, b = e % R;
+            const int v = R - 1 - a;
+            EN[e] = lam[v] > tol ? V[b * R + v] / sqrt(lam[v]) : 0.0;
+        }
+        __syncthreads();
+        for (int e = tid; e < R2; e += nt) {
+            const int a = e / R, b = e % R;
+            double acc = 0.0;
+            for (int w = 0; w < R; w++) acc = fma(EN[w * R + a], EN[w * R + b], acc);
+            Phi[e] = acc;
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < R2; e += nt) {
+        const int a = e / R, b = e % R;
+        const double p = Phi[a <= b ? a * R + b : b * R + a];
+        if (a <= b) PhiP[a * R - a * (a - 1) / 2 + (b - a)] = p;  // packed upper triangle, rows in order
+        for (int k = N - 1; k > 0; k--)
+            if (k != n) chain[(int64_t)k * R2 + e] *= p;
+    }
+}
+
+__global__ void sts_chain_chol_kernel(int N, int n, int R, const double* __restrict__ chain, double* __restrict__ E) {
+    extern __shared__ double smem[];
+    __shared__ double col[kMaxRank];
+    __shared__ int piv[kMaxRank];
+    __shared__ double dmax_w[32];
+    const int k = blockIdx.x;
+    if (k == 0 || k == n || k >= N) return;
+    const int P = R * (R + 1) / 2, R2 = R * R;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const double* A = chain + (int64_t)k * R2;
+    double* Ek = E + (int64_t)k * R2;
+    double* L = smem;
+    for (int e = tid; e < P; e += nt) {
+        int i = 0;
+        while (tri(i + 1, 0) <= e) i++;
+        const int j = e - tri(i, 0);
+        L[e] = A[j * R + i];
+    }
+    double dm = 0.0;
+    for (int i = tid; i < R; i += nt) dm = fmax(dm, A[i * R + i]);
+    for (int o = 16; o > 0; o >>= 1) dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+    if ((tid & 31) == 0) dmax_w[tid >> 5] = dm;
+    __syncthreads();
+    double dmax = 0.0;
+    for (int q = 0; q < (nt + 31) / 32; q++) dmax = fmax(dmax, dmax_w[q]);
+    int rank;
+    chol_packed_block(R, L, piv, (double)R * 2.220446049250313e-16 * dmax, col, &rank);
+    for (int e = tid; e < R2; e += nt) {  // E[k][v][piv[i]] = L[i][v]
+        const int v = e / R, i = e % R;
+        Ek[v * R + piv[i]] = (v < rank && i >= v) ? L[tri(i, v)] : 0.0;
+    }
+}
+
+size_t sts_factor_smem_bytes(int R) {
+    return std::max(sizeof(double) * 2 * (size_t)(R * (R + 1) / 2), syev_smem_bytes(R));
+}
+
+int launch_sts_factors_chol(int N, int n, int R, double tol, double* chain, double* E, double* Phi, double* PhiP,
+                            double* V, double* lam, double* vt, cudaStream_t stream) {
+    const size_t smem = sts_factor_smem_bytes(R);
+    EXAFAC_CUDA_TRY(cudaFuncSetAttribute(sts_phi_chol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int first = (n == 0) ? 1 : 0;
+    sts_phi_chol_kernel<<<1, 512, smem, stream>>>(N, n, R, first, tol, chain, E, Phi, PhiP, V, lam, vt);
+    count_launch();
+    const size_t fsm = sizeof(double) * (size_t)(R * (R + 1) / 2);
+    if (fsm > 48 * 1024)
+        EXAFAC_CUDA_TRY(
+            cudaFuncSetAttribute(sts_chain_chol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    if (N > 1) {
+        sts_chain_chol_kernel<<<N, 512, fsm, stream>>>(N, n, R, chain, E);
+        count_launch();
+    }
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
 }  // namespace exafac
 
 using namespace exafac;

@@ -30,4 +30,11 @@ int launch_sigma_pinv_f32(int R, const double* ugram, double* sigma, double* ngr
 int launch_pinv_leverage_f32(int R, const double* A, double* out, double tol, double* vt_scratch,
                              cudaStream_t stream);
 
+// STS-CP computeM of the mixed forms from Cholesky factors: Phi (full and
+// packed), E[N] and chain[k] *= Phi from chain[first] (Jacobi when not
+// provably well conditioned; V, lam, vt its scratch), then E[k] for k = 1..
+// N-1, k != n, from the pivoted Cholesky of chain[k].
+int launch_sts_factors_chol(int N, int n, int R, double tol, double* chain, double* E, double* Phi, double* PhiP,
+                            double* V, double* lam, double* vt, cudaStream_t stream);
+
 }  // namespace exafac

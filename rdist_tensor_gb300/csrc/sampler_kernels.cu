@@ -474,10 +474,10 @@ static int build_eigen_trees(Session& s, int n, cudaStream_t st) {
     return EXAFAC_OK;
 }
 
-int sts_compute_M(Session& s, int n, cudaStream_t st) {
+// The reference's factors: eigendecompositions of chain[first] (Phi, E[N])
+// and of chain[k] (E[k]).
+static int sts_eigen_factors(Session& s, int n, cudaStream_t st) {
     const int N = s.N, R = s.R, R2 = R * R;
-    sts_chain_kernel<<<1, 256, 0, st>>>(N, n, R, s.gram, s.chain); count_launch();
-    EXAFAC_CHECK_LAUNCH();
     const int first = (n == 0) ? 1 : 0;
     EXAFAC_TRY(launch_syev(R, s.chain + (int64_t)first * R2, 0, 1, s.eigV, s.eigL, 0, nullptr, 0.0, s.vt, st));
     const size_t phi_smem = sizeof(double) * R2;
@@ -491,6 +491,19 @@ int sts_compute_M(Session& s, int n, cudaStream_t st) {
     }
     sts_emat_kernel<<<1, 256, 0, st>>>(N, n, R, s.eigV, s.eigL, s.Emat); count_launch();
     EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+
+int sts_compute_M(Session& s, int n, cudaStream_t st) {
+    const int N = s.N, R = s.R, R2 = R * R;
+    sts_chain_kernel<<<1, 256, 0, st>>>(N, n, R, s.gram, s.chain); count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    if (s.cfg.precision != EXAFAC_PREC_FP64) {
+        // the mixed forms: Cholesky factors (the same row distribution)
+        EXAFAC_TRY(launch_sts_factors_chol(N, n, R, 1e-8, s.chain, s.Emat, s.Phi, s.PhiP, s.eigV, s.eigL, s.vt, st));
+    } else {
+        EXAFAC_TRY(sts_eigen_factors(s, n, st));
+    }
     EXAFAC_TRY(build_eigen_trees(s, n, st));
     if (s.cfg.precision != EXAFAC_PREC_FP64) {  // the mixed forms descend on FP32 copies
         EXAFAC_TRY(narrow_nodes(s.eigG, s.eigF, R, (int64_t)N * s.etree.node_count, st));

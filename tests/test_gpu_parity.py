@@ -256,16 +256,92 @@ def make_optimizer_prec(dims, idx, vals, factors, sampler, J_max, precision):
     return opt, lr
 
 
+def sts_quadratic_forms(factors, samples, n):
+    """h^T Phi h for each sample's rows: h the product of the sampled modes'
+    rows, Phi the pseudo-inverse of the Hadamard product of their Grams (the
+    FP64 oracle's, eigenvalues <= 1e-8 dropped as in sts_cp.hpp:110-153)."""
+    N, R = len(factors), factors[0].shape[1]
+    G = np.ones((R, R))
+    h = np.ones((samples.shape[0], R))
+    for k in range(N):
+        if k == n:
+            continue
+        G = G * (factors[k].T @ factors[k])
+        h = h * factors[k][samples[:, k].astype(np.int64)]
+    lam, V = np.linalg.eigh(G)
+    keep = lam > 1e-8
+    Phi = (V[:, keep] / lam[keep]) @ V[:, keep].T
+    return np.einsum("jr,rs,js->j", h, Phi, h)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32", "bf16"])
+@pytest.mark.parametrize("R", [3, 10])
+def test_mixed_sts_distribution(lib, oracle_mod, precision, R):
+    """The STS-CP draws follow the exact leverage distribution of the
+    Khatri-Rao product: P(rows) = h^T Phi h / rank(Phi) (the reference's
+    sampler, sts_cp.hpp:203-300, draws exactly from it).  A 40 x 12 x 9
+    tensor, all 108 (mode 1, mode 2) cells for mode 0 and 360 cells for mode
+    1, J = 2^18 seeded draws; Pearson's chi-square against the exact cell
+    probabilities, p > 1e-4.  R = 10 exceeds the 9 rows of mode 2, so its
+    Gram is singular and the pivoted Cholesky of the mixed forms stops short
+    of full rank."""
+    from scipy.stats import chi2
+
+    from rdist_tensor_gb300 import synthetic
+
+    dims = (40, 12, 9)
+    rng = np.random.default_rng(7)
+    nnz = 2000
+    idx = np.stack([rng.integers(0, d, nnz) for d in dims], axis=1).astype(np.uint32)
+    idx = np.unique(idx, axis=0)
+    vals = rng.standard_normal(idx.shape[0])
+    factors = synthetic.gaussian_factors(dims, R, seed=11)
+    J = 1 << 18
+    opt, lr = make_optimizer_prec(dims, idx, vals, factors, "sts_cp", J, precision)
+    for n in (0, 1):
+        modes = [k for k in range(3) if k != n]
+        uni = dev(rng.random((3, 2, J)), torch.float64)
+        s, w = opt.draw(n, J, uni)
+        s = s.cpu().numpy().astype(np.int64)
+        cells = np.array([(a, b) for a in range(dims[modes[0]]) for b in range(dims[modes[1]])])
+        full = np.zeros((cells.shape[0], 3), dtype=np.uint32)
+        full[:, modes[0]], full[:, modes[1]] = cells[:, 0], cells[:, 1]
+        q = sts_quadratic_forms(factors, full, n)
+        p = q / q.sum()
+        obs = np.bincount(s[:, modes[0]] * dims[modes[1]] + s[:, modes[1]], minlength=cells.shape[0])
+        exp = p * J
+        live = exp > 0
+        assert obs[~live].sum() == 0
+        stat = float(np.sum((obs[live] - exp[live]) ** 2 / exp[live]))
+        pval = float(chi2.sf(stat, live.sum() - 1))
+        print(f"{precision} R={R} mode {n}: chi2 {stat:.1f} dof {live.sum() - 1} p {pval:.3g}")
+        assert pval > 1e-4
+        w = w.cpu().numpy()
+        qs = sts_quadratic_forms(factors, s.astype(np.uint32), n)
+        assert rel_err(w, R / (qs * J)) < (1e-12 if precision == "fp64" else 1e-5)
+    opt.deinitialize()
+
+
 @pytest.mark.parametrize("R", [16, 48, 100])
 @pytest.mark.parametrize("precision", ["tf32", "bf16"])
 @pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])
 def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler, R):
-    """First step of the mixed forms (same samples as FP64: the initial
-    sampler state is FP64) against the oracle.  R <= 32: the MTTKRP is
-    accumulated in FP32 from FP32 design rows (relative error ~1e-6); R > 32:
-    FP64 design rows and MTTKRP.  The factor also passes through Phi, the
-    pseudo-inverse of a Gram formed on the tensor cores from TF32 (10-bit) or
-    BF16 (7-bit mantissa) inputs: factor within 1e-3 (TF32) / 2e-2 (BF16)."""
+    """First step of the mixed forms against the oracle.
+
+    Draws: CP-ARLS-LEV samples from the FP64 leverage scores and CDF, so its
+    indices equal the oracle's.  The mixed STS-CP draws take Cholesky factors
+    of the sampling matrices in place of the reference's scaled eigenvectors
+    and descend FP32 copies of the trees: the rows follow the same
+    distribution (test_mixed_sts_distribution) but are other samples.  Each
+    weight must still be R / (J h^T Phi h) for the rows drawn (h the product
+    of the rows, Phi the oracle's FP64 pseudo-inverse): within 1e-5, the FP32
+    quadratic form.
+
+    Solve: the oracle is run on the GPU's own draws, so the factor error is
+    that of the mixed arithmetic alone: FP32 design rows and MTTKRP, and Phi,
+    the pseudo-inverse of a Gram formed on the tensor cores from TF32 (10-bit)
+    or BF16 (7-bit mantissa) inputs: factor within 1e-3 (TF32) / 2e-2
+    (BF16)."""
     from rdist_tensor_gb300 import synthetic
 
     dims, idx, vals = synthetic.planted_uniform(dims=(300, 250, 200), nnz=60000, rank=5, seed=3)
@@ -276,8 +352,19 @@ def test_mixed_first_step_accuracy(lib, oracle_mod, precision, sampler, R):
     rng = np.random.default_rng(12)
     shape = (3, J) if sampler == "cp_arls_lev" else (3, 2, J)
     uni = rng.random(shape)
-    opt.execute_ALS_step(0, J, dev(uni, torch.float64))
-    out = ora.step(0, J, uni)
+    ud = dev(uni, torch.float64)
+    s_gpu, w_gpu = opt.draw(0, J, ud)
+    s_gpu = s_gpu.cpu().numpy().astype(np.uint32)
+    w_gpu = w_gpu.cpu().numpy()
+    if sampler == "cp_arls_lev":
+        s_ora, w_ora = ora.draw(0, J, uni)
+        assert np.array_equal(s_gpu, np.asarray(s_ora))
+        assert rel_err(w_gpu, w_ora) < 1e-12
+    else:
+        q = sts_quadratic_forms(factors, s_gpu, 0)
+        assert rel_err(w_gpu, R / (q * J)) < 1e-5
+    opt.execute_ALS_step(0, J, ud)
+    out = ora.step(0, J, uni, draws=(s_gpu, w_gpu))
     assert opt.step_info().hits == out["hits"]
     tol = 1e-3 if precision == "tf32" else 2e-2
     err_u = rel_err(lr.factors[0].data.cpu().numpy(), out["factor"])

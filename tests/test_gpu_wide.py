@@ -78,7 +78,11 @@ def test_mixed_wide_equal_fit(lib, sampler, precision, R):
     fit after the last three within 1e-3 of the FP64 form's.  R is
     far above the planted rank, so the factors are poorly determined: the
     factor error between the forms is large while the fits agree (it is
-    printed, not bounded)."""
+    printed, not bounded).  CP-ARLS-LEV draws the same samples in both forms,
+    so its first sweep (from random factors, the steepest) is also held to
+    2e-3; the mixed STS-CP draws are other samples of the same distribution
+    (Cholesky factors of the sampling matrices), so its first-sweep gap is
+    sampling noise and only the fixed-sweep bar applies."""
     from rdist_tensor_gb300 import synthetic
 
     dims, idx, vals = planted(8, 7)
@@ -104,7 +108,6 @@ def test_mixed_wide_equal_fit(lib, sampler, precision, R):
     print(f"{sampler} {precision} R={R}: fp64 fit {fits['fp64'][-1]:.6f}, gaps "
           + " ".join(f"{g:.1e}" for g in gaps) + ", factor error " + " ".join(f"{e:.1e}" for e in err))
     assert fits["fp64"][-1] > 0.1, fits
-    # the bar applies to the fit after a fixed number of sweeps; the first
-    # sweep (from random factors, the steepest) is held to 2e-3
     assert max(gaps[-3:]) < 1e-3, gaps
-    assert max(gaps) < 2e-3, gaps
+    if sampler == "cp_arls_lev":
+        assert max(gaps) < 2e-3, gaps
