@@ -80,6 +80,17 @@ int exafac_tree_sample(int64_t n, int32_t F, int32_t R, const double* G_dev, con
                        const double* x_dev, double* hmul_dev, const double* draws_dev, uint32_t* rows_out_dev,
                        int64_t rows_stride, void* stream);
 
+/* The quadratic forms of the mixed forms' breadth-first STS-CP descents
+ * (the per-level node masses of PartitionTree::PTSample,
+ * partition_tree.hpp:204-380, in FP32): q[j] = x_j^T G_{node[j]} x_j for J
+ * FP32 vectors (J x R, device) and node indices into G (packed upper
+ * triangles, rows in order, node stride (R (R + 1) / 2 rounded up to a
+ * multiple of 4) floats).  use_tc = 1: on the tensor cores (tcgen05, TF32
+ * split into hi + lo parts, R >= 32); 0: FP32 on the CUDA cores.  Slots of
+ * equal node next to each other share one staging of the node. */
+int exafac_quad_forms_f32(int32_t R, int64_t J, const float* X_dev, const int64_t* node_dev, const float* G_dev,
+                          float* q_dev, int32_t use_tc, void* stream);
+
 /* LAPACKE_dsyev('V','U') as used by the reference (sts_cp.hpp:110-116):
  * eigenvalues ascending in lambda_dev[R], eigenvector v in column v of V_dev
  * (V[u * R + v]).  Reads the upper triangle of A_dev.  One-CTA Jacobi. */

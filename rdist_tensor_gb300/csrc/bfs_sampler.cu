@@ -23,6 +23,7 @@
 // so the draws repeat run to run.
 #include "engine.cuh"
 #include "prims.cuh"
+#include "umma.cuh"
 
 namespace exafac {
 
@@ -37,6 +38,9 @@ __host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
 //         (d <= low + m_L / m goes left), node, (low, high), flag[slot].
 // MODE 2: the tail level: as MODE 1 for samples at internal nodes; samples
 //         already at a leaf stay (flag 1).
+// MODE 3: x^T G_c x with c = node[j] into mroot[j] (the quadratic forms alone,
+//         for tests).
+// order == nullptr: slot s holds sample s.
 template <int MODE>
 __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf, const float* __restrict__ G,
                                                                    const float* __restrict__ X, int64_t J,
@@ -60,7 +64,7 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
         const int n = (int)min((int64_t)kBfsTile, J - s0);
         __syncthreads();  // the previous tile is done with cs / js
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int32_t j = order[s0 + i];
+            const int32_t j = order ? order[s0 + i] : (int32_t)(s0 + i);
             js[i] = j;
             cs[i] = MODE == 0 ? 0 : node[j];
         }
@@ -75,7 +79,7 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
                 i0 = i1;
                 continue;
             }
-            const int64_t g = MODE == 0 ? 0 : 2 * c + 1;
+            const int64_t g = MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1);
             const float* Gn = G + g * Pf;
             for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
                 const int a = e / R, b = e - a * R;
@@ -105,7 +109,7 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
                 }
                 const float q = warp_sum(part);
                 if (lane == 0) {
-                    if (MODE == 0) {
+                    if (MODE == 0 || MODE == 3) {
                         mroot[j] = q;
                     } else {
                         const float2 bnd = lh[j];
@@ -121,6 +125,230 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
             __syncthreads();  // before the next run restages A
             i0 = i1;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same level on the fifth-generation tensor cores (R >= 32).  A block
+// takes 128 consecutive slots (the MMA's M); for each run of equal node in
+// them it forms Y = X A_node (128 x R) with tcgen05.mma, FP32 accumulators
+// in tensor memory, and each sample's form is q = sum_c Y[c] x[c], read back
+// by the warps that own its TMEM lane.  FP32 accuracy from TF32 inputs by the
+// split x = x_hi + x_lo, A = A_hi + A_lo (each part rounded to TF32):
+// Y ~ X_hi A_hi + X_hi A_lo + X_lo A_hi (relative error ~2^-21 of |X| |A|,
+// as FP32 sums of R products).  Operands are staged by the block's threads
+// into the K-major layout of umma.cuh: the slots' vectors once per tile
+// (hi and lo, 128 x Rk), the run's node in K chunks of at most 64 (hi and lo,
+// Rn x KC), the node read from its packed FP32 copy.  Rows of a run's MMA
+// that belong to other runs are computed and ignored.  Every wait on the MMA
+// barrier is bounded; a wait that runs out records EXAFAC_ERR_TIMEOUT, and
+// the block waits once more (bounded) for its MMAs, frees its tensor memory
+// and leaves.
+// ---------------------------------------------------------------------------
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 256;
+constexpr int kTcKChunk = 64;
+constexpr int kTcMinRank = 32;
+
+struct TcLayout {
+    int Rk, Rn, KC;    // K and N padded to 16 (the epilogue reads the slot tile over Y's N columns), K chunk
+    uint32_t a_bytes;  // one slot tile (hi or lo): 128 x Rk
+    uint32_t b_bytes;  // one node chunk (hi or lo): Rn x KC
+    uint32_t ncols;    // TMEM columns (power of two >= Rn)
+};
+__host__ __device__ inline TcLayout tc_layout(int R) {
+    TcLayout L;
+    L.Rn = (R + 15) & ~15;
+    L.Rk = L.Rn;
+    L.KC = L.Rk < kTcKChunk ? L.Rk : kTcKChunk;
+    L.a_bytes = (uint32_t)kTcRows * (uint32_t)L.Rk * 4u;
+    L.b_bytes = (uint32_t)L.Rn * (uint32_t)L.KC * 4u;
+    L.ncols = L.Rn <= 32 ? 32u : (L.Rn <= 64 ? 64u : (L.Rn <= 128 ? 128u : 256u));
+    return L;
+}
+size_t bfs_level_tc_smem(int R) {
+    const TcLayout L = tc_layout(R);
+    return 2 * (size_t)L.a_bytes + 2 * (size_t)L.b_bytes + 1024;  // + alignment of the base to 1 KB
+}
+
+// Byte offset of element (r, k) in a K-major tile with 8-row groups sbo bytes apart.
+__device__ __forceinline__ uint32_t kmajor_off(int r, int k, uint32_t sbo) {
+    return (uint32_t)(r >> 3) * sbo + (uint32_t)(k >> 2) * 128u + (uint32_t)(r & 7) * 16u + (uint32_t)(k & 3) * 4u;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    bfs_level_tc_kernel(int R, int Pf, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
+                        const int32_t* __restrict__ order, int64_t* __restrict__ node, float2* __restrict__ lh,
+                        float* __restrict__ mroot, const double* __restrict__ dv, uint32_t* __restrict__ flag,
+                        TreeShape t, DeviceStatus* status, uint32_t wait_polls) {
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    __shared__ int64_t cs[kTcRows];
+    __shared__ int32_t js[kTcRows];
+    __shared__ float qpart[2][kTcRows];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    const TcLayout L = tc_layout(R);
+    unsigned char* base = tc_raw + ((1024u - (smem_u32(tc_raw) & 1023u)) & 1023u);
+    unsigned char* Ahi = base;
+    unsigned char* Alo = base + L.a_bytes;
+    unsigned char* Bhi = base + 2 * L.a_bytes;
+    unsigned char* Blo = base + 2 * L.a_bytes + L.b_bytes;
+    const uint32_t sboA = (uint32_t)L.Rk * 32u, sboB = (uint32_t)L.KC * 32u;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    if (w == 0) tmem_alloc(&tmem_base, L.ncols);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = umma_idesc_tf32(kTcRows, L.Rn);
+    uint32_t phase = 0;
+    const int kq_per_row = L.Rk / 4;
+    const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t s0 = tile * kTcRows;
+        const int n = (int)min((int64_t)kTcRows, J - s0);
+        __syncthreads();  // the previous tile is done with cs / js and the slot tiles
+        for (int i = tid; i < n; i += kTcThreads) {
+            const int32_t j = order ? order[s0 + i] : (int32_t)(s0 + i);
+            js[i] = j;
+            cs[i] = MODE == 0 ? 0 : node[j];
+        }
+        __syncthreads();
+        // the slots' vectors, split hi + lo (rows past n and columns past R zero)
+        for (int e = tid; e < kTcRows * kq_per_row; e += kTcThreads) {
+            const int r = e / kq_per_row, kq = e - r * kq_per_row;
+            float hi[4], lo[4];
+            const float* xr = r < n ? X + (int64_t)js[r] * R : nullptr;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int k = 4 * kq + q;
+                const float x = (xr && k < R) ? xr[k] : 0.0f;
+                hi[q] = tf32_rna(x);
+                lo[q] = tf32_rna(x - hi[q]);
+            }
+            const uint32_t off = kmajor_off(r, 4 * kq, sboA);
+            *reinterpret_cast<float4*>(Ahi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<float4*>(Alo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        }
+        for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
+            const int64_t c = cs[i0];
+            int i1 = i0 + 1;
+            while (i1 < n && cs[i1] == c) i1++;
+            if (MODE == 2 && tree_is_leaf(t, c)) {
+                for (int i = i0 + tid; i < i1; i += kTcThreads) flag[s0 + i] = 1u;
+                i0 = i1;
+                continue;
+            }
+            const int64_t g = MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1);
+            const float* Gn = G + g * Pf;
+            for (int k0 = 0; k0 < L.Rk; k0 += L.KC) {
+                const int kc = min(L.KC, L.Rk - k0);
+                const int kq_c = kc / 4;
+                // the node's columns k0 .. k0 + kc - 1 (symmetric: row n of B = row n of A_node)
+                for (int e = tid; e < L.Rn * kq_c; e += kTcThreads) {
+                    const int nn = e / kq_c, kq = e - nn * kq_c;
+                    float hi[4], lo[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int k = k0 + 4 * kq + q;
+                        float a = 0.0f;
+                        if (nn < R && k < R) a = __ldg(Gn + (nn <= k ? packed_index(R, nn, k) : packed_index(R, k, nn)));
+                        hi[q] = tf32_rna(a);
+                        lo[q] = tf32_rna(a - hi[q]);
+                    }
+                    const uint32_t off = kmajor_off(nn, 4 * kq, sboB);
+                    *reinterpret_cast<float4*>(Bhi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<float4*>(Blo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                }
+                fence_proxy_async_smem();  // the staged operands, to the tensor core's proxy
+                __syncthreads();
+                if (tid == 0) {
+                    tc_fence_after();
+                    for (int s = 0; s < kc / 8; s++) {
+                        const uint32_t aoff = (uint32_t)(k0 + 8 * s) * 32u;  // (k / 4) * 128
+                        const uint32_t boff = (uint32_t)s * 256u;
+                        const uint64_t ah = umma_desc(Ahi + aoff, 128u, sboA), al = umma_desc(Alo + aoff, 128u, sboA);
+                        const uint64_t bh = umma_desc(Bhi + boff, 128u, sboB), bl = umma_desc(Blo + boff, 128u, sboB);
+                        umma_tf32(tmem, ah, bh, idesc, (k0 > 0 || s > 0) ? 1u : 0u);
+                        umma_tf32(tmem, ah, bl, idesc, 1u);
+                        umma_tf32(tmem, al, bh, idesc, 1u);
+                    }
+                    umma_commit(&bar);
+                }
+                bool done = false;  // the MMAs have read the chunk (and, after the last, written Y)
+                for (uint32_t it = 0; it < wait_polls && !done; it++) done = mbar_try_wait(&bar, phase);
+                if (!done) abort_flag = 1;
+                __syncthreads();
+                if (abort_flag) goto fail;
+                phase ^= 1u;
+            }
+            tc_fence_after();
+            {
+                // epilogue: warp w reads lanes 32 (w % 4) .. + 31 (its rows), column blocks of 16
+                // alternating between the two warp halves
+                const int qw = w & 3, half = w >> 2;
+                const int row = qw * 32 + lane;
+                float part = 0.0f;
+                for (int b = half; b < L.Rn / 16; b += 2) {
+                    float y[16];
+                    tmem_ld16(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(b * 16), y);
+#pragma unroll
+                    for (int q4 = 0; q4 < 4; q4++) {
+                        const uint32_t off = kmajor_off(row, b * 16 + 4 * q4, sboA);
+                        const float4 xh = *reinterpret_cast<const float4*>(Ahi + off);
+                        const float4 xl = *reinterpret_cast<const float4*>(Alo + off);
+                        part = fmaf(y[4 * q4 + 0], xh.x + xl.x, part);
+                        part = fmaf(y[4 * q4 + 1], xh.y + xl.y, part);
+                        part = fmaf(y[4 * q4 + 2], xh.z + xl.z, part);
+                        part = fmaf(y[4 * q4 + 3], xh.w + xl.w, part);
+                    }
+                }
+                qpart[half][row] = part;
+            }
+            tc_fence_before();
+            __syncthreads();
+            for (int i = i0 + tid; i < i1; i += kTcThreads) {
+                const float q = qpart[0][i] + qpart[1][i];
+                const int32_t j = js[i];
+                if (MODE == 0 || MODE == 3) {
+                    mroot[j] = q;
+                } else {
+                    const float2 bnd = lh[j];
+                    const float cutoff = bnd.x + q / mroot[j];
+                    const bool left = (float)dv[j] <= cutoff;
+                    node[j] = left ? 2 * c + 1 : 2 * c + 2;
+                    lh[j] = left ? make_float2(bnd.x, cutoff) : make_float2(cutoff, bnd.y);
+                    flag[s0 + i] = left ? 1u : 0u;
+                }
+            }
+            i0 = i1;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L.ncols);
+    }
+    return;
+fail:
+    if (tid == 0) report(status, EXAFAC_ERR_TIMEOUT, 20, blockIdx.x, 0);
+    {  // the MMAs in flight may still complete: wait for them once more (bounded)
+        bool done = false;
+        for (uint32_t it = 0; it < wait_polls && !done; it++) done = mbar_try_wait(&bar, phase);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L.ncols);
     }
 }
 
@@ -336,6 +564,42 @@ size_t bfs_leaf_smem(int R, int F) {
     return sizeof(float) * ((size_t)R * (round4(F) + 4) + (size_t)kBfsWarps * round4(R));
 }
 
+static void bfs_set_smem_limits() {
+    static bool done = false;  // host-side, per process: the attributes hold for every device's context
+    if (done) return;
+    const int lsm = (int)bfs_level_smem(kMaxRank), fsm = (int)bfs_leaf_smem(kMaxRank, kMaxRank);
+    const int tsm = (int)bfs_level_tc_smem(kMaxRank);
+    cudaFuncSetAttribute(bfs_level_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
+    cudaFuncSetAttribute(bfs_level_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
+    cudaFuncSetAttribute(bfs_level_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
+    cudaFuncSetAttribute(bfs_level_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
+    cudaFuncSetAttribute(bfs_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm);
+    cudaFuncSetAttribute(bfs_level_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+    cudaFuncSetAttribute(bfs_level_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+    cudaFuncSetAttribute(bfs_level_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+    cudaFuncSetAttribute(bfs_level_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+    done = true;
+}
+
+// One level (MODE as bfs_level_kernel) over slots order[0 .. J): on the
+// tensor cores for R >= kTcMinRank (use_tc), else on the CUDA cores.
+template <int MODE>
+static void bfs_level_launch(bool use_tc, int R, const float* G, const float* X, int64_t J, const int32_t* order,
+                             int64_t* node, float2* lh, float* m, const double* dv, uint32_t* flag, const TreeShape& t,
+                             DeviceStatus* status, uint32_t polls, cudaStream_t st) {
+    const int Pf = packed_stride_f32(R);
+    if (use_tc) {
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
+        bfs_level_tc_kernel<MODE><<<blocks, kTcThreads, bfs_level_tc_smem(R), st>>>(R, Pf, G, X, J, order, node, lh,
+                                                                                  m, dv, flag, t, status, polls);
+    } else {
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
+        bfs_level_kernel<MODE><<<blocks, kBfsWarps * 32, bfs_level_smem(R), st>>>(R, Pf, G, X, J, order, node, lh, m,
+                                                                                 dv, flag, t);
+    }
+    count_launch();
+}
+
 // One descent of every sample through tree t (node array G, stride Pf;
 // leaf rows U for F > 1), driven by x (J x R) and the uniforms dv[j]; the
 // chosen rows go to samples[j * N + col] (and v_out for F = 1).
@@ -343,15 +607,14 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
                        const double* dv, int64_t J, int col, int32_t* v_out, cudaStream_t st) {
     const int R = s.R, Pf = packed_stride_f32(R);
     BfsState& b = s.bfs;
-    const size_t lsm = bfs_level_smem(R);
+    const bool tc = R >= kTcMinRank;
+    const uint32_t polls = s.wait_polls ? s.wait_polls : kSpinLimit;
     // every descent starts from the identity order (a permutation of 0..J-1
     // whatever the earlier calls left)
     bfs_reset_kernel<<<grid_for_elems(J), 256, 0, st>>>(J, b.node, b.lh, b.order[b.cur], b.off[0], 1);
     count_launch();
     const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
-    bfs_level_kernel<0><<<blocks, kBfsWarps * 32, lsm, st>>>(R, Pf, G, X, J, b.order[b.cur], b.node, b.lh, b.m,
-                                                             dv, b.flag, t);
-    count_launch();
+    bfs_level_launch<0>(tc, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
     int oi = 0;                  // off[oi]: the current level's slot ranges
     int64_t lb = 0, nl = 1;      // the level's first node and node count
     const int64_t levels = t.lfill_level;
@@ -360,12 +623,9 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
         const bool is_tail = lvl == levels;
         if (is_tail && !tail) break;
         if (is_tail)
-            bfs_level_kernel<2><<<blocks, kBfsWarps * 32, lsm, st>>>(R, Pf, G, X, J, b.order[b.cur], b.node, b.lh,
-                                                                     b.m, dv, b.flag, t);
+            bfs_level_launch<2>(tc, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
         else
-            bfs_level_kernel<1><<<blocks, kBfsWarps * 32, lsm, st>>>(R, Pf, G, X, J, b.order[b.cur], b.node, b.lh,
-                                                                     b.m, dv, b.flag, t);
-        count_launch();
+            bfs_level_launch<1>(tc, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
         EXAFAC_TRY(scan_exclusive_u32_to_i64(b.flag, b.SL, J, b.SL + J, s.scan_sc, st));
         if (!is_tail) {
             bfs_offsets_kernel<<<grid_for_elems(nl), 256, 0, st>>>(nl, J, b.off[oi], b.SL, b.off[oi ^ 1]);
@@ -393,14 +653,9 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
 
 int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t st) {
     const int N = s.N, R = s.R, Pf = packed_stride_f32(R);
+    EXAFAC_CHECK_LAUNCH();
     BfsState& b = s.bfs;
-    {  // the kernels' shared-memory limits (for the largest rank)
-        const int lsm = (int)bfs_level_smem(kMaxRank), fsm = (int)bfs_leaf_smem(kMaxRank, kMaxRank);
-        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_level_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm));
-        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_level_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm));
-        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_level_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm));
-        EXAFAC_CUDA_TRY(cudaFuncSetAttribute(bfs_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
-    }
+    bfs_set_smem_limits();
     bfs_init_kernel<<<grid_for_elems(J * R), 256, 0, st>>>(R, J, b.h, b.empty);
     count_launch();
     for (int k = 0; k < N; k++) {
@@ -421,11 +676,8 @@ int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t s
         count_launch();
     }
     // h^T Phi h (one node: Phi), then the weights
-    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
-    bfs_level_kernel<0><<<blocks, kBfsWarps * 32, bfs_level_smem(R), st>>>(R, Pf, s.PhiPF, b.h, J, b.order[b.cur],
-                                                                          b.node, b.lh, b.m, nullptr, b.flag,
-                                                                          s.etree);
-    count_launch();
+    bfs_level_launch<0>(R >= kTcMinRank, R, s.PhiPF, b.h, J, b.order[b.cur], b.node, b.lh, b.m, nullptr, b.flag,
+                        s.etree, s.status, s.wait_polls ? s.wait_polls : kSpinLimit, st);
     bfs_weight_kernel<<<grid_for_elems(J), 256, 0, st>>>(R, J, b.m, b.empty, s.weights);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
@@ -433,3 +685,19 @@ int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t s
 }
 
 }  // namespace exafac
+
+using namespace exafac;
+
+extern "C" int exafac_quad_forms_f32(int32_t R, int64_t J, const float* X, const int64_t* node, const float* G,
+                                     float* q, int32_t use_tc, void* stream) {
+    EXAFAC_ARG(R >= 1 && R <= kMaxRank, "exafac_quad_forms_f32: R out of range");
+    EXAFAC_ARG(J >= 1 && J <= INT32_MAX, "exafac_quad_forms_f32: J out of range");
+    EXAFAC_ARG(X && node && G && q, "exafac_quad_forms_f32: null pointer");
+    EXAFAC_ARG(!use_tc || R >= kTcMinRank, "exafac_quad_forms_f32: the tensor-core form needs R >= 32");
+    bfs_set_smem_limits();
+    TreeShape t{};
+    bfs_level_launch<3>(use_tc != 0, R, G, X, J, nullptr, const_cast<int64_t*>(node), nullptr, q, nullptr, nullptr, t,
+                        nullptr, kSpinLimit, (cudaStream_t)stream);
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}

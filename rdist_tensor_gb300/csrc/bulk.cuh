@@ -31,6 +31,19 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
+// One poll of the phase of parity `phase`: true once it has completed.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return done != 0;
+}
+
 // Waits for the phase of parity `phase` to complete, at most kBulkWaitPolls
 // polls (each try_wait may itself suspend briefly).  False on timeout.
 constexpr uint32_t kBulkWaitPolls = 1u << 20;
