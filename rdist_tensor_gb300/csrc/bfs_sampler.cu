@@ -129,18 +129,20 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
 }
 
 // ---------------------------------------------------------------------------
-// The same level on the fifth-generation tensor cores (R >= 32).  A block
-// takes 128 consecutive slots (the MMA's M); for each run of equal node in
-// them it forms Y = X A_node (128 x R) with tcgen05.mma, FP32 accumulators
-// in tensor memory, and each sample's form is q = sum_c Y[c] x[c], read back
-// by the warps that own its TMEM lane.  FP32 accuracy from TF32 inputs by the
-// split x = x_hi + x_lo, A = A_hi + A_lo (each part rounded to TF32):
-// Y ~ X_hi A_hi + X_hi A_lo + X_lo A_hi (relative error ~2^-21 of |X| |A|,
-// as FP32 sums of R products).  Operands are staged by the block's threads
-// into the K-major layout of umma.cuh: the slots' vectors once per tile
-// (hi and lo, 128 x Rk), the run's node in K chunks of at most 64 (hi and lo,
-// Rn x KC), the node read from its packed FP32 copy.  Rows of a run's MMA
-// that belong to other runs are computed and ignored.  Every wait on the MMA
+// The level and leaf stages on the fifth-generation tensor cores (R >= 32).
+// A block takes 128 consecutive slots (the MMA's M).  For each run of equal
+// node in them it forms Y = X B^T (128 x N) with tcgen05.mma, FP32
+// accumulators in tensor memory, and reads each sample's row back in the warps
+// that own its TMEM lane: B is the node's R x R Gram for a level (the form
+// q = sum_c Y[c] x[c]), the leaf's F rows of U for the leaf stage (Y[r] =
+// U_r . x, the squared dots and their prefix).  FP32 accuracy from TF32
+// inputs by the split x = x_hi + x_lo, B = B_hi + B_lo (each part rounded to
+// TF32): Y ~ X_hi B_hi + X_hi B_lo + X_lo B_hi (relative error ~2^-21 of
+// |X| |B|, as FP32 sums of R products).  Operands are staged by the block's
+// threads into the K-major layout of umma.cuh: the slots' vectors once per
+// tile (hi and lo, 128 x Rk), B in K chunks of at most 64 (hi and lo,
+// Rn x KC), a node read from its packed FP32 copy.  Rows of a run's MMA that
+// belong to other runs are computed and ignored.  Every wait on the MMA
 // barrier is bounded; a wait that runs out records EXAFAC_ERR_TIMEOUT, and
 // the block waits once more (bounded) for its MMAs, frees its tensor memory
 // and leaves.
@@ -153,7 +155,7 @@ constexpr int kTcMinRank = 32;
 struct TcLayout {
     int Rk, Rn, KC;    // K and N padded to 16 (the epilogue reads the slot tile over Y's N columns), K chunk
     uint32_t a_bytes;  // one slot tile (hi or lo): 128 x Rk
-    uint32_t b_bytes;  // one node chunk (hi or lo): Rn x KC
+    uint32_t b_bytes;  // one B chunk (hi or lo): Rn x KC
     uint32_t ncols;    // TMEM columns (power of two >= Rn)
 };
 __host__ __device__ inline TcLayout tc_layout(int R) {
@@ -176,6 +178,178 @@ __device__ __forceinline__ uint32_t kmajor_off(int r, int k, uint32_t sbo) {
     return (uint32_t)(r >> 3) * sbo + (uint32_t)(k >> 2) * 128u + (uint32_t)(r & 7) * 16u + (uint32_t)(k & 3) * 4u;
 }
 
+// The block's tensor-core state: operand tiles, TMEM accumulator, MMA barrier.
+struct TcBlock {
+    TcLayout L;
+    unsigned char *Ahi, *Alo, *Bhi, *Blo;
+    uint32_t sboA, sboB, tmem, idesc, phase, polls;
+    uint64_t* bar;
+    int* abort_flag;
+};
+
+// Allocates TMEM (warp 0), initialises the barrier; every thread returns the same state.
+__device__ __forceinline__ TcBlock tc_begin(int R, unsigned char* raw, uint64_t* bar, uint32_t* tmem_base,
+                                            int* abort_flag, uint32_t polls) {
+    TcBlock b;
+    b.L = tc_layout(R);
+    unsigned char* base = raw + ((1024u - (smem_u32(raw) & 1023u)) & 1023u);
+    b.Ahi = base;
+    b.Alo = base + b.L.a_bytes;
+    b.Bhi = base + 2 * b.L.a_bytes;
+    b.Blo = base + 2 * b.L.a_bytes + b.L.b_bytes;
+    b.sboA = (uint32_t)b.L.Rk * 32u;
+    b.sboB = (uint32_t)b.L.KC * 32u;
+    b.idesc = umma_idesc_tf32(kTcRows, b.L.Rn);
+    b.phase = 0;
+    b.polls = polls;
+    b.bar = bar;
+    b.abort_flag = abort_flag;
+    if ((threadIdx.x >> 5) == 0) tmem_alloc(tmem_base, b.L.ncols);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        *abort_flag = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    b.tmem = *tmem_base;
+    return b;
+}
+
+// Frees TMEM; after an abort, first waits once more (bounded) for the MMAs in
+// flight and records the timeout.
+__device__ __forceinline__ void tc_end(TcBlock& b, DeviceStatus* status, int where) {
+    if (*b.abort_flag) {
+        if (threadIdx.x == 0) report(status, EXAFAC_ERR_TIMEOUT, where, blockIdx.x, 0);
+        bool done = false;
+        for (uint32_t it = 0; it < b.polls && !done; it++) done = mbar_try_wait(b.bar, b.phase);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+        tc_fence_after();
+        tmem_dealloc(b.tmem, b.L.ncols);
+    }
+}
+
+// Staging loops issue all of a thread's loads of one round (kTcUnroll
+// 16-byte chunks) before converting and storing any: the sources are
+// gathers from L2 and HBM, and the block is the only one on its SM.
+constexpr int kTcUnroll = 8;
+
+__device__ __forceinline__ void tc_store_split(unsigned char* hi_tile, unsigned char* lo_tile, uint32_t off, float4 v) {
+    float4 h, l;
+    h.x = tf32_rna(v.x);
+    h.y = tf32_rna(v.y);
+    h.z = tf32_rna(v.z);
+    h.w = tf32_rna(v.w);
+    l.x = tf32_rna(v.x - h.x);
+    l.y = tf32_rna(v.y - h.y);
+    l.z = tf32_rna(v.z - h.z);
+    l.w = tf32_rna(v.w - h.w);
+    *reinterpret_cast<float4*>(hi_tile + off) = h;
+    *reinterpret_cast<float4*>(lo_tile + off) = l;
+}
+
+// The tile's slot vectors X[js[r]] (rows past n and columns past R zero), split hi + lo.
+__device__ __forceinline__ void tc_stage_slots(const TcBlock& b, int R, const float* __restrict__ X,
+                                               const int32_t* js, int n) {
+    const int kq_per_row = b.L.Rk / 4;
+    const int total = kTcRows * kq_per_row;
+    const bool vec = (R & 3) == 0;  // rows start on 16-byte boundaries
+    for (int e0 = 0; e0 < total; e0 += kTcThreads * kTcUnroll) {
+        float4 v[kTcUnroll];
+#pragma unroll
+        for (int u = 0; u < kTcUnroll; u++) {
+            const int e = e0 + u * kTcThreads + threadIdx.x;
+            const int r = e / kq_per_row, k = 4 * (e - r * kq_per_row);
+            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (e < total && r < n && k < R) {
+                const float* xr = X + (int64_t)js[r] * R + k;
+                if (vec) {
+                    v[u] = __ldg(reinterpret_cast<const float4*>(xr));
+                } else {
+                    v[u].x = __ldg(xr);
+                    if (k + 1 < R) v[u].y = __ldg(xr + 1);
+                    if (k + 2 < R) v[u].z = __ldg(xr + 2);
+                    if (k + 3 < R) v[u].w = __ldg(xr + 3);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kTcUnroll; u++) {
+            const int e = e0 + u * kTcThreads + threadIdx.x;
+            if (e < total) {
+                const int r = e / kq_per_row, kq = e - r * kq_per_row;
+                tc_store_split(b.Ahi, b.Alo, kmajor_off(r, 4 * kq, b.sboA), v[u]);
+            }
+        }
+    }
+}
+
+// Y (TMEM) = X B^T over all K chunks, B(nn, k .. k + 3) = load4(nn, k) for
+// nn < Rn, k < Rk a multiple of 4 (zero outside the matrix is the loader's
+// job).  Returns false (in every thread) when a wait ran out; the caller then
+// ends the block.
+template <typename Load4>
+__device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
+    const int tid = threadIdx.x;
+    for (int k0 = 0; k0 < b.L.Rk; k0 += b.L.KC) {
+        const int kc = min(b.L.KC, b.L.Rk - k0);
+        const int kq_c = kc / 4;
+        const int total = b.L.Rn * kq_c;
+        for (int e0 = 0; e0 < total; e0 += kTcThreads * kTcUnroll) {
+            float4 v[kTcUnroll];
+#pragma unroll
+            for (int u = 0; u < kTcUnroll; u++) {
+                const int e = e0 + u * kTcThreads + tid;
+                const int nn = e / kq_c, kq = e - nn * kq_c;
+                v[u] = e < total ? load4(nn, k0 + 4 * kq) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < kTcUnroll; u++) {
+                const int e = e0 + u * kTcThreads + tid;
+                if (e < total) {
+                    const int nn = e / kq_c, kq = e - nn * kq_c;
+                    tc_store_split(b.Bhi, b.Blo, kmajor_off(nn, 4 * kq, b.sboB), v[u]);
+                }
+            }
+        }
+        fence_proxy_async_smem();  // the staged operands, to the tensor core's proxy
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            for (int s = 0; s < kc / 8; s++) {
+                const uint32_t aoff = (uint32_t)(k0 + 8 * s) * 32u;  // (k / 4) * 128
+                const uint32_t boff = (uint32_t)s * 256u;
+                const uint64_t ah = umma_desc(b.Ahi + aoff, 128u, b.sboA), al = umma_desc(b.Alo + aoff, 128u, b.sboA);
+                const uint64_t bh = umma_desc(b.Bhi + boff, 128u, b.sboB), bl = umma_desc(b.Blo + boff, 128u, b.sboB);
+                umma_tf32(b.tmem, ah, bh, b.idesc, (k0 > 0 || s > 0) ? 1u : 0u);
+                umma_tf32(b.tmem, ah, bl, b.idesc, 1u);
+                umma_tf32(b.tmem, al, bh, b.idesc, 1u);
+            }
+            umma_commit(b.bar);
+        }
+        bool done = false;  // the MMAs have read the chunk (and, after the last, written Y)
+        for (uint32_t it = 0; it < b.polls && !done; it++) done = mbar_try_wait(b.bar, b.phase);
+        if (!done) *b.abort_flag = 1;
+        __syncthreads();
+        if (*b.abort_flag) return false;
+        b.phase ^= 1u;
+    }
+    tc_fence_after();
+    return true;
+}
+
+// x of the slot in row `row` of the tile, columns c .. c + 3 (hi + lo).
+__device__ __forceinline__ float4 tc_slot_x4(const TcBlock& b, int row, int c) {
+    const uint32_t off = kmajor_off(row, c, b.sboA);
+    const float4 h = *reinterpret_cast<const float4*>(b.Ahi + off);
+    const float4 l = *reinterpret_cast<const float4*>(b.Alo + off);
+    return make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
     bfs_level_tc_kernel(int R, int Pf, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
@@ -189,27 +363,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    const TcLayout L = tc_layout(R);
-    unsigned char* base = tc_raw + ((1024u - (smem_u32(tc_raw) & 1023u)) & 1023u);
-    unsigned char* Ahi = base;
-    unsigned char* Alo = base + L.a_bytes;
-    unsigned char* Bhi = base + 2 * L.a_bytes;
-    unsigned char* Blo = base + 2 * L.a_bytes + L.b_bytes;
-    const uint32_t sboA = (uint32_t)L.Rk * 32u, sboB = (uint32_t)L.KC * 32u;
+    TcBlock b = tc_begin(R, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    if (w == 0) tmem_alloc(&tmem_base, L.ncols);
-    if (tid == 0) {
-        mbar_init(&bar, 1);
-        fence_mbar_init();
-        abort_flag = 0;
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = tmem_base;
-    const uint32_t idesc = umma_idesc_tf32(kTcRows, L.Rn);
-    uint32_t phase = 0;
-    const int kq_per_row = L.Rk / 4;
     const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t s0 = tile * kTcRows;
@@ -221,22 +376,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             cs[i] = MODE == 0 ? 0 : node[j];
         }
         __syncthreads();
-        // the slots' vectors, split hi + lo (rows past n and columns past R zero)
-        for (int e = tid; e < kTcRows * kq_per_row; e += kTcThreads) {
-            const int r = e / kq_per_row, kq = e - r * kq_per_row;
-            float hi[4], lo[4];
-            const float* xr = r < n ? X + (int64_t)js[r] * R : nullptr;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int k = 4 * kq + q;
-                const float x = (xr && k < R) ? xr[k] : 0.0f;
-                hi[q] = tf32_rna(x);
-                lo[q] = tf32_rna(x - hi[q]);
-            }
-            const uint32_t off = kmajor_off(r, 4 * kq, sboA);
-            *reinterpret_cast<float4*>(Ahi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4*>(Alo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-        }
+        tc_stage_slots(b, R, X, js, n);
         for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
             const int64_t c = cs[i0];
             int i1 = i0 + 1;
@@ -248,66 +388,38 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             const int64_t g = MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1);
             const float* Gn = G + g * Pf;
-            for (int k0 = 0; k0 < L.Rk; k0 += L.KC) {
-                const int kc = min(L.KC, L.Rk - k0);
-                const int kq_c = kc / 4;
-                // the node's columns k0 .. k0 + kc - 1 (symmetric: row n of B = row n of A_node)
-                for (int e = tid; e < L.Rn * kq_c; e += kTcThreads) {
-                    const int nn = e / kq_c, kq = e - nn * kq_c;
-                    float hi[4], lo[4];
+            // the node (symmetric: row nn of B = row nn of A)
+            const bool ok = tc_product(b, [&](int nn, int k) -> float4 {
+                float a[4];
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const int k = k0 + 4 * kq + q;
-                        float a = 0.0f;
-                        if (nn < R && k < R) a = __ldg(Gn + (nn <= k ? packed_index(R, nn, k) : packed_index(R, k, nn)));
-                        hi[q] = tf32_rna(a);
-                        lo[q] = tf32_rna(a - hi[q]);
-                    }
-                    const uint32_t off = kmajor_off(nn, 4 * kq, sboB);
-                    *reinterpret_cast<float4*>(Bhi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                    *reinterpret_cast<float4*>(Blo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                for (int q = 0; q < 4; q++) {
+                    const int kk = k + q;
+                    a[q] = (nn < R && kk < R)
+                               ? __ldg(Gn + (nn <= kk ? packed_index(R, nn, kk) : packed_index(R, kk, nn)))
+                               : 0.0f;
                 }
-                fence_proxy_async_smem();  // the staged operands, to the tensor core's proxy
-                __syncthreads();
-                if (tid == 0) {
-                    tc_fence_after();
-                    for (int s = 0; s < kc / 8; s++) {
-                        const uint32_t aoff = (uint32_t)(k0 + 8 * s) * 32u;  // (k / 4) * 128
-                        const uint32_t boff = (uint32_t)s * 256u;
-                        const uint64_t ah = umma_desc(Ahi + aoff, 128u, sboA), al = umma_desc(Alo + aoff, 128u, sboA);
-                        const uint64_t bh = umma_desc(Bhi + boff, 128u, sboB), bl = umma_desc(Blo + boff, 128u, sboB);
-                        umma_tf32(tmem, ah, bh, idesc, (k0 > 0 || s > 0) ? 1u : 0u);
-                        umma_tf32(tmem, ah, bl, idesc, 1u);
-                        umma_tf32(tmem, al, bh, idesc, 1u);
-                    }
-                    umma_commit(&bar);
-                }
-                bool done = false;  // the MMAs have read the chunk (and, after the last, written Y)
-                for (uint32_t it = 0; it < wait_polls && !done; it++) done = mbar_try_wait(&bar, phase);
-                if (!done) abort_flag = 1;
-                __syncthreads();
-                if (abort_flag) goto fail;
-                phase ^= 1u;
+                return make_float4(a[0], a[1], a[2], a[3]);
+            });
+            if (!ok) {
+                tc_end(b, status, 20);
+                return;
             }
-            tc_fence_after();
             {
-                // epilogue: warp w reads lanes 32 (w % 4) .. + 31 (its rows), column blocks of 16
-                // alternating between the two warp halves
+                // warp w reads lanes 32 (w % 4) .. + 31 (its rows); column
+                // blocks of 16 alternate between the two warp halves
                 const int qw = w & 3, half = w >> 2;
                 const int row = qw * 32 + lane;
                 float part = 0.0f;
-                for (int b = half; b < L.Rn / 16; b += 2) {
+                for (int cb = half; cb < b.L.Rn / 16; cb += 2) {
                     float y[16];
-                    tmem_ld16(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(b * 16), y);
+                    tmem_ld16(b.tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(cb * 16), y);
 #pragma unroll
                     for (int q4 = 0; q4 < 4; q4++) {
-                        const uint32_t off = kmajor_off(row, b * 16 + 4 * q4, sboA);
-                        const float4 xh = *reinterpret_cast<const float4*>(Ahi + off);
-                        const float4 xl = *reinterpret_cast<const float4*>(Alo + off);
-                        part = fmaf(y[4 * q4 + 0], xh.x + xl.x, part);
-                        part = fmaf(y[4 * q4 + 1], xh.y + xl.y, part);
-                        part = fmaf(y[4 * q4 + 2], xh.z + xl.z, part);
-                        part = fmaf(y[4 * q4 + 3], xh.w + xl.w, part);
+                        const float4 x = tc_slot_x4(b, row, cb * 16 + 4 * q4);
+                        part = fmaf(y[4 * q4 + 0], x.x, part);
+                        part = fmaf(y[4 * q4 + 1], x.y, part);
+                        part = fmaf(y[4 * q4 + 2], x.z, part);
+                        part = fmaf(y[4 * q4 + 3], x.w, part);
                     }
                 }
                 qpart[half][row] = part;
@@ -331,25 +443,123 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             i0 = i1;
         }
     }
-    tc_fence_before();
-    __syncthreads();
-    if (w == 0) {
-        tc_fence_after();
-        tmem_dealloc(tmem, L.ncols);
+    tc_end(b, status, 20);
+}
+
+// Leaf stage on the tensor cores (F > 1, F <= Rn): Y[r] = U_r . x for the
+// leaf's rows, then in each sample's own thread the squared dots' inclusive
+// prefix in row order and the first row r < F - 1 with frac < prefix_r /
+// total, else the last row the leaf holds (as bfs_leaf_kernel).  Warps 0-3
+// hold the lanes; a thread keeps its row's squares in registers, 16 columns
+// per TMEM load.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    bfs_leaf_tc_kernel(int R, TreeShape t, const float* __restrict__ U, const float* __restrict__ X, int64_t J,
+                       const int32_t* __restrict__ order, const int64_t* __restrict__ node,
+                       const float2* __restrict__ lh, const double* __restrict__ dv, int N, int col,
+                       uint32_t* __restrict__ samples, int32_t* __restrict__ empty, DeviceStatus* status,
+                       uint32_t wait_polls) {
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    __shared__ int64_t cs[kTcRows];
+    __shared__ int32_t js[kTcRows];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    TcBlock b = tc_begin(R, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int F = (int)t.F;
+    const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t s0 = tile * kTcRows;
+        const int n = (int)min((int64_t)kTcRows, J - s0);
+        __syncthreads();
+        for (int i = tid; i < n; i += kTcThreads) {
+            const int32_t j = order[s0 + i];
+            js[i] = j;
+            cs[i] = node[j];
+        }
+        __syncthreads();
+        tc_stage_slots(b, R, X, js, n);
+        for (int i0 = 0; i0 < n;) {
+            const int64_t c = cs[i0];
+            int i1 = i0 + 1;
+            while (i1 < n && cs[i1] == c) i1++;
+            const int64_t leaf = tree_leaf_idx(t, c);
+            const int rows = (int)min((int64_t)F, t.n - leaf * F);
+            const float* Ub = U + leaf * F * R;
+            const bool vec = (R & 3) == 0;
+            const bool ok = tc_product(b, [&](int r, int k) -> float4 {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (r < rows && k < R) {
+                    const float* u = Ub + (int64_t)r * R + k;
+                    if (vec) {
+                        v = __ldg(reinterpret_cast<const float4*>(u));
+                    } else {
+                        v.x = __ldg(u);
+                        if (k + 1 < R) v.y = __ldg(u + 1);
+                        if (k + 2 < R) v.z = __ldg(u + 2);
+                        if (k + 3 < R) v.w = __ldg(u + 3);
+                    }
+                }
+                return v;
+            });
+            if (!ok) {
+                tc_end(b, status, 21);
+                return;
+            }
+            if (w < 4) {
+                const int row = w * 32 + lane;  // this thread's slot in the tile
+                const bool mine = row >= i0 && row < i1;
+                const uint32_t tl = b.tmem + ((uint32_t)(w * 32) << 16);
+                const int nb = b.L.Rn / 16;
+                float total = 0.0f;  // the squared dots summed in row order
+                for (int cb = 0; cb < nb; cb++) {
+                    float y[16];
+                    tmem_ld16(tl + (uint32_t)(cb * 16), y);
+#pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        if (cb * 16 + q < F) total += y[q] * y[q];
+                }
+                const int32_t j = mine ? js[row] : 0;
+                const bool is_empty = !(total > 0.0f);
+                float frac = 0.0f;
+                if (mine && !is_empty) {
+                    const float2 bnd = lh[j];
+                    frac = ((float)dv[j] - bnd.x) / (bnd.y - bnd.x);
+                }
+                // the same sum again, stopping at the first r < F - 1 with
+                // frac < prefix_r / total (prefix_{F-1} equals total)
+                int res = F - 1;
+                bool found = !mine || is_empty;
+                float prefix = 0.0f;
+                for (int cb = 0; cb < nb; cb++) {
+                    if (__all_sync(0xffffffffu, found)) break;
+                    float y[16];
+                    tmem_ld16(tl + (uint32_t)(cb * 16), y);
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int r = cb * 16 + q;
+                        if (!found && r < F - 1) {
+                            prefix += y[q] * y[q];
+                            if (frac < prefix / total) {
+                                res = r;
+                                found = true;
+                            }
+                        }
+                    }
+                }
+                if (mine) {
+                    if (is_empty) res = 0;
+                    else if (res >= rows) res = rows - 1;  // frac >= 1 in a partial leaf
+                    samples[(int64_t)j * N + col] = (uint32_t)(leaf * F + res);
+                    if (is_empty) empty[j] = 1;
+                }
+            }
+            tc_fence_before();
+            __syncthreads();
+            i0 = i1;
+        }
     }
-    return;
-fail:
-    if (tid == 0) report(status, EXAFAC_ERR_TIMEOUT, 20, blockIdx.x, 0);
-    {  // the MMAs in flight may still complete: wait for them once more (bounded)
-        bool done = false;
-        for (uint32_t it = 0; it < wait_polls && !done; it++) done = mbar_try_wait(&bar, phase);
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (w == 0) {
-        tc_fence_after();
-        tmem_dealloc(tmem, L.ncols);
-    }
+    tc_end(b, status, 21);
 }
 
 // Slot ranges of the next level's nodes from the parents' (nl of them,
@@ -578,6 +788,7 @@ static void bfs_set_smem_limits() {
     cudaFuncSetAttribute(bfs_level_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     cudaFuncSetAttribute(bfs_level_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     cudaFuncSetAttribute(bfs_level_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+    cudaFuncSetAttribute(bfs_leaf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     done = true;
 }
 
@@ -639,7 +850,12 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
         lb = 2 * lb + 1;
         nl *= 2;
     }
-    if (t.F > 1) {
+    if (t.F > 1 && tc && t.F <= tc_layout(R).Rn) {
+        const unsigned tblocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
+        bfs_leaf_tc_kernel<<<tblocks, kTcThreads, bfs_level_tc_smem(R), st>>>(R, t, U, X, J, b.order[b.cur], b.node,
+                                                                            b.lh, dv, s.N, col, s.samples, b.empty,
+                                                                            s.status, polls);
+    } else if (t.F > 1) {
         const size_t fsm = bfs_leaf_smem(R, (int)t.F);
         bfs_leaf_kernel<<<blocks, kBfsWarps * 32, fsm, st>>>(R, t, U, X, J, b.order[b.cur], b.node, b.lh, dv, s.N, col,
                                                             s.samples, b.empty);

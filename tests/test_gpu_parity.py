@@ -275,7 +275,7 @@ def sts_quadratic_forms(factors, samples, n):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "tf32", "bf16"])
-@pytest.mark.parametrize("R", [3, 10])
+@pytest.mark.parametrize("R", [3, 10, 40])
 def test_mixed_sts_distribution(lib, oracle_mod, precision, R):
     """The STS-CP draws follow the exact leverage distribution of the
     Khatri-Rao product: P(rows) = h^T Phi h / rank(Phi) (the reference's
@@ -284,7 +284,8 @@ def test_mixed_sts_distribution(lib, oracle_mod, precision, R):
     1, J = 2^18 seeded draws; Pearson's chi-square against the exact cell
     probabilities, p > 1e-4.  R = 10 exceeds the 9 rows of mode 2, so its
     Gram is singular and the pivoted Cholesky of the mixed forms stops short
-    of full rank."""
+    of full rank; R = 40 takes the mixed forms' tensor-core level and leaf
+    kernels, every row tree a single partial leaf."""
     from scipy.stats import chi2
 
     from rdist_tensor_gb300 import synthetic
