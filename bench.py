@@ -170,6 +170,51 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def level_kernel_roofline(R, J, nodes=1024, launches=5, seed=0):
+    """Roofline of the mixed forms' dominant kernel, the tcgen05 level kernel
+    of the breadth-first STS-CP descents, timed live: exafac_quad_forms_f32 on
+    the tensor cores (the level kernel's quadratic forms, without the branch
+    epilogue) over J FP32 vectors of rank R, slots sorted by node over
+    `nodes` distinct packed nodes, as at a middle level of a descent.  One
+    launch reads every vector once (J R 4 bytes, gathered rows) and each
+    node's packed Gram once; its tensor-core work is two TF32 MMAs per K step
+    (2 J R^2 multiply-adds) against the 2 J R^2 flops of the forms.  CUDA
+    events on the launching stream, the average of `launches` launches after
+    two warm-up launches; inputs (J R 4 bytes, 268 MB at J = 2^19, R = 128)
+    larger than L2."""
+    import torch
+
+    from rdist_tensor_gb300 import _lib
+
+    Pf = (R * (R + 1) // 2 + 3) & ~3
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    X = torch.randn((J, R), generator=g, device="cuda", dtype=torch.float32)
+    G = torch.randn((nodes, Pf), generator=g, device="cuda", dtype=torch.float32)
+    node = torch.sort(torch.randint(0, nodes, (J,), generator=g, device="cuda")).values.contiguous()
+    q = torch.empty(J, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    args = (R, J, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(node.data_ptr()), ctypes.c_void_p(G.data_ptr()),
+            ctypes.c_void_p(q.data_ptr()), 1, ctypes.c_void_p(st.cuda_stream))
+    for _ in range(2):
+        _lib.call("exafac_quad_forms_f32", *args)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(launches):
+        _lib.call("exafac_quad_forms_f32", *args)
+    e1.record(st)
+    torch.cuda.synchronize()
+    dur = e0.elapsed_time(e1) * 1e-3 / launches
+    used = int(torch.unique(node).numel())
+    algo = J * R * 4 + used * Pf * 4
+    peak, peak_kind = measured_peaks()
+    achieved = algo / dur / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "bfs_level_tc_kernel (tcgen05 quadratic forms of a descent level)",
+            "algorithmic_bytes": algo, "duration_s": dur, "launches": launches, "peak_source": peak_kind,
+            "tensor_tflops": 2.0 * J * R * R / dur / 1e12, "J": J, "R": R, "nodes": used}
+
+
 def make_workload(w, seed=0):
     """Seeded synthetic tensor of the workload on the GPU: (dims, int32
     coordinates, values) as device tensors."""
@@ -357,6 +402,9 @@ def run_gpu(args, w):
     ws, rank, local = dist_init()
     torch.cuda.set_device(local)
     lib = _lib.load()
+    if args.kernel_only:  # the dominant kernel alone (for a kernel profile)
+        print(json.dumps({"roofline": level_kernel_roofline(w["R"], w["J"])}), flush=True)
+        return 0
     dims, idx, vals = make_workload(w, seed=args.seed + rank)
     N, R, J = len(dims), w["R"], w["J"]
     nnz = int(idx.shape[0])
@@ -447,6 +495,25 @@ def run_gpu(args, w):
         return {"value": ws * sweeps / el, "unit": "sweeps/s", "h2d_bytes_per_step": N * per * 8,
                 "d2h_bytes_per_step": R * 8, "sweeps": sweeps}
 
+    if args.nvtx_sweep:  # one sweep step by step inside an NVTX range (for a launch list)
+        opt, lr, _ = build_optimizer(w, dims, idx, vals, J, precision)
+        for _ in range(warmup):
+            for n in range(N):
+                opt.execute_ALS_step(n, J)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push("sweep")
+        for n in range(N):
+            opt.execute_ALS_step(n, J)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        opt.step_info()
+        print(json.dumps({"nvtx_sweep_s": el, "precision": precision, "workload": w["desc"],
+                          "fit": opt.compute_exact_fit()}), flush=True)
+        opt.deinitialize()
+        return 0
+
     # ---- the FP64 form (the reference's arithmetic), and other mixed forms --
     forms = {}
     compare = [] if (precision == "fp64" or args.no_fp64_form) else ["fp64"]
@@ -499,6 +566,12 @@ def run_gpu(args, w):
                 "regions_s": dict(zip(region_names, list(regions))),
                 "units_per_step": [{"unique_samples": a, "hits": b, "touched_rows": c} for a, b, c in units]}
 
+    # ---- roofline of the dominant kernel (the mixed STS-CP descents') -----
+    mttkrp = None
+    if w["sampler"] == "sts_cp" and precision != "fp64" and R >= 32:
+        mttkrp = roofline
+        roofline = level_kernel_roofline(R, J)
+
     # ---- the drop-in round loop (execute_ALS_rounds, region timers on) ----
     rounds = 2
     opt.execute_ALS_rounds(rounds, J, rounds)
@@ -543,6 +616,8 @@ def run_gpu(args, w):
             "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded; no public dataset is named for these shapes)",
             "config": cfg, "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if mttkrp is not None:
+        line["roofline_sampled_mttkrp"] = mttkrp
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -564,6 +639,11 @@ def main():
     ap.add_argument("--ref-sweeps", type=int, default=1)
     ap.add_argument("--no-fp64-form", action="store_true",
                     help="skip timing the FP64 form beside a mixed form (for kernel profiling runs)")
+    ap.add_argument("--nvtx-sweep", action="store_true",
+                    help="after the warm-up sweeps, run one sweep step by step inside the NVTX range 'sweep', "
+                         "print its time and exit (for an ncu launch list)")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="time the dominant kernel alone on the workload's J and R and exit (for a kernel profile)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -72,6 +72,12 @@ int64_t exafac_tree_node_count(int64_t n, int32_t F);
  * for leaves, pairwise sums above.  G is node_count x R x R. */
 int exafac_tree_build(int64_t n, int32_t F, int32_t R, const double* U_dev, double* G_dev, void* stream);
 
+/* The mixed forms' PartitionTree::build_tree from an FP32 copy of U (n x R,
+ * device): leaf Grams on the tensor cores (TF32 hi + lo parts, 32 <= R,
+ * F <= 128) or as compensated FP32 sums, internal sums in FP64; G as for
+ * exafac_tree_build. */
+int exafac_tree_build_f32(int64_t n, int32_t F, int32_t R, const float* U_dev, double* G_dev, void* stream);
+
 /* PartitionTree::PTSample (partition_tree.hpp:204-380): for each of J samples
  * descend by the quadratic forms x_j^T G x_j with the explicit uniform
  * draws_dev[j]; write the chosen row to rows_out_dev[j * rows_stride] and

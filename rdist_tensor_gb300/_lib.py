@@ -54,6 +54,7 @@ SIGNATURES = {
     "exafac_tree_build": (ctypes.c_int, [_I64, _I32, _I32, _P, _P, _P]),
     "exafac_tree_sample": (ctypes.c_int, [_I64, _I32, _I32, _P, _P, _I64, _P, _P, _P, _P, _I64, _P]),
     "exafac_quad_forms_f32": (ctypes.c_int, [_I32, _I64, _P, _P, _P, _P, _I32, _P]),
+    "exafac_tree_build_f32": (ctypes.c_int, [_I64, _I32, _I32, _P, _P, _P]),
     "exafac_syev": (ctypes.c_int, [_I32, _P, _P, _P, _P, _SZ, _P]),
     "exafac_pinv_square": (ctypes.c_int, [_I32, _P, _P, ctypes.c_double, _P, _SZ, _P]),
     "exafac_dense_workspace_bytes": (_SZ, [_I32]),

@@ -133,45 +133,53 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
 // A block takes 128 consecutive slots (the MMA's M).  For each run of equal
 // node in them it forms Y = X B^T (128 x N) with tcgen05.mma, FP32
 // accumulators in tensor memory, and reads each sample's row back in the warps
-// that own its TMEM lane: B is the node's R x R Gram for a level (the form
-// q = sum_c Y[c] x[c]), the leaf's F rows of U for the leaf stage (Y[r] =
-// U_r . x, the squared dots and their prefix).  FP32 accuracy from TF32
-// inputs by the split x = x_hi + x_lo, B = B_hi + B_lo (each part rounded to
-// TF32): Y ~ X_hi B_hi + X_hi B_lo + X_lo B_hi (relative error ~2^-21 of
-// |X| |B|, as FP32 sums of R products).  Operands are staged by the block's
-// threads into the K-major layout of umma.cuh: the slots' vectors once per
-// tile (hi and lo, 128 x Rk), B in K chunks of at most 64 (hi and lo,
-// Rn x KC), a node read from its packed FP32 copy.  Rows of a run's MMA that
-// belong to other runs are computed and ignored.  Every wait on the MMA
-// barrier is bounded; a wait that runs out records EXAFAC_ERR_TIMEOUT, and
-// the block waits once more (bounded) for its MMAs, frees its tensor memory
-// and leaves.
+// that own its TMEM lane.  Operands are split into TF32 parts, v = v_hi +
+// v_lo (each rounded to TF32), for FP32 accuracy:
+// - a level: B = the node's R x R Gram A, symmetric.  Y = X_hi (A_hi + A_lo)
+//   ~ A x_hi, and q = sum_c Y[c] (x_hi[c] + 2 x_lo[c]) = x^T A x - x_lo^T A
+//   x_lo: two MMAs per K step, no x_lo tile, error ~2^-22 of x^T |A| x plus
+//   the FP32 sums (x re-read from L2 for the sum);
+// - the leaf stage: B = the leaf's F rows of U, Y[r] = U_r . x ~ X_hi U_hi +
+//   X_hi U_lo + X_lo U_hi (three MMAs per K step), then the squared dots and
+//   their prefix.
+// Operands are staged by the block's threads into the K-major layout of
+// umma.cuh: the slots' vectors once per tile (128 x Rk), B in K chunks (Rn x
+// KC; 32 for a level, so that a level block's ~100 KB of shared memory lets
+// two blocks share an SM, 64 for the leaf stage), a node read from its packed
+// FP32 copy.  Rows of a run's MMA that belong to other runs are computed and
+// ignored.  Every wait on the MMA barrier is bounded; a wait that runs out
+// records EXAFAC_ERR_TIMEOUT, and the block waits once more (bounded) for its
+// MMAs, frees its tensor memory and leaves.
 // ---------------------------------------------------------------------------
 constexpr int kTcRows = 128;
 constexpr int kTcThreads = 256;
-constexpr int kTcKChunk = 64;
 constexpr int kTcMinRank = 32;
 
 struct TcLayout {
-    int Rk, Rn, KC;    // K and N padded to 16 (the epilogue reads the slot tile over Y's N columns), K chunk
-    uint32_t a_bytes;  // one slot tile (hi or lo): 128 x Rk
+    int Rk, Rn, KC;    // K and N padded to 16, K chunk of B
+    bool split_a;      // an x_lo tile (the leaf stage) or not (a level)
+    uint32_t a_bytes;  // one slot tile: 128 x Rk
     uint32_t b_bytes;  // one B chunk (hi or lo): Rn x KC
     uint32_t ncols;    // TMEM columns (power of two >= Rn)
 };
-__host__ __device__ inline TcLayout tc_layout(int R) {
+__host__ __device__ inline TcLayout tc_layout(int R, bool split_a) {
     TcLayout L;
     L.Rn = (R + 15) & ~15;
     L.Rk = L.Rn;
-    L.KC = L.Rk < kTcKChunk ? L.Rk : kTcKChunk;
+    const int kc = split_a ? 64 : 32;
+    L.KC = L.Rk < kc ? L.Rk : kc;
+    L.split_a = split_a;
     L.a_bytes = (uint32_t)kTcRows * (uint32_t)L.Rk * 4u;
     L.b_bytes = (uint32_t)L.Rn * (uint32_t)L.KC * 4u;
     L.ncols = L.Rn <= 32 ? 32u : (L.Rn <= 64 ? 64u : (L.Rn <= 128 ? 128u : 256u));
     return L;
 }
-size_t bfs_level_tc_smem(int R) {
-    const TcLayout L = tc_layout(R);
-    return 2 * (size_t)L.a_bytes + 2 * (size_t)L.b_bytes + 1024;  // + alignment of the base to 1 KB
+static size_t tc_smem(int R, bool split_a) {  // + alignment of the base to 1 KB
+    const TcLayout L = tc_layout(R, split_a);
+    return (split_a ? 2 : 1) * (size_t)L.a_bytes + 2 * (size_t)L.b_bytes + 1024;
 }
+size_t bfs_level_tc_smem(int R) { return tc_smem(R, false); }
+size_t bfs_leaf_tc_smem(int R) { return tc_smem(R, true); }
 
 // Byte offset of element (r, k) in a K-major tile with 8-row groups sbo bytes apart.
 __device__ __forceinline__ uint32_t kmajor_off(int r, int k, uint32_t sbo) {
@@ -181,22 +189,22 @@ __device__ __forceinline__ uint32_t kmajor_off(int r, int k, uint32_t sbo) {
 // The block's tensor-core state: operand tiles, TMEM accumulator, MMA barrier.
 struct TcBlock {
     TcLayout L;
-    unsigned char *Ahi, *Alo, *Bhi, *Blo;
+    unsigned char *Ahi, *Alo, *Bhi, *Blo;  // Alo null for a level
     uint32_t sboA, sboB, tmem, idesc, phase, polls;
     uint64_t* bar;
     int* abort_flag;
 };
 
 // Allocates TMEM (warp 0), initialises the barrier; every thread returns the same state.
-__device__ __forceinline__ TcBlock tc_begin(int R, unsigned char* raw, uint64_t* bar, uint32_t* tmem_base,
-                                            int* abort_flag, uint32_t polls) {
+__device__ __forceinline__ TcBlock tc_begin(int R, bool split_a, unsigned char* raw, uint64_t* bar,
+                                            uint32_t* tmem_base, int* abort_flag, uint32_t polls) {
     TcBlock b;
-    b.L = tc_layout(R);
+    b.L = tc_layout(R, split_a);
     unsigned char* base = raw + ((1024u - (smem_u32(raw) & 1023u)) & 1023u);
     b.Ahi = base;
-    b.Alo = base + b.L.a_bytes;
-    b.Bhi = base + 2 * b.L.a_bytes;
-    b.Blo = base + 2 * b.L.a_bytes + b.L.b_bytes;
+    b.Alo = split_a ? base + b.L.a_bytes : nullptr;
+    b.Bhi = base + (split_a ? 2 : 1) * b.L.a_bytes;
+    b.Blo = b.Bhi + b.L.b_bytes;
     b.sboA = (uint32_t)b.L.Rk * 32u;
     b.sboB = (uint32_t)b.L.KC * 32u;
     b.idesc = umma_idesc_tf32(kTcRows, b.L.Rn);
@@ -235,83 +243,86 @@ __device__ __forceinline__ void tc_end(TcBlock& b, DeviceStatus* status, int whe
 
 // Staging loops issue all of a thread's loads of one round (kTcUnroll
 // 16-byte chunks) before converting and storing any: the sources are
-// gathers from L2 and HBM, and the block is the only one on its SM.
+// gathers from L2 and HBM.  The row index runs fastest across the threads:
+// rows of a core matrix are 16 bytes apart, so a warp's 16-byte stores fill 4
+// whole 128-byte wavefronts (with the K index fastest, the 32 stores would be
+// 128 bytes apart, all in the same banks).
 constexpr int kTcUnroll = 8;
 
-__device__ __forceinline__ void tc_store_split(unsigned char* hi_tile, unsigned char* lo_tile, uint32_t off, float4 v) {
-    float4 h, l;
-    h.x = tf32_rna(v.x);
-    h.y = tf32_rna(v.y);
-    h.z = tf32_rna(v.z);
-    h.w = tf32_rna(v.w);
-    l.x = tf32_rna(v.x - h.x);
-    l.y = tf32_rna(v.y - h.y);
-    l.z = tf32_rna(v.z - h.z);
-    l.w = tf32_rna(v.w - h.w);
-    *reinterpret_cast<float4*>(hi_tile + off) = h;
-    *reinterpret_cast<float4*>(lo_tile + off) = l;
+__device__ __forceinline__ float4 tf32_rna4(float4 v) {
+    return make_float4(tf32_rna(v.x), tf32_rna(v.y), tf32_rna(v.z), tf32_rna(v.w));
 }
 
-// The tile's slot vectors X[js[r]] (rows past n and columns past R zero), split hi + lo.
+// v rounded to TF32 into hi_tile and, when lo_tile is not null, the rounded
+// remainder into lo_tile.
+__device__ __forceinline__ void tc_store_split(unsigned char* hi_tile, unsigned char* lo_tile, uint32_t off, float4 v) {
+    const float4 h = tf32_rna4(v);
+    *reinterpret_cast<float4*>(hi_tile + off) = h;
+    if (lo_tile)
+        *reinterpret_cast<float4*>(lo_tile + off) =
+            tf32_rna4(make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w));
+}
+
+// x of a slot, columns k .. k + 3 (zero past R).
+__device__ __forceinline__ float4 load_x4(const float* __restrict__ xr, int k, int R, bool vec) {
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (k < R) {
+        if (vec) {
+            v = __ldg(reinterpret_cast<const float4*>(xr + k));
+        } else {
+            v.x = __ldg(xr + k);
+            if (k + 1 < R) v.y = __ldg(xr + k + 1);
+            if (k + 2 < R) v.z = __ldg(xr + k + 2);
+            if (k + 3 < R) v.w = __ldg(xr + k + 3);
+        }
+    }
+    return v;
+}
+
+// The tile's slot vectors X[js[r]] (rows past n and columns past R zero).
 __device__ __forceinline__ void tc_stage_slots(const TcBlock& b, int R, const float* __restrict__ X,
                                                const int32_t* js, int n) {
-    const int kq_per_row = b.L.Rk / 4;
-    const int total = kTcRows * kq_per_row;
+    const int total = kTcRows * (b.L.Rk / 4);
     const bool vec = (R & 3) == 0;  // rows start on 16-byte boundaries
     for (int e0 = 0; e0 < total; e0 += kTcThreads * kTcUnroll) {
         float4 v[kTcUnroll];
 #pragma unroll
         for (int u = 0; u < kTcUnroll; u++) {
             const int e = e0 + u * kTcThreads + threadIdx.x;
-            const int r = e / kq_per_row, k = 4 * (e - r * kq_per_row);
-            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (e < total && r < n && k < R) {
-                const float* xr = X + (int64_t)js[r] * R + k;
-                if (vec) {
-                    v[u] = __ldg(reinterpret_cast<const float4*>(xr));
-                } else {
-                    v[u].x = __ldg(xr);
-                    if (k + 1 < R) v[u].y = __ldg(xr + 1);
-                    if (k + 2 < R) v[u].z = __ldg(xr + 2);
-                    if (k + 3 < R) v[u].w = __ldg(xr + 3);
-                }
-            }
+            const int r = e & (kTcRows - 1), k = 4 * (e / kTcRows);
+            v[u] = (e < total && r < n) ? load_x4(X + (int64_t)js[r] * R, k, R, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < kTcUnroll; u++) {
             const int e = e0 + u * kTcThreads + threadIdx.x;
-            if (e < total) {
-                const int r = e / kq_per_row, kq = e - r * kq_per_row;
-                tc_store_split(b.Ahi, b.Alo, kmajor_off(r, 4 * kq, b.sboA), v[u]);
-            }
+            if (e < total) tc_store_split(b.Ahi, b.Alo, kmajor_off(e & (kTcRows - 1), 4 * (e / kTcRows), b.sboA), v[u]);
         }
     }
 }
 
-// Y (TMEM) = X B^T over all K chunks, B(nn, k .. k + 3) = load4(nn, k) for
-// nn < Rn, k < Rk a multiple of 4 (zero outside the matrix is the loader's
-// job).  Returns false (in every thread) when a wait ran out; the caller then
-// ends the block.
+// Y (TMEM) = X_hi (B_hi + B_lo)^T (+ X_lo B_hi^T with an x_lo tile) over all
+// K chunks, B(nn, k .. k + 3) = load4(nn, k) for nn < Rn, k < Rk a multiple
+// of 4 (zero outside the matrix is the loader's job).  Returns false (in
+// every thread) when a wait ran out; the caller then ends the block.
 template <typename Load4>
 __device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
     const int tid = threadIdx.x;
     for (int k0 = 0; k0 < b.L.Rk; k0 += b.L.KC) {
         const int kc = min(b.L.KC, b.L.Rk - k0);
-        const int kq_c = kc / 4;
-        const int total = b.L.Rn * kq_c;
+        const int total = b.L.Rn * (kc / 4);
         for (int e0 = 0; e0 < total; e0 += kTcThreads * kTcUnroll) {
             float4 v[kTcUnroll];
 #pragma unroll
             for (int u = 0; u < kTcUnroll; u++) {
                 const int e = e0 + u * kTcThreads + tid;
-                const int nn = e / kq_c, kq = e - nn * kq_c;
+                const int kq = e / b.L.Rn, nn = e - kq * b.L.Rn;
                 v[u] = e < total ? load4(nn, k0 + 4 * kq) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
 #pragma unroll
             for (int u = 0; u < kTcUnroll; u++) {
                 const int e = e0 + u * kTcThreads + tid;
                 if (e < total) {
-                    const int nn = e / kq_c, kq = e - nn * kq_c;
+                    const int kq = e / b.L.Rn, nn = e - kq * b.L.Rn;
                     tc_store_split(b.Bhi, b.Blo, kmajor_off(nn, 4 * kq, b.sboB), v[u]);
                 }
             }
@@ -323,11 +334,11 @@ __device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
             for (int s = 0; s < kc / 8; s++) {
                 const uint32_t aoff = (uint32_t)(k0 + 8 * s) * 32u;  // (k / 4) * 128
                 const uint32_t boff = (uint32_t)s * 256u;
-                const uint64_t ah = umma_desc(b.Ahi + aoff, 128u, b.sboA), al = umma_desc(b.Alo + aoff, 128u, b.sboA);
+                const uint64_t ah = umma_desc(b.Ahi + aoff, 128u, b.sboA);
                 const uint64_t bh = umma_desc(b.Bhi + boff, 128u, b.sboB), bl = umma_desc(b.Blo + boff, 128u, b.sboB);
                 umma_tf32(b.tmem, ah, bh, b.idesc, (k0 > 0 || s > 0) ? 1u : 0u);
                 umma_tf32(b.tmem, ah, bl, b.idesc, 1u);
-                umma_tf32(b.tmem, al, bh, b.idesc, 1u);
+                if (b.Alo) umma_tf32(b.tmem, umma_desc(b.Alo + aoff, 128u, b.sboA), bh, b.idesc, 1u);
             }
             umma_commit(b.bar);
         }
@@ -342,16 +353,8 @@ __device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
     return true;
 }
 
-// x of the slot in row `row` of the tile, columns c .. c + 3 (hi + lo).
-__device__ __forceinline__ float4 tc_slot_x4(const TcBlock& b, int row, int c) {
-    const uint32_t off = kmajor_off(row, c, b.sboA);
-    const float4 h = *reinterpret_cast<const float4*>(b.Ahi + off);
-    const float4 l = *reinterpret_cast<const float4*>(b.Alo + off);
-    return make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
-}
-
 template <int MODE>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 2)
     bfs_level_tc_kernel(int R, int Pf, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
                         const int32_t* __restrict__ order, int64_t* __restrict__ node, float2* __restrict__ lh,
                         float* __restrict__ mroot, const double* __restrict__ dv, uint32_t* __restrict__ flag,
@@ -363,8 +366,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    TcBlock b = tc_begin(R, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
+    TcBlock b = tc_begin(R, false, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const bool vec = (R & 3) == 0;
     const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t s0 = tile * kTcRows;
@@ -407,19 +411,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             {
                 // warp w reads lanes 32 (w % 4) .. + 31 (its rows); column
                 // blocks of 16 alternate between the two warp halves
+                // q = sum_c Y[c] (x_hi[c] + 2 x_lo[c]), x re-read (L2)
                 const int qw = w & 3, half = w >> 2;
                 const int row = qw * 32 + lane;
+                const float* xr = X + (int64_t)js[row < n ? row : 0] * R;
                 float part = 0.0f;
                 for (int cb = half; cb < b.L.Rn / 16; cb += 2) {
+                    float4 x[4];
+#pragma unroll
+                    for (int q4 = 0; q4 < 4; q4++)
+                        x[q4] = row < n ? load_x4(xr, cb * 16 + 4 * q4, R, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
                     float y[16];
                     tmem_ld16(b.tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(cb * 16), y);
 #pragma unroll
                     for (int q4 = 0; q4 < 4; q4++) {
-                        const float4 x = tc_slot_x4(b, row, cb * 16 + 4 * q4);
-                        part = fmaf(y[4 * q4 + 0], x.x, part);
-                        part = fmaf(y[4 * q4 + 1], x.y, part);
-                        part = fmaf(y[4 * q4 + 2], x.z, part);
-                        part = fmaf(y[4 * q4 + 3], x.w, part);
+                        const float4 h = tf32_rna4(x[q4]);
+                        part = fmaf(y[4 * q4 + 0], fmaf(2.0f, x[q4].x - h.x, h.x), part);
+                        part = fmaf(y[4 * q4 + 1], fmaf(2.0f, x[q4].y - h.y, h.y), part);
+                        part = fmaf(y[4 * q4 + 2], fmaf(2.0f, x[q4].z - h.z, h.z), part);
+                        part = fmaf(y[4 * q4 + 3], fmaf(2.0f, x[q4].w - h.w, h.w), part);
                     }
                 }
                 qpart[half][row] = part;
@@ -464,7 +474,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    TcBlock b = tc_begin(R, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
+    TcBlock b = tc_begin(R, true, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int F = (int)t.F;
     const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
@@ -778,7 +788,7 @@ static void bfs_set_smem_limits() {
     static bool done = false;  // host-side, per process: the attributes hold for every device's context
     if (done) return;
     const int lsm = (int)bfs_level_smem(kMaxRank), fsm = (int)bfs_leaf_smem(kMaxRank, kMaxRank);
-    const int tsm = (int)bfs_level_tc_smem(kMaxRank);
+    const int tsm = (int)bfs_level_tc_smem(kMaxRank), tlsm = (int)bfs_leaf_tc_smem(kMaxRank);
     cudaFuncSetAttribute(bfs_level_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
     cudaFuncSetAttribute(bfs_level_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
     cudaFuncSetAttribute(bfs_level_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lsm);
@@ -788,7 +798,7 @@ static void bfs_set_smem_limits() {
     cudaFuncSetAttribute(bfs_level_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     cudaFuncSetAttribute(bfs_level_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     cudaFuncSetAttribute(bfs_level_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
-    cudaFuncSetAttribute(bfs_leaf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+    cudaFuncSetAttribute(bfs_leaf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tlsm);
     done = true;
 }
 
@@ -800,7 +810,7 @@ static void bfs_level_launch(bool use_tc, int R, const float* G, const float* X,
                              DeviceStatus* status, uint32_t polls, cudaStream_t st) {
     const int Pf = packed_stride_f32(R);
     if (use_tc) {
-        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 2 * 152));
         bfs_level_tc_kernel<MODE><<<blocks, kTcThreads, bfs_level_tc_smem(R), st>>>(R, Pf, G, X, J, order, node, lh,
                                                                                   m, dv, flag, t, status, polls);
     } else {
@@ -850,9 +860,9 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
         lb = 2 * lb + 1;
         nl *= 2;
     }
-    if (t.F > 1 && tc && t.F <= tc_layout(R).Rn) {
+    if (t.F > 1 && tc && t.F <= tc_layout(R, true).Rn) {
         const unsigned tblocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
-        bfs_leaf_tc_kernel<<<tblocks, kTcThreads, bfs_level_tc_smem(R), st>>>(R, t, U, X, J, b.order[b.cur], b.node,
+        bfs_leaf_tc_kernel<<<tblocks, kTcThreads, bfs_leaf_tc_smem(R), st>>>(R, t, U, X, J, b.order[b.cur], b.node,
                                                                             b.lh, dv, s.N, col, s.samples, b.empty,
                                                                             s.status, polls);
     } else if (t.F > 1) {

@@ -93,6 +93,10 @@ __device__ __forceinline__ void report(DeviceStatus* st, int code, int where, lo
     }
 }
 
+// Polls of a device-side wait (a look-back status word, an MMA barrier)
+// before the wait is declared failed (EXAFAC_ERR_TIMEOUT).
+constexpr uint32_t kSpinLimit = 1u << 22;
+
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 

@@ -25,9 +25,6 @@ constexpr int kGuideBuckets = 1 << 16;   // buckets of the CDF guide tables (a p
 constexpr int kExpandChunk = 256;  // hits per warp chunk in the hit expansion
 constexpr int kSortEpochSlot = 14;  // counters[] slot of the row sort's look-back epoch
 constexpr int kRngSlot = 15;              // counters[] slot of the session's Philox counter
-// Polls of a look-back status word before the wait is declared failed
-// (EXAFAC_ERR_TIMEOUT); each poll after the 32nd sleeps ~64 ns.
-constexpr uint32_t kSpinLimit = 1u << 22;
 
 struct Slot1 {
     unsigned long long key;

@@ -591,7 +591,8 @@ int sts_refresh_f32(Session& s, int k, cudaStream_t st) {
 int sts_rebuild_tree(Session& s, int k, cudaStream_t st) {
     if (s.cfg.precision == EXAFAC_PREC_FP64) return launch_tree_build(s.rtree[k], s.R, s.F.U[k], s.treeG[k], st);
     EXAFAC_TRY(narrow_copy(s.F.U[k], s.Uf[k], s.dims[k] * s.R, st));
-    EXAFAC_TRY(launch_tree_build_f32(s.rtree[k], s.R, s.Uf[k], s.treeG[k], st));
+    const uint32_t polls = s.wait_polls ? s.wait_polls : kSpinLimit;
+    EXAFAC_TRY(launch_tree_build_f32(s.rtree[k], s.R, s.Uf[k], s.treeG[k], s.status, polls, st));
     return narrow_nodes(s.treeG[k], s.treeF[k], s.R, s.rtree[k].node_count, st);
 }
 

@@ -1,5 +1,6 @@
 // PartitionTree build and PTSample kernels (partition_tree.hpp:117-380).
 #include "tree.cuh"
+#include "umma.cuh"
 
 namespace exafac {
 
@@ -69,6 +70,128 @@ __global__ void tree_leaf_gram_f32_kernel(TreeShape t, int R, const float* __res
                 g[base + (b - a)] = (double)hi + (double)lo;
             }
         }
+    }
+}
+
+// Leaf Grams of the mixed forms on the tensor cores (32 <= R <= 128, F <=
+// 128): a block per leaf in turn, G_leaf = U_leaf^T U_leaf as one tcgen05.mma
+// product whose A and B operands are the same staged tile, row a = component
+// a over the leaf's rows (K-major: element (a, r) = U[leaf F + r][a], rows a
+// >= R and r >= the leaf's rows zero), split into TF32 hi + lo parts:
+// G ~ A_hi A_hi^T + A_hi A_lo^T + A_lo A_hi^T (relative error ~2^-21 of
+// |U|^T |U|, FP32 accumulation in tensor memory).  The mixed forms use the
+// tree only through its FP32 copy, so this accuracy is what they keep.  Warps
+// read back their TMEM lanes (row a) and write the packed upper triangle as
+// FP64 for the tree's FP64 internal sums.  The MMA barrier's waits are
+// bounded as in the descents.
+constexpr int kLeafTcThreads = 256;
+
+__global__ void __launch_bounds__(kLeafTcThreads, 1)
+    tree_leaf_gram_tc_kernel(TreeShape t, int R, const float* __restrict__ U, double* __restrict__ G,
+                             DeviceStatus* status, uint32_t polls) {
+    extern __shared__ __align__(16) unsigned char lg_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int F = (int)t.F;
+    const int Rn = (R + 15) & ~15, Fk = (F + 15) & ~15;
+    const uint32_t ncols = Rn <= 32 ? 32u : (Rn <= 64 ? 64u : 128u);
+    const uint32_t sbo = (uint32_t)Fk * 32u;     // 8-row groups of the 128 x Fk tile
+    const uint32_t tile_bytes = 128u * sbo / 8u;  // 128 x Fk x 4
+    unsigned char* Ahi = lg_raw + ((1024u - (smem_u32(lg_raw) & 1023u)) & 1023u);
+    unsigned char* Alo = Ahi + tile_bytes;
+    if (w == 0) tmem_alloc(&tmem_base, ncols);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = umma_idesc_tf32(128, Rn);
+    uint32_t phase = 0;
+    const int P = packed_size(R);
+    const int64_t first_leaf = t.node_count - t.leaf_count;
+    for (int64_t li = blockIdx.x; li < t.leaf_count; li += gridDim.x) {
+        const int64_t c = first_leaf + li;
+        const int64_t leaf = tree_leaf_idx(t, c);
+        const int rows = (int)((t.n - leaf * t.F) < t.F ? (t.n - leaf * t.F) : t.F);
+        const float* Ub = U + leaf * t.F * R;
+        __syncthreads();  // the previous leaf's MMAs and read-back are done with the tile
+        // element (a, r .. r + 3): lanes over a (coalesced loads of a row,
+        // 16-byte stores 16 bytes apart)
+        const int total = 128 * (Fk / 4);
+        for (int e = tid; e < total; e += kLeafTcThreads) {
+            const int a = e & 127, r0 = 4 * (e >> 7);
+            float v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) v[q] = (a < R && r0 + q < rows) ? __ldg(Ub + (int64_t)(r0 + q) * R + a) : 0.0f;
+            float4 h, l;
+            h.x = tf32_rna(v[0]);
+            h.y = tf32_rna(v[1]);
+            h.z = tf32_rna(v[2]);
+            h.w = tf32_rna(v[3]);
+            l.x = tf32_rna(v[0] - h.x);
+            l.y = tf32_rna(v[1] - h.y);
+            l.z = tf32_rna(v[2] - h.z);
+            l.w = tf32_rna(v[3] - h.w);
+            const uint32_t off = (uint32_t)(a >> 3) * sbo + (uint32_t)(r0 >> 2) * 128u + (uint32_t)(a & 7) * 16u;
+            *reinterpret_cast<float4*>(Ahi + off) = h;
+            *reinterpret_cast<float4*>(Alo + off) = l;
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            for (int s = 0; s < Fk / 8; s++) {
+                const uint32_t off = (uint32_t)s * 256u;
+                const uint64_t dh = umma_desc(Ahi + off, 128u, sbo), dl = umma_desc(Alo + off, 128u, sbo);
+                umma_tf32(tmem, dh, dh, idesc, s > 0 ? 1u : 0u);
+                umma_tf32(tmem, dh, dl, idesc, 1u);
+                umma_tf32(tmem, dl, dh, idesc, 1u);
+            }
+            umma_commit(&bar);
+        }
+        bool done = false;
+        for (uint32_t it = 0; it < polls && !done; it++) done = mbar_try_wait(&bar, phase);
+        if (!done) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) break;
+        phase ^= 1u;
+        tc_fence_after();
+        {
+            // warp w: lanes 32 (w % 4) .. + 31 = rows a; column blocks of 16
+            // alternate between the two warp halves
+            const int qw = w & 3, half = w >> 2;
+            const int a = qw * 32 + lane;
+            double* g = G + c * P;
+            for (int cb = half; cb < Rn / 16; cb += 2) {
+                float y[16];
+                tmem_ld16(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(cb * 16), y);
+                if (a < R) {
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int b = cb * 16 + q;
+                        if (b >= a && b < R) g[packed_index(R, a, b)] = (double)y[q];
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+    }
+    if (abort_flag) {
+        if (tid == 0) report(status, EXAFAC_ERR_TIMEOUT, 22, blockIdx.x, 0);
+        bool done = false;
+        for (uint32_t it = 0; it < polls && !done; it++) done = mbar_try_wait(&bar, phase);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
     }
 }
 
@@ -150,14 +273,23 @@ int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cud
     return EXAFAC_OK;
 }
 
-int launch_tree_build_f32(const TreeShape& t, int R, const float* U, double* G, cudaStream_t stream) {
+int launch_tree_build_f32(const TreeShape& t, int R, const float* U, double* G, DeviceStatus* status, uint32_t polls,
+                          cudaStream_t stream) {
     const int P = packed_size(R);
-    const size_t smem = sizeof(float) * t.F * R;
-    if (smem > 48 * 1024)
+    if (R >= 32 && t.F > 1 && t.F <= 128) {
+        const size_t smem = 2 * sizeof(float) * 128 * (size_t)((t.F + 15) & ~15) + 1024;
         EXAFAC_CUDA_TRY(
-            cudaFuncSetAttribute(tree_leaf_gram_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int blocks = (int)std::min<int64_t>(t.leaf_count, 152 * 4);
-    tree_leaf_gram_f32_kernel<<<blocks, 128, smem, stream>>>(t, R, U, G);
+            cudaFuncSetAttribute(tree_leaf_gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int blocks = (int)std::min<int64_t>(t.leaf_count, 152);
+        tree_leaf_gram_tc_kernel<<<blocks, kLeafTcThreads, smem, stream>>>(t, R, U, G, status, polls);
+    } else {
+        const size_t smem = sizeof(float) * t.F * R;
+        if (smem > 48 * 1024)
+            EXAFAC_CUDA_TRY(
+                cudaFuncSetAttribute(tree_leaf_gram_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int blocks = (int)std::min<int64_t>(t.leaf_count, 152 * 4);
+        tree_leaf_gram_f32_kernel<<<blocks, 128, smem, stream>>>(t, R, U, G);
+    }
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     int64_t start = t.nodes_before_lfill, end = t.node_count - t.leaf_count;
@@ -209,6 +341,12 @@ extern "C" int exafac_tree_build(int64_t n, int32_t F, int32_t R, const double* 
     EXAFAC_ARG(n >= 1 && F >= 1 && R >= 1 && R <= kMaxRank, "exafac_tree_build: bad shape");
     EXAFAC_ARG(U && G, "exafac_tree_build: null pointer");
     return launch_tree_build(make_tree_shape(n, F), R, U, G, (cudaStream_t)stream);
+}
+
+extern "C" int exafac_tree_build_f32(int64_t n, int32_t F, int32_t R, const float* U, double* G, void* stream) {
+    EXAFAC_ARG(n >= 1 && F >= 1 && R >= 1 && R <= kMaxRank, "exafac_tree_build_f32: bad shape");
+    EXAFAC_ARG(U && G, "exafac_tree_build_f32: null pointer");
+    return launch_tree_build_f32(make_tree_shape(n, F), R, U, G, nullptr, kSpinLimit, (cudaStream_t)stream);
 }
 
 extern "C" int exafac_tree_sample(int64_t n, int32_t F, int32_t R, const double* G, const double* U, int64_t J,

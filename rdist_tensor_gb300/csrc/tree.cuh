@@ -48,9 +48,12 @@ __host__ __device__ __forceinline__ int packed_index(int R, int a, int b) { retu
 
 // Builds the tree over U (n x R, row-major).  G: node_count * P doubles.
 int launch_tree_build(const TreeShape& t, int R, const double* U, double* G, cudaStream_t stream);
-// The same from an FP32 copy of U: leaf Grams as compensated FP32 sums of
-// exactly split products (about 48 bits), internal sums in FP64.
-int launch_tree_build_f32(const TreeShape& t, int R, const float* U, double* G, cudaStream_t stream);
+// The same from an FP32 copy of U, internal sums in FP64; leaf Grams on the
+// tensor cores in TF32 hi + lo parts for 32 <= R, F <= 128 (waits bounded by
+// `polls`, a timeout recorded in *status), else as compensated FP32 sums of
+// exactly split products (about 48 bits).
+int launch_tree_build_f32(const TreeShape& t, int R, const float* U, double* G, DeviceStatus* status, uint32_t polls,
+                          cudaStream_t stream);
 
 // Multiplies every node elementwise by the symmetric matrix M (R x R full)
 // (multiply_matrices_against_provided, partition_tree.hpp:176-187).

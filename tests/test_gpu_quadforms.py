@@ -89,3 +89,31 @@ def test_quad_forms_repeat(lib):
                  ctypes.c_void_p(Gd.data_ptr()), ctypes.c_void_p(q.data_ptr()), 1, None)
         res.append(q.cpu().numpy())
     assert np.array_equal(res[0], res[1])
+
+
+@pytest.mark.parametrize("R", [16, 48, 128])
+def test_tree_build_f32(lib, R):
+    """The mixed forms' tree build from the FP32 factor copy against the FP64
+    build of the same values (PartitionTree::build_tree,
+    partition_tree.hpp:117-167): every packed node entry within 2e-6 (tensor
+    cores, R >= 32: TF32 hi + lo parts) or 1e-12 (compensated FP32 sums,
+    R < 32) of the same entry of the tree of |U|.  1000 rows, F = R rows per
+    leaf (partial last leaf)."""
+    rng = np.random.default_rng(R + 1)
+    n, F = 1000, R
+    U32 = rng.standard_normal((n, R)).astype(np.float32)
+    U64 = U32.astype(np.float64)
+    nodes = lib.load().exafac_tree_node_count(n, F)
+    P = R * (R + 1) // 2
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a)).cuda()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    out = {}
+    for name, U in (("f32", dev(U32)), ("f64", dev(U64)), ("abs", dev(np.abs(U64)))):
+        G = torch.zeros((nodes, P), dtype=torch.float64, device="cuda")
+        fn = "exafac_tree_build_f32" if name == "f32" else "exafac_tree_build"
+        lib.call(fn, n, F, R, ptr(U), ptr(G), None)
+        torch.cuda.synchronize()
+        out[name] = G.cpu().numpy()
+    err = np.max(np.abs(out["f32"] - out["f64"]) / np.maximum(out["abs"], 1e-300))
+    print(f"R={R}: max error / |U|^T|U| = {err:.2e}")
+    assert err < (2e-6 if R >= 32 else 1e-12)
