@@ -89,11 +89,11 @@ int exafac_tree_sample(int64_t n, int32_t F, int32_t R, const double* G_dev, con
 /* The quadratic forms of the mixed forms' breadth-first STS-CP descents
  * (the per-level node masses of PartitionTree::PTSample,
  * partition_tree.hpp:204-380, in FP32): q[j] = x_j^T G_{node[j]} x_j for J
- * FP32 vectors (J x R, device) and node indices into G (packed upper
- * triangles, rows in order, node stride (R (R + 1) / 2 rounded up to a
- * multiple of 4) floats).  use_tc = 1: on the tensor cores (tcgen05, TF32
- * split into hi + lo parts, R >= 32); 0: FP32 on the CUDA cores.  Slots of
- * equal node next to each other share one staging of the node. */
+ * FP32 vectors (J x R, device) and node indices into G, packed upper
+ * triangles (rows in order, node stride R (R + 1) / 2 rounded up to a
+ * multiple of 4 floats).  use_tc = 1 (R >= 32): on the tensor cores
+ * (tcgen05); 0: FP32 on the CUDA cores.  Slots of equal node next to each
+ * other share one staging of the node. */
 int exafac_quad_forms_f32(int32_t R, int64_t J, const float* X_dev, const int64_t* node_dev, const float* G_dev,
                           float* q_dev, int32_t use_tc, void* stream);
 

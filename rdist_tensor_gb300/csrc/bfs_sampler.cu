@@ -153,7 +153,6 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
 // ---------------------------------------------------------------------------
 constexpr int kTcRows = 128;
 constexpr int kTcThreads = 256;
-constexpr int kTcMinRank = 32;
 
 struct TcLayout {
     int Rk, Rn, KC;    // K and N padded to 16, K chunk of B
@@ -178,7 +177,6 @@ static size_t tc_smem(int R, bool split_a) {  // + alignment of the base to 1 KB
     const TcLayout L = tc_layout(R, split_a);
     return (split_a ? 2 : 1) * (size_t)L.a_bytes + 2 * (size_t)L.b_bytes + 1024;
 }
-size_t bfs_level_tc_smem(int R) { return tc_smem(R, false); }
 size_t bfs_leaf_tc_smem(int R) { return tc_smem(R, true); }
 
 // Byte offset of element (r, k) in a K-major tile with 8-row groups sbo bytes apart.
@@ -230,8 +228,7 @@ __device__ __forceinline__ TcBlock tc_begin(int R, bool split_a, unsigned char* 
 __device__ __forceinline__ void tc_end(TcBlock& b, DeviceStatus* status, int where) {
     if (*b.abort_flag) {
         if (threadIdx.x == 0) report(status, EXAFAC_ERR_TIMEOUT, where, blockIdx.x, 0);
-        bool done = false;
-        for (uint32_t it = 0; it < b.polls && !done; it++) done = mbar_try_wait(b.bar, b.phase);
+        mbar_wait_limited(b.bar, b.phase, b.polls);
     }
     tc_fence_before();
     __syncthreads();
@@ -342,9 +339,8 @@ __device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
             }
             umma_commit(b.bar);
         }
-        bool done = false;  // the MMAs have read the chunk (and, after the last, written Y)
-        for (uint32_t it = 0; it < b.polls && !done; it++) done = mbar_try_wait(b.bar, b.phase);
-        if (!done) *b.abort_flag = 1;
+        // the MMAs have read the chunk (and, after the last, written Y)
+        if (!mbar_wait_limited(b.bar, b.phase, b.polls)) *b.abort_flag = 1;
         __syncthreads();
         if (*b.abort_flag) return false;
         b.phase ^= 1u;
@@ -353,107 +349,327 @@ __device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
     return true;
 }
 
+// ---- the level kernel: swizzled operands, packed nodes expanded in shared memory
+
+// Level-kernel shapes: N = round16(R) rows of B, K = round32(R) in blocks of
+// 32 FP32 values (one 128-byte swizzle row).
+struct TcLevelShape {
+    int Rn, Rk, nkb, Pf;
+    uint32_t a_kb;   // bytes of one K block of the slot tile: 128 rows x 128
+    uint32_t b_kb;   // bytes of one K block of one part (hi or lo) of the node: Rn x 128
+    uint32_t pk;     // bytes of the packed node buffer (Pf floats, rounded up to 1 KB)
+    uint32_t ncols;  // TMEM columns
+};
+__host__ __device__ inline TcLevelShape tc_level_shape(int R) {
+    TcLevelShape L;
+    L.Rn = (R + 15) & ~15;
+    L.Rk = (R + 31) & ~31;
+    L.nkb = L.Rk / 32;
+    L.Pf = packed_stride_f32(R);
+    L.a_kb = 128u * 128u;
+    L.b_kb = (uint32_t)L.Rn * 128u;
+    L.pk = ((uint32_t)L.Pf * 4u + 1023u) & ~1023u;
+    L.ncols = L.Rn <= 32 ? 32u : (L.Rn <= 64 ? 64u : 128u);
+    return L;
+}
+// Two slot buffers (this tile's, the next tile's in flight), the packed node,
+// one node K block (hi and lo parts), 1 KB alignment slack.
+size_t bfs_level_tc_smem(int R) {
+    const TcLevelShape L = tc_level_shape(R);
+    return 2 * (size_t)L.nkb * L.a_kb + L.pk + 2 * (size_t)L.b_kb + 1024;
+}
+
+constexpr int kTcLevelThreads = 512;
+
+// The slot vectors X[js[r]] of a tile into a swizzled slot buffer by 16-byte
+// asynchronous copies (4-byte ones when rows are not 16-byte aligned), zero
+// past R and past the tile's n slots.  The raw FP32 values are the MMA's A
+// operand: the tensor core reads an FP32 value as TF32 by dropping its low
+// 13 mantissa bits (measured on GB300: the forms from truncated inputs match
+// FP64 to ~2.5e-7 of x^T |A| x, from rounded inputs only to ~1.5e-4), so the
+// read-back takes x_hi = x with those bits cleared.  One commit group.
+__device__ __forceinline__ void tc_issue_slots(unsigned char* A, const float* __restrict__ X, const int32_t* js,
+                                               int n, int R, const TcLevelShape& L) {
+    const int kqr = L.Rk / 4;
+    const bool vec = (R & 3) == 0;
+    for (int e = threadIdx.x; e < kTcRows * kqr; e += kTcLevelThreads) {
+        const int r = e / kqr, k = 4 * (e - r * kqr);
+        unsigned char* dst = A + sw128_off(r, k, L.a_kb);
+        const float* row = X + (int64_t)js[r < n ? r : 0] * R;
+        if (vec) {
+            const bool live = r < n && k < R;
+            cp_async16(dst, live ? row + k : X, live ? 16u : 0u);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const bool live = r < n && k + q < R;
+                cp_async4(dst + 4 * q, live ? row + k + q : X, live ? 4u : 0u);
+            }
+        }
+    }
+    cp_async_commit();
+}
+
+// K block kb of the packed node in shared memory as the B operand: rows n <
+// Rn, columns 32 kb .. 32 kb + 31 of the full symmetric matrix, split into
+// TF32 hi and lo parts (the row index fastest: conflict-free swizzled stores).
+__device__ __forceinline__ void tc_expand_kblock(const float* Pk, int R, int kb, unsigned char* Bhi,
+                                                 unsigned char* Blo, const TcLevelShape& L) {
+    for (int e = threadIdx.x; e < L.Rn * 8; e += kTcLevelThreads) {
+        const int c = e / L.Rn, n = e - c * L.Rn;
+        const int k0 = kb * 32 + 4 * c;
+        float v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = k0 + q;
+            v[q] = (n < R && k < R) ? Pk[n <= k ? packed_index(R, n, k) : packed_index(R, k, n)] : 0.0f;
+        }
+        const uint32_t off = (uint32_t)n * 128u + (((uint32_t)c ^ ((uint32_t)n & 7u)) * 16u);
+        tc_store_split(Bhi, Blo, off, make_float4(v[0], v[1], v[2], v[3]));
+    }
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(kTcThreads, 2)
-    bfs_level_tc_kernel(int R, int Pf, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
+__global__ void __launch_bounds__(kTcLevelThreads, 1)
+    bfs_level_tc_kernel(int R, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
                         const int32_t* __restrict__ order, int64_t* __restrict__ node, float2* __restrict__ lh,
                         float* __restrict__ mroot, const double* __restrict__ dv, uint32_t* __restrict__ flag,
                         TreeShape t, DeviceStatus* status, uint32_t wait_polls) {
     extern __shared__ __align__(16) unsigned char tc_raw[];
-    __shared__ int64_t cs[kTcRows];
-    __shared__ int32_t js[kTcRows];
-    __shared__ float qpart[2][kTcRows];
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ int32_t cs2[2][kTcRows];  // current node of each slot (node counts < 2^31)
+    __shared__ int32_t js2[2][kTcRows];  // sample of each slot
+    __shared__ float qpart[4][kTcRows];
+    __shared__ __align__(8) uint64_t bars[2];  // [0] packed node copy, [1] MMAs
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    TcBlock b = tc_begin(R, false, tc_raw, &bar, &tmem_base, &abort_flag, wait_polls);
+    const TcLevelShape L = tc_level_shape(R);
+    unsigned char* base = tc_raw + ((1024u - (smem_u32(tc_raw) & 1023u)) & 1023u);
+    unsigned char* Abuf[2] = {base, base + L.nkb * L.a_kb};
+    float* Pk = reinterpret_cast<float*>(base + 2 * L.nkb * L.a_kb);
+    unsigned char* Bhi = base + 2 * L.nkb * L.a_kb + L.pk;
+    unsigned char* Blo = Bhi + L.b_kb;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    const bool vec = (R & 3) == 0;
-    const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t s0 = tile * kTcRows;
-        const int n = (int)min((int64_t)kTcRows, J - s0);
-        __syncthreads();  // the previous tile is done with cs / js and the slot tiles
-        for (int i = tid; i < n; i += kTcThreads) {
-            const int32_t j = order ? order[s0 + i] : (int32_t)(s0 + i);
-            js[i] = j;
-            cs[i] = MODE == 0 ? 0 : node[j];
+    if (w == 0) tmem_alloc(&tmem_base, L.ncols);
+    if (tid == 0) {
+        mbar_init(&bars[0], kTcLevelThreads);  // every thread's node copies
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = umma_idesc_tf32(kTcRows, L.Rn);
+    // the packed-node buffer (state kept alike by every thread) and, in
+    // thread 0, the MMA barrier's phase
+    uint32_t fphase = 0, mphase = 0;
+    int64_t pk_node = -1;  // node in (or on its way to) Pk
+    bool pk_flight = false;
+    // one node into Pk: 16-byte asynchronous copies by every thread, each
+    // thread's landing signalled on bars[0] (a single bulk copy of a packed
+    // node was measured to land ~8 us after issue, these in time)
+    auto issue_node = [&](int64_t g) {
+        const float4* src = reinterpret_cast<const float4*>(G + g * L.Pf);
+        for (int e = tid; e < L.Pf / 4; e += kTcLevelThreads) cp_async16(Pk + 4 * e, src + e, 16u);
+        cp_async_arrive(&bars[0]);
+        pk_node = g;
+        pk_flight = true;
+    };
+    auto land_node = [&]() -> bool {  // the copy in flight has landed
+        if (!pk_flight) return true;
+        pk_flight = false;
+        if (!mbar_wait_limited(&bars[0], fphase, wait_polls)) return false;
+        fphase ^= 1u;
+        return true;
+    };
+    // the node whose Gram a run of current node c multiplies, or -1 for a leaf that stays
+    auto run_node = [&](int64_t c) -> int64_t {
+        if (MODE == 2 && tree_is_leaf(t, c)) return -1;
+        return MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1);
+    };
+    // the first run needing an MMA among slots [from, n) of a header, or -1
+    auto next_run_node = [&](const int32_t* cs, int from, int n) -> int64_t {
+        int i = from;
+        while (i < n) {
+            const int64_t g = run_node(cs[i]);
+            if (g >= 0) return g;
+            const int32_t c = cs[i];
+            while (i < n && cs[i] == c) i++;
         }
+        return -1;
+    };
+    const int64_t ntiles = (J + kTcRows - 1) / kTcRows;
+    const int64_t stride = gridDim.x;
+    auto tile_n = [&](int64_t tile) -> int { return (int)min((int64_t)kTcRows, J - tile * kTcRows); };
+    // header registers: slot tid of a tile two ahead (threads < 128)
+    int32_t hj = 0, hc = 0;
+    // prologue: the headers of the first two tiles, the first tile's slot copies
+    for (int b = 0; b < 2; b++) {
+        const int64_t tile = blockIdx.x + b * stride;
+        if (tile < ntiles && tid < tile_n(tile)) {
+            const int32_t j = order ? order[tile * kTcRows + tid] : (int32_t)(tile * kTcRows + tid);
+            js2[b][tid] = j;
+            cs2[b][tid] = MODE == 0 ? 0 : (int32_t)node[j];
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x < ntiles) tc_issue_slots(Abuf[0], X, js2[0], tile_n(blockIdx.x), R, L);
+    int it = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += stride, it++) {
+        const int a = it & 1;
+        const int64_t s0 = tile * kTcRows;
+        const int n = tile_n(tile);
+        const int32_t* cs = cs2[a];
+        const int32_t* js = js2[a];
+        const int64_t t1 = tile + stride, t2 = tile + 2 * stride;
+        // the next tile's slot copies (its header is in [a ^ 1]), in flight during this tile
+        if (t1 < ntiles) tc_issue_slots(Abuf[a ^ 1], X, js2[a ^ 1], tile_n(t1), R, L);
+        else cp_async_commit();  // an empty group keeps the count
+        // the header two tiles ahead into registers (its node reads follow below)
+        const bool h_live = t2 < ntiles && tid < tile_n(t2);
+        if (h_live) hj = order ? order[t2 * kTcRows + tid] : (int32_t)(t2 * kTcRows + tid);
+        // this tile's decision inputs (thread i = slot i)
+        float2 pl = make_float2(0.f, 0.f);
+        float pm = 1.0f;
+        double pd = 0.0;
+        if ((MODE == 1 || MODE == 2) && tid < n) {
+            const int32_t j = js[tid];
+            pl = lh[j];
+            pm = mroot[j];
+            pd = dv[j];
+        }
+        {  // the first run's node, if not already there
+            const int64_t g = next_run_node(cs, 0, n);
+            if (g >= 0 && g != pk_node) {
+                if (!land_node()) abort_flag = 1;
+                else issue_node(g);
+            }
+        }
+        cp_async_wait<1>();        // this tile's slot copies (all groups but the newest)
+        fence_proxy_async_smem();  // the slot tile, to the tensor core's proxy
         __syncthreads();
-        tc_stage_slots(b, R, X, js, n);
+        if (abort_flag) goto fail;
+        if (h_live) hc = MODE == 0 ? 0 : (int32_t)node[hj];
+        unsigned char* A = Abuf[a];
         for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
-            const int64_t c = cs[i0];
+            const int32_t c = cs[i0];
             int i1 = i0 + 1;
             while (i1 < n && cs[i1] == c) i1++;
-            if (MODE == 2 && tree_is_leaf(t, c)) {
-                for (int i = i0 + tid; i < i1; i += kTcThreads) flag[s0 + i] = 1u;
+            const int64_t g = run_node(c);
+            if (g < 0) {
+                if (tid >= i0 && tid < i1) flag[s0 + tid] = 1u;
                 i0 = i1;
                 continue;
             }
-            const int64_t g = MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1);
-            const float* Gn = G + g * Pf;
-            // the node (symmetric: row nn of B = row nn of A)
-            const bool ok = tc_product(b, [&](int nn, int k) -> float4 {
-                float a[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int kk = k + q;
-                    a[q] = (nn < R && kk < R)
-                               ? __ldg(Gn + (nn <= kk ? packed_index(R, nn, kk) : packed_index(R, kk, nn)))
-                               : 0.0f;
+            {  // the run's node in Pk
+                bool ok = true;
+                if (pk_node != g) {
+                    ok = land_node();
+                    if (ok) issue_node(g);
                 }
-                return make_float4(a[0], a[1], a[2], a[3]);
-            });
-            if (!ok) {
-                tc_end(b, status, 20);
-                return;
+                if (ok) ok = land_node();
+                if (!ok) abort_flag = 1;
             }
-            {
-                // warp w reads lanes 32 (w % 4) .. + 31 (its rows); column
-                // blocks of 16 alternate between the two warp halves
-                // q = sum_c Y[c] (x_hi[c] + 2 x_lo[c]), x re-read (L2)
-                const int qw = w & 3, half = w >> 2;
-                const int row = qw * 32 + lane;
-                const float* xr = X + (int64_t)js[row < n ? row : 0] * R;
-                float part = 0.0f;
-                for (int cb = half; cb < b.L.Rn / 16; cb += 2) {
-                    float4 x[4];
+            __syncthreads();
+            if (abort_flag) goto fail;
+            for (int kb = 0; kb < L.nkb; kb++) {
+                tc_expand_kblock(Pk, R, kb, Bhi, Blo, L);
+                fence_proxy_async_smem();  // the K block, to the tensor core's proxy
+                __syncthreads();
+                if (kb + 1 == L.nkb) {  // Pk is free: the next run's node
+                    int64_t g2 = next_run_node(cs, i1, n);
+                    if (g2 < 0 && t1 < ntiles) g2 = next_run_node(cs2[a ^ 1], 0, tile_n(t1));
+                    if (g2 >= 0 && g2 != g) issue_node(g2);
+                }
+                if (tid == 0) {
+                    tc_fence_after();
 #pragma unroll
-                    for (int q4 = 0; q4 < 4; q4++)
-                        x[q4] = row < n ? load_x4(xr, cb * 16 + 4 * q4, R, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int sub = 0; sub < 4; sub++) {
+                        const uint64_t ad = umma_desc_sw128(A + kb * L.a_kb + sub * 32);
+                        umma_tf32(tmem, ad, umma_desc_sw128(Bhi + sub * 32), idesc, (kb > 0 || sub > 0) ? 1u : 0u);
+                        umma_tf32(tmem, ad, umma_desc_sw128(Blo + sub * 32), idesc, 1u);
+                    }
+                    umma_commit(&bars[1]);
+                    if (!mbar_wait_limited(&bars[1], mphase, wait_polls)) abort_flag = 1;
+                    mphase ^= 1u;
+                }
+                __syncthreads();  // the MMAs are done with the K block (and, after the last, Y is written)
+                if (abort_flag) goto fail;
+            }
+            tc_fence_after();
+            {
+                // q = sum_c Y[c] (x_hi[c] + 2 x_lo[c]) with x_hi = x truncated
+                // to TF32 (what the MMA used); warp w reads lanes 32 (w % 4)
+                // .. + 31, column blocks of 16 shared by the four warps of a
+                // lane quarter
+                const int qw = w & 3, part = w >> 2;
+                const int row = qw * 32 + lane;
+                float acc = 0.0f;
+                for (int cb = part; cb < L.Rn / 16; cb += 4) {
                     float y[16];
-                    tmem_ld16(b.tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(cb * 16), y);
+                    tmem_ld16(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(cb * 16), y);
 #pragma unroll
                     for (int q4 = 0; q4 < 4; q4++) {
-                        const float4 h = tf32_rna4(x[q4]);
-                        part = fmaf(y[4 * q4 + 0], fmaf(2.0f, x[q4].x - h.x, h.x), part);
-                        part = fmaf(y[4 * q4 + 1], fmaf(2.0f, x[q4].y - h.y, h.y), part);
-                        part = fmaf(y[4 * q4 + 2], fmaf(2.0f, x[q4].z - h.z, h.z), part);
-                        part = fmaf(y[4 * q4 + 3], fmaf(2.0f, x[q4].w - h.w, h.w), part);
+                        const float4 x = *reinterpret_cast<const float4*>(A + sw128_off(row, cb * 16 + 4 * q4, L.a_kb));
+                        const float xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                        for (int qq = 0; qq < 4; qq++) {
+                            const float h = __uint_as_float(__float_as_uint(xs[qq]) & 0xFFFFE000u);
+                            acc = fmaf(y[4 * q4 + qq], fmaf(2.0f, xs[qq] - h, h), acc);
+                        }
                     }
                 }
-                qpart[half][row] = part;
+                qpart[part][row] = acc;
             }
             tc_fence_before();
             __syncthreads();
-            for (int i = i0 + tid; i < i1; i += kTcThreads) {
-                const float q = qpart[0][i] + qpart[1][i];
-                const int32_t j = js[i];
+            if (tid >= i0 && tid < i1) {  // slot tid, with its prefetched inputs
+                const float q = (qpart[0][tid] + qpart[1][tid]) + (qpart[2][tid] + qpart[3][tid]);
+                const int32_t j = js[tid];
                 if (MODE == 0 || MODE == 3) {
                     mroot[j] = q;
                 } else {
-                    const float2 bnd = lh[j];
-                    const float cutoff = bnd.x + q / mroot[j];
-                    const bool left = (float)dv[j] <= cutoff;
-                    node[j] = left ? 2 * c + 1 : 2 * c + 2;
-                    lh[j] = left ? make_float2(bnd.x, cutoff) : make_float2(cutoff, bnd.y);
-                    flag[s0 + i] = left ? 1u : 0u;
+                    const float cutoff = pl.x + q / pm;
+                    const bool left = (float)pd <= cutoff;
+                    node[j] = left ? 2 * (int64_t)c + 1 : 2 * (int64_t)c + 2;
+                    lh[j] = left ? make_float2(pl.x, cutoff) : make_float2(cutoff, pl.y);
+                    flag[s0 + tid] = left ? 1u : 0u;
                 }
             }
             i0 = i1;
         }
+        __syncthreads();  // this tile is done with js2 / cs2 [a] and Abuf[a]
+        if (h_live) {
+            js2[a][tid] = hj;
+            cs2[a][tid] = hc;
+        }
+        __syncthreads();
     }
-    tc_end(b, status, 20);
+    cp_async_wait<0>();
+    if (!land_node()) abort_flag = 1;  // a prefetched node no run used
+    __syncthreads();
+    if (abort_flag) goto fail;
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L.ncols);
+    }
+    return;
+fail:
+    cp_async_wait<0>();  // this thread's copies (the node's included) have landed
+    if (tid == 0) {
+        report(status, EXAFAC_ERR_TIMEOUT, 20, blockIdx.x, 0);
+        // the MMAs in flight may still complete: wait once more (bounded)
+        mbar_wait_limited(&bars[1], mphase, wait_polls);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L.ncols);
+    }
 }
 
 // Leaf stage on the tensor cores (F > 1, F <= Rn): Y[r] = U_r . x for the
@@ -802,17 +1018,18 @@ static void bfs_set_smem_limits() {
     done = true;
 }
 
-// One level (MODE as bfs_level_kernel) over slots order[0 .. J): on the
-// tensor cores for R >= kTcMinRank (use_tc), else on the CUDA cores.
+// One level (MODE as bfs_level_kernel) over slots order[0 .. J) of the packed
+// FP32 nodes G: on the tensor cores when use_tc (R >= kTcMinRank), else on
+// the CUDA cores.
 template <int MODE>
 static void bfs_level_launch(bool use_tc, int R, const float* G, const float* X, int64_t J, const int32_t* order,
                              int64_t* node, float2* lh, float* m, const double* dv, uint32_t* flag, const TreeShape& t,
                              DeviceStatus* status, uint32_t polls, cudaStream_t st) {
     const int Pf = packed_stride_f32(R);
     if (use_tc) {
-        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 2 * 152));
-        bfs_level_tc_kernel<MODE><<<blocks, kTcThreads, bfs_level_tc_smem(R), st>>>(R, Pf, G, X, J, order, node, lh,
-                                                                                  m, dv, flag, t, status, polls);
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
+        bfs_level_tc_kernel<MODE><<<blocks, kTcLevelThreads, bfs_level_tc_smem(R), st>>>(R, G, X, J, order, node, lh,
+                                                                                       m, dv, flag, t, status, polls);
     } else {
         const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
         bfs_level_kernel<MODE><<<blocks, kBfsWarps * 32, bfs_level_smem(R), st>>>(R, Pf, G, X, J, order, node, lh, m,

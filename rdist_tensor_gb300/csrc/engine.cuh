@@ -185,6 +185,8 @@ int sts_compute_M(Session& s, int n, cudaStream_t st);
 int sts_draw(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
 // The mixed forms' STS-CP draws, breadth first (bfs_sampler.cu).
 int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t st);
+// Tensor-core descents (bfs_sampler.cu): used for R >= kTcMinRank.
+constexpr int kTcMinRank = 32;
 // FP32 copies of factor k and its row tree (mixed STS-CP sessions; else a no-op).
 int sts_refresh_f32(Session& s, int k, cudaStream_t st);
 // Row tree of mode k after a sampled update: FP64 build (FP64 form), or the

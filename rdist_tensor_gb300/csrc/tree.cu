@@ -155,9 +155,7 @@ __global__ void __launch_bounds__(kLeafTcThreads, 1)
             }
             umma_commit(&bar);
         }
-        bool done = false;
-        for (uint32_t it = 0; it < polls && !done; it++) done = mbar_try_wait(&bar, phase);
-        if (!done) abort_flag = 1;
+        if (!mbar_wait_limited(&bar, phase, polls)) abort_flag = 1;
         __syncthreads();
         if (abort_flag) break;
         phase ^= 1u;
@@ -184,8 +182,7 @@ __global__ void __launch_bounds__(kLeafTcThreads, 1)
     }
     if (abort_flag) {
         if (tid == 0) report(status, EXAFAC_ERR_TIMEOUT, 22, blockIdx.x, 0);
-        bool done = false;
-        for (uint32_t it = 0; it < polls && !done; it++) done = mbar_try_wait(&bar, phase);
+        mbar_wait_limited(&bar, phase, polls);
     }
     tc_fence_before();
     __syncthreads();

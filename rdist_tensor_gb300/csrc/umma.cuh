@@ -27,6 +27,29 @@ __device__ __forceinline__ uint64_t umma_desc(const void* smem_ptr, uint32_t lbo
     return d;
 }
 
+// The same for the K-major 128-byte swizzled layout: 8-row atoms of 128-byte
+// rows (1024 bytes, 1024-byte aligned), the 16-byte chunk c of row r stored
+// at chunk c ^ (r % 8); 8-row groups 1024 bytes apart (stride offset), the
+// leading offset unused (set to 16 bytes), swizzle mode 2 (bits 61-63).  A
+// K step inside an atom advances the start address by its byte offset in the
+// row.
+__device__ __forceinline__ uint64_t umma_desc_sw128(const void* smem_ptr) {
+    const uint32_t a = smem_u32(smem_ptr);
+    uint64_t d = (uint64_t)((a & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;          // leading byte offset 16 (unused)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset 1024
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Byte offset of element (r, k) of a K-major, 128-byte swizzled operand whose
+// K is cut into blocks of 32 FP32 values, `kb_bytes` apart (rows x 128 each).
+__host__ __device__ __forceinline__ uint32_t sw128_off(int r, int k, uint32_t kb_bytes) {
+    return (uint32_t)(k >> 5) * kb_bytes + (uint32_t)r * 128u + ((((uint32_t)k >> 2) & 7u) ^ ((uint32_t)r & 7u)) * 16u +
+           ((uint32_t)k & 3u) * 4u;
+}
+
 // Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
 // (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
 // 17-22, M >> 4 at bits 24-28.

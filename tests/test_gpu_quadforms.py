@@ -59,12 +59,12 @@ def test_quad_forms(lib, R, layout):
     scale = np.einsum("jr,jrs,js->j", np.abs(X64), np.abs(full[node]), np.abs(X64))
     Xd = torch.as_tensor(X).cuda()
     nd = torch.as_tensor(node.astype(np.int64)).cuda()
-    Gd = torch.as_tensor(packed).cuda()
+    Gd = {0: torch.as_tensor(packed).cuda(), 1: torch.as_tensor(packed).cuda()}
     out = {}
     for tc in (0, 1):
         q = torch.full((J,), float("nan"), dtype=torch.float32, device="cuda")
         lib.call("exafac_quad_forms_f32", R, J, ctypes.c_void_p(Xd.data_ptr()), ctypes.c_void_p(nd.data_ptr()),
-                 ctypes.c_void_p(Gd.data_ptr()), ctypes.c_void_p(q.data_ptr()), tc, None)
+                 ctypes.c_void_p(Gd[tc].data_ptr()), ctypes.c_void_p(q.data_ptr()), tc, None)
         torch.cuda.synchronize()
         out[tc] = q.cpu().numpy().astype(np.float64)
         err = np.max(np.abs(out[tc] - exact) / scale)
