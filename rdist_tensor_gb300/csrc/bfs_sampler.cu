@@ -411,21 +411,28 @@ __device__ __forceinline__ void tc_issue_slots(unsigned char* A, const float* __
 }
 
 // K block kb of the packed node in shared memory as the B operand: rows n <
-// Rn, columns 32 kb .. 32 kb + 31 of the full symmetric matrix, split into
-// TF32 hi and lo parts (the row index fastest: conflict-free swizzled stores).
-__device__ __forceinline__ void tc_expand_kblock(const float* Pk, int R, int kb, unsigned char* Bhi,
+// Rn, columns 32 kb .. 32 kb + 31 of the full symmetric matrix, as hi = the
+// FP32 value (the tensor core keeps its TF32 part, the value truncated) and
+// lo = the value minus its truncation (exact in FP32; the tensor core
+// truncates it in turn, ~2^-21 of the entry).  rs[a]: the packed index of
+// (a, a).  The row index runs fastest: conflict-free swizzled stores.
+__device__ __forceinline__ float tf32_trunc(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
+__device__ __forceinline__ void tc_expand_kblock(const float* Pk, const int* rs, int R, int kb, unsigned char* Bhi,
                                                  unsigned char* Blo, const TcLevelShape& L) {
     for (int e = threadIdx.x; e < L.Rn * 8; e += kTcLevelThreads) {
         const int c = e / L.Rn, n = e - c * L.Rn;
         const int k0 = kb * 32 + 4 * c;
         float v[4];
+        const int rn = n < R ? rs[n] : 0;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int k = k0 + q;
-            v[q] = (n < R && k < R) ? Pk[n <= k ? packed_index(R, n, k) : packed_index(R, k, n)] : 0.0f;
+            v[q] = (n < R && k < R) ? Pk[k >= n ? rn + (k - n) : rs[k] + (n - k)] : 0.0f;
         }
         const uint32_t off = (uint32_t)n * 128u + (((uint32_t)c ^ ((uint32_t)n & 7u)) * 16u);
-        tc_store_split(Bhi, Blo, off, make_float4(v[0], v[1], v[2], v[3]));
+        *reinterpret_cast<float4*>(Bhi + off) = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4*>(Blo + off) = make_float4(v[0] - tf32_trunc(v[0]), v[1] - tf32_trunc(v[1]),
+                                                            v[2] - tf32_trunc(v[2]), v[3] - tf32_trunc(v[3]));
     }
 }
 
@@ -439,6 +446,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
     __shared__ int32_t cs2[2][kTcRows];  // current node of each slot (node counts < 2^31)
     __shared__ int32_t js2[2][kTcRows];  // sample of each slot
     __shared__ float qpart[4][kTcRows];
+    __shared__ int rs[kMaxRank];  // packed index of (a, a)
     __shared__ __align__(8) uint64_t bars[2];  // [0] packed node copy, [1] MMAs
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
@@ -450,6 +458,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
     unsigned char* Blo = Bhi + L.b_kb;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     if (w == 0) tmem_alloc(&tmem_base, L.ncols);
+    for (int a = tid; a < R; a += kTcLevelThreads) rs[a] = packed_index(R, a, a);
     if (tid == 0) {
         mbar_init(&bars[0], kTcLevelThreads);  // every thread's node copies
         mbar_init(&bars[1], 1);
@@ -476,12 +485,15 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
         pk_node = g;
         pk_flight = true;
     };
-    auto land_node = [&]() -> bool {  // the copy in flight has landed
+    // the copy in flight has landed: thread 0 waits on the barrier, the
+    // others at the block barrier that follows every call (no spinning warps)
+    auto land_node = [&]() -> bool {
         if (!pk_flight) return true;
         pk_flight = false;
-        if (!mbar_wait_limited(&bars[0], fphase, wait_polls)) return false;
+        bool ok = true;
+        if (tid == 0) ok = mbar_wait_limited(&bars[0], fphase, wait_polls);
         fphase ^= 1u;
-        return true;
+        return ok;
     };
     // the node whose Gram a run of current node c multiplies, or -1 for a leaf that stays
     auto run_node = [&](int64_t c) -> int64_t {
@@ -539,11 +551,14 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
             pm = mroot[j];
             pd = dv[j];
         }
-        {  // the first run's node, if not already there
+        {  // the first run's node, if not already there (Pk is free only once the copy in flight landed)
             const int64_t g = next_run_node(cs, 0, n);
             if (g >= 0 && g != pk_node) {
-                if (!land_node()) abort_flag = 1;
-                else issue_node(g);
+                if (pk_flight) {
+                    if (!land_node()) abort_flag = 1;
+                    __syncthreads();
+                }
+                issue_node(g);
             }
         }
         cp_async_wait<1>();        // this tile's slot copies (all groups but the newest)
@@ -562,19 +577,18 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
                 i0 = i1;
                 continue;
             }
-            {  // the run's node in Pk
-                bool ok = true;
-                if (pk_node != g) {
-                    ok = land_node();
-                    if (ok) issue_node(g);
+            if (pk_node != g) {  // the run's node into Pk (free once the copy in flight landed)
+                if (pk_flight) {
+                    if (!land_node()) abort_flag = 1;
+                    __syncthreads();
                 }
-                if (ok) ok = land_node();
-                if (!ok) abort_flag = 1;
+                issue_node(g);
             }
+            if (!land_node()) abort_flag = 1;
             __syncthreads();
             if (abort_flag) goto fail;
             for (int kb = 0; kb < L.nkb; kb++) {
-                tc_expand_kblock(Pk, R, kb, Bhi, Blo, L);
+                tc_expand_kblock(Pk, rs, R, kb, Bhi, Blo, L);
                 fence_proxy_async_smem();  // the K block, to the tensor core's proxy
                 __syncthreads();
                 if (kb + 1 == L.nkb) {  // Pk is free: the next run's node
