@@ -436,6 +436,28 @@ __device__ __forceinline__ void tc_expand_kblock(const float* Pk, const int* rs,
     }
 }
 
+// Run starts of a 128-slot header as a bit mask (bit i: slot i begins a run
+// of equal node, or i = n), built by warps 0-3 with one ballot each.
+__device__ __forceinline__ void tc_run_mask(const int32_t* cs, int n, uint32_t* mask) {
+    const int i = threadIdx.x;
+    if (i >= kTcRows) return;
+    const bool start = i < n ? (i == 0 || cs[i] != cs[i - 1]) : i == n;
+    const uint32_t b = __ballot_sync(0xffffffffu, start);
+    if ((i & 31) == 0) mask[i >> 5] = b;
+}
+// The end of the run that starts at i0: the next run start after i0, or n.
+__device__ __forceinline__ int tc_run_end(const uint32_t* mask, int i0, int n) {
+    for (int w = (i0 + 1) >> 5; w < 4; w++) {
+        uint32_t bits = mask[w];
+        if (w == ((i0 + 1) >> 5)) bits &= ~0u << ((i0 + 1) & 31);
+        if (bits) {
+            const int i = (w << 5) + __ffs(bits) - 1;
+            return i < n ? i : n;
+        }
+    }
+    return n;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kTcLevelThreads, 1)
     bfs_level_tc_kernel(int R, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
@@ -445,6 +467,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
     extern __shared__ __align__(16) unsigned char tc_raw[];
     __shared__ int32_t cs2[2][kTcRows];  // current node of each slot (node counts < 2^31)
     __shared__ int32_t js2[2][kTcRows];  // sample of each slot
+    __shared__ uint32_t rm2[2][4];       // run starts of each header
     __shared__ float qpart[4][kTcRows];
     __shared__ int rs[kMaxRank];  // packed index of (a, a)
     __shared__ __align__(8) uint64_t bars[2];  // [0] packed node copy, [1] MMAs
@@ -501,13 +524,10 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
         return MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1);
     };
     // the first run needing an MMA among slots [from, n) of a header, or -1
-    auto next_run_node = [&](const int32_t* cs, int from, int n) -> int64_t {
-        int i = from;
-        while (i < n) {
+    auto next_run_node = [&](const int32_t* cs, const uint32_t* rm, int from, int n) -> int64_t {
+        for (int i = from; i < n; i = tc_run_end(rm, i, n)) {
             const int64_t g = run_node(cs[i]);
             if (g >= 0) return g;
-            const int32_t c = cs[i];
-            while (i < n && cs[i] == c) i++;
         }
         return -1;
     };
@@ -526,6 +546,11 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
         }
     }
     __syncthreads();
+    for (int b = 0; b < 2; b++) {
+        const int64_t tile = blockIdx.x + b * stride;
+        tc_run_mask(cs2[b], tile < ntiles ? tile_n(tile) : 0, rm2[b]);
+    }
+    __syncthreads();
     if (blockIdx.x < ntiles) tc_issue_slots(Abuf[0], X, js2[0], tile_n(blockIdx.x), R, L);
     int it = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += stride, it++) {
@@ -534,6 +559,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
         const int n = tile_n(tile);
         const int32_t* cs = cs2[a];
         const int32_t* js = js2[a];
+        const uint32_t* rm = rm2[a];
         const int64_t t1 = tile + stride, t2 = tile + 2 * stride;
         // the next tile's slot copies (its header is in [a ^ 1]), in flight during this tile
         if (t1 < ntiles) tc_issue_slots(Abuf[a ^ 1], X, js2[a ^ 1], tile_n(t1), R, L);
@@ -552,7 +578,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
             pd = dv[j];
         }
         {  // the first run's node, if not already there (Pk is free only once the copy in flight landed)
-            const int64_t g = next_run_node(cs, 0, n);
+            const int64_t g = next_run_node(cs, rm, 0, n);
             if (g >= 0 && g != pk_node) {
                 if (pk_flight) {
                     if (!land_node()) abort_flag = 1;
@@ -569,8 +595,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
         unsigned char* A = Abuf[a];
         for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
             const int32_t c = cs[i0];
-            int i1 = i0 + 1;
-            while (i1 < n && cs[i1] == c) i1++;
+            const int i1 = tc_run_end(rm, i0, n);
             const int64_t g = run_node(c);
             if (g < 0) {
                 if (tid >= i0 && tid < i1) flag[s0 + tid] = 1u;
@@ -592,8 +617,8 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
                 fence_proxy_async_smem();  // the K block, to the tensor core's proxy
                 __syncthreads();
                 if (kb + 1 == L.nkb) {  // Pk is free: the next run's node
-                    int64_t g2 = next_run_node(cs, i1, n);
-                    if (g2 < 0 && t1 < ntiles) g2 = next_run_node(cs2[a ^ 1], 0, tile_n(t1));
+                    int64_t g2 = next_run_node(cs, rm, i1, n);
+                    if (g2 < 0 && t1 < ntiles) g2 = next_run_node(cs2[a ^ 1], rm2[a ^ 1], 0, tile_n(t1));
                     if (g2 >= 0 && g2 != g) issue_node(g2);
                 }
                 if (tid == 0) {
@@ -659,6 +684,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
             cs2[a][tid] = hc;
         }
         __syncthreads();
+        tc_run_mask(cs2[a], t2 < ntiles ? tile_n(t2) : 0, rm2[a]);  // read after the next iteration's barriers
     }
     cp_async_wait<0>();
     if (!land_node()) abort_flag = 1;  // a prefetched node no run used
