@@ -33,6 +33,30 @@ constexpr int kBfsBlocks = 152 * 3;
 
 __host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
 
+// Run starts of a header of `rows` slots (a multiple of 32) as a bit mask:
+// bit i set when slot i begins a run of equal node, or i = n.  One ballot per
+// warp of the first rows threads; the caller synchronises before reading.
+template <typename T>
+__device__ __forceinline__ void run_mask(const T* cs, int n, int rows, uint32_t* mask) {
+    const int i = threadIdx.x;
+    if (i >= rows) return;
+    const bool start = i < n ? (i == 0 || cs[i] != cs[i - 1]) : i == n;
+    const uint32_t b = __ballot_sync(0xffffffffu, start);
+    if ((i & 31) == 0) mask[i >> 5] = b;
+}
+// The end of the run that starts at i0: the next run start after i0, or n.
+__device__ __forceinline__ int run_end(const uint32_t* mask, int words, int i0, int n) {
+    for (int w = (i0 + 1) >> 5; w < words; w++) {
+        uint32_t bits = mask[w];
+        if (w == ((i0 + 1) >> 5)) bits &= ~0u << ((i0 + 1) & 31);
+        if (bits) {
+            const int i = (w << 5) + __ffs(bits) - 1;
+            return i < n ? i : n;
+        }
+    }
+    return n;
+}
+
 // MODE 0: the mass x^T G_0 x of the node G (one node) into mroot[j].
 // MODE 1: a level of the descent: the left child's mass m_L, the branch
 //         (d <= low + m_L / m goes left), node, (low, high), flag[slot].
@@ -55,6 +79,7 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
     float* xs = A + R * AS;   // per warp: the sample's vector
     __shared__ int64_t cs[kBfsTile];
     __shared__ int32_t js[kBfsTile];
+    __shared__ uint32_t rmask[kBfsTile / 32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* xw = xs + w * AS;
     const int b0 = 4 * lane;
@@ -69,10 +94,11 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
             cs[i] = MODE == 0 ? 0 : node[j];
         }
         __syncthreads();
+        run_mask(cs, n, kBfsTile, rmask);
+        __syncthreads();
         for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
             const int64_t c = cs[i0];
-            int i1 = i0 + 1;
-            while (i1 < n && cs[i1] == c) i1++;
+            const int i1 = run_end(rmask, kBfsTile / 32, i0, n);
             const bool stay = MODE == 2 && tree_is_leaf(t, c);
             if (stay) {
                 for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) flag[s0 + i] = 1u;
@@ -436,28 +462,6 @@ __device__ __forceinline__ void tc_expand_kblock(const float* Pk, const int* rs,
     }
 }
 
-// Run starts of a 128-slot header as a bit mask (bit i: slot i begins a run
-// of equal node, or i = n), built by warps 0-3 with one ballot each.
-__device__ __forceinline__ void tc_run_mask(const int32_t* cs, int n, uint32_t* mask) {
-    const int i = threadIdx.x;
-    if (i >= kTcRows) return;
-    const bool start = i < n ? (i == 0 || cs[i] != cs[i - 1]) : i == n;
-    const uint32_t b = __ballot_sync(0xffffffffu, start);
-    if ((i & 31) == 0) mask[i >> 5] = b;
-}
-// The end of the run that starts at i0: the next run start after i0, or n.
-__device__ __forceinline__ int tc_run_end(const uint32_t* mask, int i0, int n) {
-    for (int w = (i0 + 1) >> 5; w < 4; w++) {
-        uint32_t bits = mask[w];
-        if (w == ((i0 + 1) >> 5)) bits &= ~0u << ((i0 + 1) & 31);
-        if (bits) {
-            const int i = (w << 5) + __ffs(bits) - 1;
-            return i < n ? i : n;
-        }
-    }
-    return n;
-}
-
 template <int MODE>
 __global__ void __launch_bounds__(kTcLevelThreads, 1)
     bfs_level_tc_kernel(int R, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
@@ -525,7 +529,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
     };
     // the first run needing an MMA among slots [from, n) of a header, or -1
     auto next_run_node = [&](const int32_t* cs, const uint32_t* rm, int from, int n) -> int64_t {
-        for (int i = from; i < n; i = tc_run_end(rm, i, n)) {
+        for (int i = from; i < n; i = run_end(rm, 4, i, n)) {
             const int64_t g = run_node(cs[i]);
             if (g >= 0) return g;
         }
@@ -548,7 +552,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
     __syncthreads();
     for (int b = 0; b < 2; b++) {
         const int64_t tile = blockIdx.x + b * stride;
-        tc_run_mask(cs2[b], tile < ntiles ? tile_n(tile) : 0, rm2[b]);
+        run_mask(cs2[b], tile < ntiles ? tile_n(tile) : 0, kTcRows, rm2[b]);
     }
     __syncthreads();
     if (blockIdx.x < ntiles) tc_issue_slots(Abuf[0], X, js2[0], tile_n(blockIdx.x), R, L);
@@ -595,7 +599,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
         unsigned char* A = Abuf[a];
         for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
             const int32_t c = cs[i0];
-            const int i1 = tc_run_end(rm, i0, n);
+            const int i1 = run_end(rm, 4, i0, n);
             const int64_t g = run_node(c);
             if (g < 0) {
                 if (tid >= i0 && tid < i1) flag[s0 + tid] = 1u;
@@ -684,7 +688,7 @@ __global__ void __launch_bounds__(kTcLevelThreads, 1)
             cs2[a][tid] = hc;
         }
         __syncthreads();
-        tc_run_mask(cs2[a], t2 < ntiles ? tile_n(t2) : 0, rm2[a]);  // read after the next iteration's barriers
+        run_mask(cs2[a], t2 < ntiles ? tile_n(t2) : 0, kTcRows, rm2[a]);  // read after the next iteration's barriers
     }
     cp_async_wait<0>();
     if (!land_node()) abort_flag = 1;  // a prefetched node no run used
@@ -727,6 +731,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     extern __shared__ __align__(16) unsigned char tc_raw[];
     __shared__ int64_t cs[kTcRows];
     __shared__ int32_t js[kTcRows];
+    __shared__ uint32_t rmask[kTcRows / 32];
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
@@ -745,10 +750,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         __syncthreads();
         tc_stage_slots(b, R, X, js, n);
+        run_mask(cs, n, kBfsTile, rmask);
+        __syncthreads();
         for (int i0 = 0; i0 < n;) {
             const int64_t c = cs[i0];
-            int i1 = i0 + 1;
-            while (i1 < n && cs[i1] == c) i1++;
+            const int i1 = run_end(rmask, kBfsTile / 32, i0, n);
             const int64_t leaf = tree_leaf_idx(t, c);
             const int rows = (int)min((int64_t)F, t.n - leaf * F);
             const float* Ub = U + leaf * F * R;
@@ -898,6 +904,7 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_leaf_kernel(int R, TreeSha
     float* xs = UT + R * FS;     // per warp
     __shared__ int64_t cs[kBfsTile];
     __shared__ int32_t js[kBfsTile];
+    __shared__ uint32_t rmask[kBfsTile / 32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* xw = xs + w * AS;
     const int r0 = 4 * lane;
@@ -912,10 +919,11 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_leaf_kernel(int R, TreeSha
             cs[i] = node[j];
         }
         __syncthreads();
+        run_mask(cs, n, kTcRows, rmask);
+        __syncthreads();
         for (int i0 = 0; i0 < n;) {
             const int64_t c = cs[i0];
-            int i1 = i0 + 1;
-            while (i1 < n && cs[i1] == c) i1++;
+            const int i1 = run_end(rmask, kTcRows / 32, i0, n);
             const int64_t leaf = tree_leaf_idx(t, c);
             const int rows = (int)min((int64_t)F, t.n - leaf * F);
             const float* Ub = U + leaf * F * R;
