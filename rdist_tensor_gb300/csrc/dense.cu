@@ -647,6 +647,35 @@ __global__ void spd_pinv_packed_kernel(int R, const double* __restrict__ A, doub
     if (refine) newton_refine_global(R, A, out, vt_scratch);
 }
 
+// The Newton step X <- X + X (I - A X) (= 2X - X A X, the fixed point a
+// pseudo-inverse) for the packed path, spread over R blocks of one row each
+// in FP64: T = I - A X (A's upper triangle read), then X += X T.  On one SM
+// the two R^3 products took ~1.2 ms at R = 128 (GB300 retires ~1.6 FP64
+// FMA per clock per SM); this form runs them on R SMs.  T: R^2 doubles.
+__global__ void newton_residual_kernel(int R, const double* __restrict__ A, const double* __restrict__ X,
+                                       double* __restrict__ T) {
+    __shared__ double arow[kMaxRank];
+    const int i = blockIdx.x;
+    for (int k = threadIdx.x; k < R; k += blockDim.x) arow[k] = i <= k ? A[i * R + k] : A[k * R + i];
+    __syncthreads();
+    for (int j = threadIdx.x; j < R; j += blockDim.x) {
+        double acc = 0.0;
+        for (int k = 0; k < R; k++) acc = fma(arow[k], X[k * R + j], acc);
+        T[i * R + j] = (i == j ? 1.0 : 0.0) - acc;
+    }
+}
+__global__ void newton_update_kernel(int R, const double* __restrict__ T, double* __restrict__ X) {
+    __shared__ double xrow[kMaxRank];
+    const int i = blockIdx.x;
+    for (int k = threadIdx.x; k < R; k += blockDim.x) xrow[k] = X[i * R + k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < R; j += blockDim.x) {
+        double acc = 0.0;
+        for (int k = 0; k < R; k++) acc = fma(xrow[k], T[k * R + j], acc);
+        X[i * R + j] = xrow[j] + acc;
+    }
+}
+
 // Shared memory of the Cholesky path (L, L^{-1}, and the Newton step's
 // third matrix).  The Cholesky path in full matrices is used when its buffers
 // fit under kPinvSmemCap (R <= 92); larger ranks take the packed kernel.
@@ -674,8 +703,14 @@ static int launch_pinv_impl(int R, const double* A, double* out, double tol, dou
         const size_t smem = std::max(chol_packed_smem_bytes(R), syev_smem_bytes(R));
         EXAFAC_CUDA_TRY(
             cudaFuncSetAttribute(spd_pinv_packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        spd_pinv_packed_kernel<<<1, 512, smem, stream>>>(R, A, out, tol, vt_scratch, refine);
+        spd_pinv_packed_kernel<<<1, 512, smem, stream>>>(R, A, out, tol, vt_scratch, 0);
         count_launch();
+        if (refine) {
+            newton_residual_kernel<<<R, 128, 0, stream>>>(R, A, out, vt_scratch);
+            count_launch();
+            newton_update_kernel<<<R, 128, 0, stream>>>(R, vt_scratch, out);
+            count_launch();
+        }
         EXAFAC_CHECK_LAUNCH();
         return EXAFAC_OK;
     }
