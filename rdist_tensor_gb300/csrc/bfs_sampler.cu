@@ -1104,7 +1104,9 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
     int oi = 0;                  // off[oi]: the current level's slot ranges
     int64_t lb = 0, nl = 1;      // the level's first node and node count
     const int64_t levels = t.lfill_level;
-    const bool tail = t.node_count > t.nodes_before_lfill;
+    // the tail level moves samples at internal nodes of level lfill one level
+    // down; a complete tree (every node of that level a leaf) has none
+    const bool tail = t.node_count > t.nodes_upto_lfill;
     for (int64_t lvl = 0; lvl <= levels; lvl++) {
         const bool is_tail = lvl == levels;
         if (is_tail && !tail) break;

@@ -556,6 +556,36 @@ __global__ void __launch_bounds__(kSmallPinvThreads)
 // sessions' scratch holds (N + 1) R^2).
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
+// Sums with four independent FP64 accumulators (a dependent FP64 operation
+// takes ~64 cycles on GB300, so one chain of R FMAs is latency-bound).
+// sub_dot: s0 - sum_{t in [t0, t1)} L(i, t) Li(t, c); gram_dot: sum_{k in
+// [k0, R)} Li(k, a) Li(k, b); both over packed lower triangles.
+__device__ __forceinline__ double sub_dot(const double* L, const double* Li, int i, int c, int t0, int t1,
+                                          double s0) {
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int t = t0;
+    for (; t + 3 < t1; t += 4) {
+        s0 -= L[tri(i, t)] * Li[tri(t, c)];
+        s1 -= L[tri(i, t + 1)] * Li[tri(t + 1, c)];
+        s2 -= L[tri(i, t + 2)] * Li[tri(t + 2, c)];
+        s3 -= L[tri(i, t + 3)] * Li[tri(t + 3, c)];
+    }
+    for (; t < t1; t++) s0 -= L[tri(i, t)] * Li[tri(t, c)];
+    return (s0 + s1) + (s2 + s3);
+}
+__device__ __forceinline__ double gram_dot(const double* Li, int a, int b, int k0, int R) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int k = k0;
+    for (; k + 3 < R; k += 4) {
+        s0 = fma(Li[tri(k, a)], Li[tri(k, b)], s0);
+        s1 = fma(Li[tri(k + 1, a)], Li[tri(k + 1, b)], s1);
+        s2 = fma(Li[tri(k + 2, a)], Li[tri(k + 2, b)], s2);
+        s3 = fma(Li[tri(k + 3, a)], Li[tri(k + 3, b)], s3);
+    }
+    for (; k < R; k++) s0 = fma(Li[tri(k, a)], Li[tri(k, b)], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
 __device__ void newton_refine_global(int R, const double* __restrict__ A, double* __restrict__ out,
                                      double* __restrict__ scratch) {
     double* X = scratch;
@@ -616,8 +646,7 @@ __global__ void spd_pinv_packed_kernel(int R, const double* __restrict__ A, doub
     if (!fail) {
         for (int c = tid; c < R; c += nt) {
             for (int i = c; i < R; i++) {
-                double sacc = (i == c) ? 1.0 : 0.0;
-                for (int t = c; t < i; t++) sacc -= L[tri(i, t)] * Li[tri(t, c)];
+                const double sacc = sub_dot(L, Li, i, c, c, i, (i == c) ? 1.0 : 0.0);
                 Li[tri(i, c)] = sacc / L[tri(i, i)];
             }
         }
@@ -626,8 +655,7 @@ __global__ void spd_pinv_packed_kernel(int R, const double* __restrict__ A, doub
         for (int e = tid; e < R * R; e += nt) {
             const int a = e / R, b = e % R;
             const int k0 = a > b ? a : b;
-            double acc = 0.0;
-            for (int k = k0; k < R; k++) acc = fma(Li[tri(k, a)], Li[tri(k, b)], acc);
+            const double acc = gram_dot(Li, a, b, k0, R);
             out[e] = acc;
             part += acc * acc;
         }
@@ -921,8 +949,7 @@ __global__ void sts_phi_chol_kernel(int N, int n, int R, int first, double tol, 
     if (ok) {
         for (int c = tid; c < R; c += nt) {  // L^{-1}, column c by forward substitution
             for (int i = c; i < R; i++) {
-                double s = (i == c) ? 1.0 : 0.0;
-                for (int t = c; t < i; t++) s -= L[tri(i, t)] * Li[tri(t, c)];
+                const double s = sub_dot(L, Li, i, c, c, i, (i == c) ? 1.0 : 0.0);
                 Li[tri(i, c)] = s / L[tri(i, i)];
             }
         }
@@ -931,8 +958,7 @@ __global__ void sts_phi_chol_kernel(int N, int n, int R, int first, double tol, 
         for (int e = tid; e < R2; e += nt) {  // Phi = L^{-T} L^{-1}
             const int a = e / R, b = e % R;
             const int k0 = a > b ? a : b;
-            double acc = 0.0;
-            for (int k = k0; k < R; k++) acc = fma(Li[tri(k, a)], Li[tri(k, b)], acc);
+            const double acc = gram_dot(Li, a, b, k0, R);
             Phi[e] = acc;
             part += acc * acc;
         }
