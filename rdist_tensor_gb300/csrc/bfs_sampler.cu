@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_level_kernel(int R, int Pf
 // MMAs, frees its tensor memory and leaves.
 // ---------------------------------------------------------------------------
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;
 
 struct TcLayout {
     int Rk, Rn, KC;    // K and N padded to 16, K chunk of B
@@ -272,18 +272,16 @@ __device__ __forceinline__ void tc_end(TcBlock& b, DeviceStatus* status, int whe
 // 128 bytes apart, all in the same banks).
 constexpr int kTcUnroll = 8;
 
-__device__ __forceinline__ float4 tf32_rna4(float4 v) {
-    return make_float4(tf32_rna(v.x), tf32_rna(v.y), tf32_rna(v.z), tf32_rna(v.w));
-}
 
-// v rounded to TF32 into hi_tile and, when lo_tile is not null, the rounded
-// remainder into lo_tile.
+// v into hi_tile as FP32 (the tensor core keeps its TF32 part: the value
+// truncated to 10 explicit mantissa bits) and, when lo_tile is not null, the
+// value minus that truncation (exact in FP32) into lo_tile.
+__device__ __forceinline__ float tf32_trunc(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
 __device__ __forceinline__ void tc_store_split(unsigned char* hi_tile, unsigned char* lo_tile, uint32_t off, float4 v) {
-    const float4 h = tf32_rna4(v);
-    *reinterpret_cast<float4*>(hi_tile + off) = h;
+    *reinterpret_cast<float4*>(hi_tile + off) = v;
     if (lo_tile)
         *reinterpret_cast<float4*>(lo_tile + off) =
-            tf32_rna4(make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w));
+            make_float4(v.x - tf32_trunc(v.x), v.y - tf32_trunc(v.y), v.z - tf32_trunc(v.z), v.w - tf32_trunc(v.w));
 }
 
 // x of a slot, columns k .. k + 3 (zero past R).
@@ -442,7 +440,6 @@ __device__ __forceinline__ void tc_issue_slots(unsigned char* A, const float* __
 // lo = the value minus its truncation (exact in FP32; the tensor core
 // truncates it in turn, ~2^-21 of the entry).  rs[a]: the packed index of
 // (a, a).  The row index runs fastest: conflict-free swizzled stores.
-__device__ __forceinline__ float tf32_trunc(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
 __device__ __forceinline__ void tc_expand_kblock(const float* Pk, const int* rs, int R, int kb, unsigned char* Bhi,
                                                  unsigned char* Blo, const TcLevelShape& L) {
     for (int e = threadIdx.x; e < L.Rn * 8; e += kTcLevelThreads) {
