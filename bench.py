@@ -12,6 +12,10 @@ sampled-ALS solvers are quoted on; no public dataset is named):
   planted3      the same tensor, STS-CP, R=25, J=65536, FP64 form.
   zipf4         4-mode Zipf(1.2) tensor 5e6 x 5e6 x 2e4 x 1e3, 1e8 nonzeros,
                 log-normal values, CP-ARLS-LEV, R=25, J=2^17, TF32 vs FP64.
+  gcp4          3-mode Poisson count tensor 1e6 x 1e6 x 1e4, 5e7 nonzeros,
+                gradient-based GCP (Poisson loss, sampled entries, Adam),
+                R=32, 200 steps: its own metric, GCP steps/s (no reference
+                counterpart; --impl reference prints an unavailable line).
 
 A sweep updates every mode once.  Randomly initialised factors give the Zipf
 tensors empty sampled fibres (zero factors, then NaN, in the reference too),
@@ -51,6 +55,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "sampled-ALS sweeps/s at equal fit (±1e-3): mixed vs FP64 form, 1 GB300"
+GCP_METRIC = "GCP Adam steps/s (Poisson loss on sampled entries), 1 GB300"
 WORKLOADS = {
     "zipf5": dict(desc="5-mode Zipf(1.1) tensor 1e6 x 1e6 x 1e5 x 1e3 x 100, 2e8 nonzeros, N(0,1) values, STS-CP, "
                        "R=128, J=2^19",
@@ -70,6 +75,11 @@ WORKLOADS = {
                   gen="zipf", dims=(5_000_000, 5_000_000, 20_000, 1_000), nnz=100_000_000, alpha=1.2,
                   values="lognormal", R=25, J=1 << 17, sampler="cp_arls_lev", precision="tf32", exact_pre=True,
                   steps=100, cpu_J=1 << 17),
+    "gcp4": dict(desc="3-mode Poisson count tensor 1e6 x 1e6 x 1e4, 5e7 nonzeros (Zipf(1.1) support, rates from a "
+                      "planted rank-16 CP model with Gamma(0.5,1) factors), GCP Poisson loss, R=32, J=2^17 sampled "
+                      "entries per step (2^16 nonzeros + 2^16 zeros), Adam lr=1e-2, FP32",
+                 kind="gcp", dims=(1_000_000, 1_000_000, 10_000), nnz=50_000_000, planted_rank=16, R=32, J=1 << 17,
+                 lr=1e-2, steps=200, cpu_steps=3),
     "zipf4_small": dict(desc="4-mode Zipf(1.2) tensor 5e5 x 5e5 x 2e4 x 1e3, 1e7 nonzeros (reduced)",
                         gen="zipf", dims=(500_000, 500_000, 20_000, 1_000), nnz=10_000_000, alpha=1.2,
                         values="lognormal", R=25, J=1 << 17, sampler="cp_arls_lev", precision="tf32", exact_pre=True,
@@ -213,6 +223,205 @@ def level_kernel_roofline(R, J, nodes=1024, launches=5, seed=0):
             "traffic": None, "kernel": "bfs_level_tc_kernel (tcgen05 quadratic forms of a descent level)",
             "algorithmic_bytes": algo, "duration_s": dur, "launches": launches, "peak_source": peak_kind,
             "tensor_tflops": 2.0 * J * R * R / dur / 1e12, "J": J, "R": R, "nodes": used}
+
+
+def gcp_adjoint_roofline(model, J_nz, J_z, launches=20):
+    """Roofline of the GCP step's dominant kernel of this library, the
+    sampled adjoint (cp_adjoint_kernel, the sampled MTTKRP of the loss
+    derivatives into every factor), timed live: `launches` launches, each on
+    its own fresh stratified sample (so the rows it touches are not the last
+    launch's), CUDA events on the launching stream after two warm-ups.
+    Algorithmic bytes per launch, J entries: per entry its N coordinates and
+    its loss derivative (4 N + 4), the N factor rows it reads (N R 4) and the
+    N gradient rows it adds into (N R 4, each counted once)."""
+    import torch
+
+    from rdist_tensor_gb300 import _lib, gcp
+
+    N, R, J = model.N, model.R, J_nz + J_z
+    samples = [model.step_sample(J_nz, J_z)[0] for _ in range(launches)]
+    gm = torch.rand(J, dtype=torch.float32, device="cuda")
+    grads = [torch.zeros_like(U) for U in model.factors]
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream()
+    dims = gcp._dims_arg(model.dims)
+
+    def launch(idx):
+        _lib.call("exafac_cp_sampled_adjoint", N, R, dims, J, ctypes.c_void_p(idx.data_ptr()),
+                  ctypes.c_void_p(gm.data_ptr()), gcp._ptrs([U.detach() for U in model.factors]), gcp._ptrs(grads),
+                  0, ctypes.c_void_p(status.data_ptr()), ctypes.c_void_p(st.cuda_stream))
+
+    for k in range(2):
+        launch(samples[k])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for idx in samples:
+        launch(idx)
+    e1.record(st)
+    torch.cuda.synchronize()
+    if int(status.item()) != 0:
+        raise RuntimeError("adjoint flagged an out-of-range entry")
+    dur = e0.elapsed_time(e1) * 1e-3 / launches
+    algo = J * (4 * N + 4) + 2 * J * N * R * 4
+    peak, peak_kind = measured_peaks()
+    achieved = algo / dur / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "cp_adjoint_kernel (sampled MTTKRP of the loss derivatives, every mode)",
+            "algorithmic_bytes": algo, "duration_s": dur, "launches": launches, "peak_source": peak_kind, "J": J,
+            "R": R}
+
+
+def gcp_cpu_sample(dims, idx_np, vals_np, R, J_nz, J_z, lr, steps, seed=0):
+    """The same GCP step restated with torch on the host cores (no
+    counterpart exists in the reference): stratified sample, model values
+    from gathered factor rows, weighted Poisson loss, autograd gradient
+    (index-add backward), Adam and the projection onto nonnegative factors,
+    on factors of the workload's full size.  Returns (steps/s, threads)."""
+    import torch
+
+    g = torch.Generator().manual_seed(seed)
+    idx = torch.as_tensor(idx_np.astype(np.int64))
+    vals = torch.as_tensor(vals_np.astype(np.float32))
+    U = [torch.rand((int(d), R), generator=g) * 0.5 for d in dims]
+    for u in U:
+        u.requires_grad_()
+    opt = torch.optim.Adam(U, lr=lr)
+    nnz, total = idx.shape[0], float(np.prod([float(d) for d in dims]))
+    wnz, wz = nnz / J_nz, (total - nnz) / J_z
+
+    def step():
+        pick = torch.randint(0, nnz, (J_nz,), generator=g)
+        rows = torch.cat([idx[pick], torch.stack([torch.randint(0, int(d), (J_z,), generator=g) for d in dims], 1)])
+        x = torch.cat([vals[pick], torch.zeros(J_z)])
+        w = torch.cat([torch.full((J_nz,), wnz), torch.full((J_z,), wz)])
+        m = U[0][rows[:, 0]]
+        for k in range(1, len(U)):
+            m = m * U[k][rows[:, k]]
+        m = m.sum(dim=1)
+        opt.zero_grad(set_to_none=True)
+        f = (w * (m - x * torch.log(m + 1e-10))).sum()
+        f.backward()
+        opt.step()
+        with torch.no_grad():
+            for u in U:
+                u.clamp_(min=0.0)
+
+    step()
+    t = time.perf_counter()
+    for _ in range(steps):
+        step()
+    return steps / (time.perf_counter() - t), torch.get_num_threads()
+
+
+def run_gcp(args, w):
+    """Config-4 line: gradient-based Poisson GCP through the autograd sampled
+    adjoint, K Adam steps timed with CUDA events after W warm-up steps, the
+    tensor resident on the GPU."""
+    import torch
+
+    from rdist_tensor_gb300 import _lib, gcp, synthetic
+
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    t = time.perf_counter()
+    dims, idx, vals, _ = synthetic.poisson_counts_device(w["dims"], w["nnz"], rank=w["planted_rank"],
+                                                         seed=args.seed + rank)
+    torch.cuda.synchronize()
+    log(f"generated {idx.shape[0]} nonzeros in {time.perf_counter() - t:.1f}s")
+    R, J, lr = w["R"], w["J"], w["lr"]
+    J_nz = J // 2
+    J_z = J - J_nz
+    steps = args.steps if args.steps is not None else w["steps"]
+    warmup = args.warmup
+    model = gcp.GCP(idx, vals, dims, rank=R, loss="poisson", seed=1)
+    f_start = model.full_objective()
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(warmup):
+        model.step(J_nz, J_z, lr)
+    torch.cuda.synchronize()
+    l0 = lib.exafac_kernel_launches()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.begin()
+    e0.record()
+    for _ in range(steps):
+        f = model.step(J_nz, J_z, lr)
+    e1.record()
+    torch.cuda.synchronize()
+    clocks.end()
+    barrier(ws)
+    elapsed = max_over_ranks(e0.elapsed_time(e1) * 1e-3, ws)
+    launches = lib.exafac_kernel_launches() - l0
+    clk = clocks.stop()
+    value = ws * steps / elapsed
+    f_end = model.full_objective()
+    log(f"gcp: {value:.1f} steps/s, objective {f_start:.6e} -> {f_end:.6e}")
+
+    # optimizer share: Adam + projection alone, on the last step's gradients
+    opt = model.optimizer(lr)
+    k_opt = 20
+    torch.cuda.synchronize()
+    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    o0.record()
+    for _ in range(k_opt):
+        opt.step()
+        with torch.no_grad():
+            torch._foreach_clamp_min_(model.factors, 0.0)
+    o1.record()
+    torch.cuda.synchronize()
+    opt_ms = o0.elapsed_time(o1) / k_opt
+
+    roofline = gcp_adjoint_roofline(model, J_nz, J_z)
+
+    # e2e: the public API step with every step's objective read back to
+    # pinned host memory inside the timed region
+    e2e_steps = min(steps, 50)
+    host_f = torch.empty(e2e_steps, dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        host_f[k].copy_(model.step(J_nz, J_z, lr), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_el = max_over_ranks(time.perf_counter() - t0, ws)
+    if not bool(torch.isfinite(host_f).all()):
+        raise RuntimeError("a sampled objective is not finite")
+    e2e = {"value": ws * e2e_steps / e2e_el, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4,
+           "steps": e2e_steps,
+           "note": "GCP.step through the public API; the step's sample is drawn on the device from (seed, "
+                   "counter), so it has no host input; its sampled objective is read back every step"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        idx_np, vals_np = idx.cpu().numpy(), vals.cpu().numpy()
+        cval, cores = gcp_cpu_sample(dims, idx_np, vals_np, R, J_nz, J_z, lr, w["cpu_steps"])
+        cpu = {"value": cval, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": f"{w['cpu_steps']} full-size steps (after one untimed) of the same GCP step restated "
+                         "with torch on the host cores; the reference has no GCP"}
+    if rank != 0:
+        return 0
+    cfg = {"workload": w["desc"], "nnz": int(idx.shape[0]), "R": R, "J": J, "J_nonzeros": J_nz, "J_zeros": J_z,
+           "lr": lr, "loss": "poisson", "init": "Uniform(0, 0.5) factors",
+           "parallelism": f"{ws} independent replica(s)",
+           "l2": "inputs larger than L2 (factors, Adam moments and gradients: 1.03 GB)",
+           "objective_start": f_start, "objective_end": f_end,
+           "objective": "exact Poisson objective over all 1e16 entries (model mass - sum_nz x log m)",
+           "steps_run": warmup + steps, "optimizer_ms_per_step": opt_ms,
+           "step_kernels_of_this_library": "gcp_sample_kernel, cp_model_kernel, cp_adjoint_kernel; "
+                                           "loss terms and fused Adam are torch's"}
+    line = {"metric": GCP_METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": steps,
+            "warmup": warmup, "ms_per_step": 1000.0 * elapsed / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded; no public dataset is named for this shape)", "config": cfg,
+            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def make_workload(w, seed=0):
@@ -646,6 +855,13 @@ def main():
                     help="time the dominant kernel alone on the workload's J and R and exit (for a kernel profile)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if w.get("kind") == "gcp":
+        if args.impl == "reference":
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no GCP (config 4); its "
+                                                                      "CPU restatement is this line's cpu_baseline"}))
+            return 0
+        return run_gcp(args, w)
     if args.impl == "reference":
         if args.steps is None:
             args.steps = w["steps"]

@@ -124,7 +124,7 @@ def sample_entries(idx: torch.Tensor, vals: torch.Tensor, dims: Sequence[int], J
 class GCP:
     """Gradient-based GCP of a sparse tensor with stratified entry sampling,
     Adam steps, and (for the Poisson and Bernoulli losses) nonnegative
-    factors by projection after every step."""
+    factors by projection after every step.  Factors start Uniform(0, 0.5)."""
 
     def __init__(self, idx, vals, dims: Sequence[int], rank: int, loss: str = "poisson",
                  dtype: torch.dtype = torch.float32, seed: int = 0, device: str = "cuda"):
@@ -137,6 +137,29 @@ class GCP:
         g.manual_seed(int(seed))
         self.factors = [torch.rand((d, self.R), generator=g, dtype=dtype, device=device).mul_(0.5).requires_grad_()
                         for d in self.dims]
+        self._opt, self._lr = None, None
+
+    def model_mass(self) -> float:
+        """Sum of the model over every entry of the tensor:
+        sum_r prod_k (sum_i U_k[i, r]), in FP64."""
+        with torch.no_grad():
+            tot = torch.ones(self.R, dtype=torch.float64, device=self.factors[0].device)
+            for U in self.factors:
+                tot *= U.detach().double().sum(dim=0)
+            return float(tot.sum())
+
+    def full_objective(self, chunk: int = 1 << 24) -> float:
+        """The Poisson objective over every entry of the tensor, zeros
+        included: sum_all m - sum_nz x log(m + EPS).  The first sum is the
+        model mass (column sums), so only the nonzeros are evaluated."""
+        if self.loss != "poisson":
+            raise ValueError("full_objective is defined for the Poisson loss")
+        nz = 0.0
+        with torch.no_grad():
+            for a in range(0, self.idx.shape[0], chunk):
+                m = sampled_model(self.idx[a:a + chunk], self.factors)
+                nz += float((self.vals[a:a + chunk].double() * torch.log(m.double() + EPS)).sum())
+        return self.model_mass() - nz
 
     def objective(self, idx, x, w) -> torch.Tensor:
         m = sampled_model(idx, self.factors)
@@ -147,18 +170,31 @@ class GCP:
         self.counter += 1
         return out
 
+    def optimizer(self, lr: float = 1e-2) -> torch.optim.Optimizer:
+        """The model's Adam optimizer (torch's fused CUDA Adam); its moments
+        persist across steps and fit calls while the rate stays the same."""
+        if self._opt is None or self._lr != lr:
+            self._opt = torch.optim.Adam(self.factors, lr=lr, fused=True)
+            self._lr = lr
+        return self._opt
+
+    def step(self, J_nz: int, J_z: int, lr: float = 1e-2) -> torch.Tensor:
+        """One gradient step: a fresh stratified sample, the weighted loss on
+        it, its gradient through the sampled adjoint, an Adam update and (for
+        the Poisson and Bernoulli losses) the projection onto nonnegative
+        factors.  Returns the sampled objective as a device scalar; nothing is
+        read back to the host."""
+        opt = self.optimizer(lr)
+        idx, x, w = self.step_sample(J_nz, J_z)
+        opt.zero_grad(set_to_none=True)
+        f = self.objective(idx, x, w)
+        f.backward()
+        opt.step()
+        if self.loss in ("poisson", "bernoulli"):
+            with torch.no_grad():
+                torch._foreach_clamp_min_(self.factors, 0.0)
+        return f.detach()
+
     def fit(self, steps: int, J_nz: int, J_z: int, lr: float = 1e-2):
-        opt = torch.optim.Adam(self.factors, lr=lr)
-        history = []
-        for _ in range(steps):
-            idx, x, w = self.step_sample(J_nz, J_z)
-            opt.zero_grad(set_to_none=True)
-            f = self.objective(idx, x, w)
-            f.backward()
-            opt.step()
-            if self.loss in ("poisson", "bernoulli"):
-                with torch.no_grad():
-                    for U in self.factors:
-                        U.clamp_(min=0.0)
-            history.append(f.detach())
+        history = [self.step(J_nz, J_z, lr) for _ in range(steps)]
         return torch.stack(history) if history else torch.empty(0)

@@ -193,6 +193,36 @@ def poisson_counts(dims, nnz, rank=16, seed=0):
     return d, idx, vals, A
 
 
+def poisson_counts_device(dims, nnz, rank=16, seed=0, device="cuda"):
+    """``poisson_counts`` built with torch on a CUDA device, for the
+    5e7-nonzero count tensors: the Zipf(1.1) support of
+    ``zipf_tensor_device``, Gamma(0.5, 1) planted factors drawn as Z^2 / 2
+    with Z ~ N(0, 1) (the chi-square with one degree of freedom, halved),
+    entries ~ Poisson(sum_r prod_k A_k[i_k, r]) with zeros redrawn as 1.
+    Returns (dims int64 numpy, idx int32 [nnz, N] device tensor, float32
+    values device tensor, planted factors as float32 device tensors)."""
+    import torch
+
+    d, idx, _ = zipf_tensor_device(dims, nnz, alpha=1.1, values="normal", seed=seed + 1, device=device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    A = []
+    for n in d:
+        z = torch.randn((int(n), rank), dtype=torch.float32, device=device, generator=gen)
+        A.append(0.5 * z * z)
+    lam = torch.empty(idx.shape[0], dtype=torch.float32, device=device)
+    step = 1 << 24
+    for a in range(0, idx.shape[0], step):
+        rows = idx[a:a + step].to(torch.int64)
+        rate = A[0][rows[:, 0]]
+        for k in range(1, len(A)):
+            rate = rate * A[k][rows[:, k]]
+        lam[a:a + step] = rate.sum(dim=1)
+    vals = torch.poisson(lam, generator=gen)
+    vals[vals == 0] = 1.0
+    return d, idx, vals, A
+
+
 def gaussian_factors(dims, R, seed=0):
     """initialize_factors_gaussian_random (low_rank_tensor.hpp:35-41,
     distmat.hpp:153-168, 85-138): N(0,1) entries, columns normalised."""

@@ -1,5 +1,6 @@
 """Host-side logic of bench.py that needs no GPU: the clock record of the
-timed region and the algorithmic-bytes formula."""
+timed region, the algorithmic-bytes formula, the config-4 CPU baseline and
+reference line."""
 import datetime
 
 import bench
@@ -38,3 +39,30 @@ def test_algorithmic_bytes_per_step():
     # J_u (N-1) 4 + J_u 8 + J_u R 8 + H (4 + 8) + 2 T R 8
     assert bench.algorithmic_bytes(4, 25, 1000, 5000, 300) == 1000 * 3 * 4 + 1000 * 8 + 1000 * 25 * 8 + 5000 * 12 + \
         2 * 300 * 25 * 8
+
+
+def test_gcp_cpu_baseline_runs():
+    """The config-4 CPU baseline (the GCP step restated with torch on the
+    host) on a tiny tensor: it steps and reports a rate."""
+    import numpy as np
+
+    dims = (30, 20, 10)
+    rng = np.random.default_rng(0)
+    idx = np.stack([rng.integers(0, d, 200) for d in dims], axis=1).astype(np.int32)
+    vals = rng.poisson(2.0, 200).astype(np.float32) + 1.0
+    rate, threads = bench.gcp_cpu_sample(dims, idx, vals, 4, 64, 64, 1e-2, 2)
+    assert rate > 0 and threads >= 1
+
+
+def test_gcp_reference_arm_is_unavailable(capsys):
+    import json
+    import sys
+
+    argv = sys.argv
+    sys.argv = ["bench.py", "--impl", "reference", "--workload", "gcp4"]
+    try:
+        assert bench.main() == 0
+    finally:
+        sys.argv = argv
+    line = json.loads(capsys.readouterr().out.strip())
+    assert line["impl"] == "reference" and "unavailable" in line

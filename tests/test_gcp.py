@@ -167,3 +167,66 @@ def test_poisson_fit_decreases_objective():
     model.fit(200, J_nz=4096, J_z=4096, lr=2e-2)
     f1 = full()
     assert np.isfinite(f1) and f1 < 0.9 * f0, (f0, f1)
+
+
+def test_full_objective_matches_dense():
+    """The exact Poisson objective over every entry (model mass from column
+    sums, nonzero terms from the kernels) against the dense FP64 sum."""
+    gcp = _cuda()
+    from rdist_tensor_gb300 import synthetic
+
+    dims = (30, 20, 10)
+    _, nz_idx, nz_vals, _ = synthetic.poisson_counts(dims, 900, rank=3, seed=4)
+    model = gcp.GCP(nz_idx, nz_vals, dims, rank=5, loss="poisson", dtype=torch.float64, seed=2)
+    X = torch.zeros(dims, dtype=torch.float64, device="cuda")
+    X[tuple(torch.as_tensor(nz_idx.astype(np.int64), device="cuda").T)] = torch.as_tensor(
+        nz_vals.astype(np.float64), device="cuda")
+    M = _dense_model([u.detach() for u in model.factors])
+    ref = float((M - X * torch.log(M + gcp.EPS)).sum())
+    got = model.full_objective(chunk=256)  # several chunks
+    assert abs(got - ref) <= 1e-10 * abs(ref), (got, ref)
+    assert abs(model.model_mass() - float(M.sum())) <= 1e-12 * float(M.sum())
+
+
+def test_poisson_counts_device():
+    """The device generator of the count tensors: distinct in-range
+    coordinates, positive integer counts, and a mean count near the planted
+    model's mean rate at those coordinates."""
+    _cuda()
+    from rdist_tensor_gb300 import synthetic
+
+    dims = (20_000, 20_000, 500)
+    d, idx, vals, A = synthetic.poisson_counts_device(dims, 200_000, rank=16, seed=3)
+    assert idx.shape == (200_000, 3) and idx.dtype == torch.int32
+    for k in range(3):
+        assert int(idx[:, k].min()) >= 0 and int(idx[:, k].max()) < dims[k]
+    key = (idx[:, 0].long() * dims[1] + idx[:, 1].long()) * dims[2] + idx[:, 2].long()
+    assert torch.unique(key).numel() == idx.shape[0]
+    assert bool((vals >= 1).all()) and bool((vals == torch.round(vals)).all())
+    rows = idx.long()
+    lam = (A[0][rows[:, 0]] * A[1][rows[:, 1]] * A[2][rows[:, 2]]).sum(dim=1).double()
+    # E[max(Poisson(lam), 1)] = lam + exp(-lam)
+    expect = float((lam + torch.exp(-lam)).mean())
+    assert abs(float(vals.double().mean()) - expect) < 0.02 * expect
+    # Gamma(0.5, 1) factors: mean 0.5, variance 0.5
+    a = torch.cat([x.reshape(-1) for x in A]).double()
+    assert abs(float(a.mean()) - 0.5) < 0.01 and abs(float(a.var()) - 0.5) < 0.03
+
+
+def test_gcp_reduced_config4_decreases_objective():
+    """Config 4's step (R = 32, J = 2^17 entries, Adam lr = 1e-2) on a
+    reduced count tensor, 1e5 x 1e5 x 1e3 with 5e6 nonzeros: the exact
+    objective over all entries falls (by two orders of magnitude in a torch
+    CPU restatement of the same steps), and every sampled objective is
+    finite."""
+    gcp = _cuda()
+    from rdist_tensor_gb300 import synthetic
+
+    dims, idx, vals, _ = synthetic.poisson_counts_device((100_000, 100_000, 1_000), 5_000_000, rank=16, seed=1)
+    model = gcp.GCP(idx, vals, dims, rank=32, loss="poisson", seed=1)
+    f0 = model.full_objective()
+    hist = model.fit(60, J_nz=1 << 16, J_z=1 << 16, lr=1e-2)
+    f1 = model.full_objective()
+    assert bool(torch.isfinite(hist).all())
+    assert np.isfinite(f1) and f1 < 0.1 * f0, (f0, f1)
+    assert min(float(u.detach().min()) for u in model.factors) >= 0.0
