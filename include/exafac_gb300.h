@@ -300,6 +300,21 @@ int exafac_gcp_sample_entries(int32_t N, const int64_t* dims_host, int64_t nnz, 
                               const void* nz_vals_dev, int64_t J_nz, int64_t J_z, uint64_t seed, uint64_t counter,
                               int32_t* idx_dev, void* x_dev, void* w_dev, int32_t dtype, void* stream);
 
+/* One Adam step over `count` (<= 8) device tensors of `dtype` in one launch,
+ * fused with the projection onto x >= lower when project != 0: per element
+ *   m = m + (1 - beta1) (g - m);  v = beta2 v + (1 - beta2) g^2;
+ *   p = p - lr / (1 - beta1^step) * m / (sqrt(v) / sqrt(1 - beta2^step) + eps);
+ *   p = max(p, lower)   (projection; a NaN stays NaN)
+ * in the tensors' own precision: the update of torch.optim.Adam (no weight
+ * decay, no amsgrad), the optimizer of gradient-based GCP, followed by the
+ * nonnegativity projection of its Poisson and Bernoulli losses.  `step` is
+ * the step count after this update (>= 1).  grads (or one entry of it) may be
+ * null: a zero gradient.  No reference counterpart (the reference has no
+ * GCP). */
+int exafac_adam_step(int32_t count, void* const* params_dev, const void* const* grads_dev, void* const* exp_avg_dev,
+                     void* const* exp_avg_sq_dev, const int64_t* numel_host, int32_t dtype, double lr, double beta1,
+                     double beta2, double eps, int64_t step, int32_t project, double lower, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

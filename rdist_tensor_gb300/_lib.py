@@ -83,6 +83,8 @@ SIGNATURES = {
     "exafac_cp_sampled_adjoint": (ctypes.c_int, [_I32, _I32, _P, _I64, _P, _P, _P, _P, _I32, _P, _P]),
     "exafac_gcp_sample_entries": (ctypes.c_int, [_I32, _P, _I64, _P, _P, _I64, _I64, ctypes.c_uint64,
                                                  ctypes.c_uint64, _P, _P, _P, _I32, _P]),
+    "exafac_adam_step": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _I32, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, _I64, _I32, ctypes.c_double, _P]),
 }
 
 _lib = None

@@ -10,9 +10,15 @@
 //             Khatri-Rao rows are recomputed here, never stored
 //   sampler   J_nz nonzeros uniformly (weight nnz / J_nz) and J_z coordinates
 //             uniformly (value 0, weight (prod dims - nnz) / J_z), Philox
+//   adam      one Adam step over all factors in one launch, fused with the
+//             projection onto nonnegative factors: 7 words of traffic per
+//             parameter (parameter, moments read and written; gradient read)
 //
 // The adjoint accumulates with atomic adds, so its last bits depend on the
 // order in which entries that share a row arrive.
+#include <cmath>
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace exafac {
@@ -130,6 +136,73 @@ __global__ void gcp_sample_kernel(int N, Dims dims, int64_t nnz, const int32_t* 
             }
             x_out[j] = T(0);
             w_out[j] = wz;
+        }
+    }
+}
+
+// Adam (Kingma and Ba; torch.optim.Adam's update without weight decay or
+// amsgrad), per element in the parameter's own precision:
+//   m = m + (1 - b1) (g - m);  v = b2 v + (1 - b2) g^2;
+//   p = p - step_size m / (sqrt(v) / sqrt(1 - b2^t) + eps),  step_size = lr / (1 - b1^t)
+// then p = max(p, lower) when projecting (a NaN stays NaN).  A null gradient
+// counts as zero (the moments still decay and the parameter still moves).
+struct AdamTensors {
+    void* p[kMaxModes];
+    const void* g[kMaxModes];
+    void* m[kMaxModes];
+    void* v[kMaxModes];
+    int64_t n[kMaxModes];
+};
+
+template <typename T>
+struct AdamCoef {
+    T step_size, omb1, b2, omb2, bc2_sqrt, eps, lower;
+    int project;
+};
+
+template <typename T>
+__device__ __forceinline__ void adam_elem(T& p, T g, T& m, T& v, const AdamCoef<T>& c) {
+    m = m + c.omb1 * (g - m);
+    v = c.b2 * v + c.omb2 * (g * g);
+    const T denom = sqrt(v) / c.bc2_sqrt + c.eps;
+    p = p - c.step_size * (m / denom);
+    if (c.project && p < c.lower) p = c.lower;
+}
+
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(256) adam_step_kernel(int count, AdamTensors ts, AdamCoef<T> c) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int t = 0; t < count; t++) {
+        T* __restrict__ p = static_cast<T*>(ts.p[t]);
+        const T* __restrict__ g = static_cast<const T*>(ts.g[t]);
+        T* __restrict__ m = static_cast<T*>(ts.m[t]);
+        T* __restrict__ v = static_cast<T*>(ts.v[t]);
+        const int64_t n = ts.n[t];
+        int64_t done = 0;
+        if constexpr (VEC) {  // float4 body; every base is 16-byte aligned
+            const int64_t nv = n >> 2;
+            for (int64_t i = tid; i < nv; i += stride) {
+                float4 P = reinterpret_cast<float4*>(p)[i];
+                const float4 G = g ? reinterpret_cast<const float4*>(g)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                float4 M = reinterpret_cast<float4*>(m)[i];
+                float4 V = reinterpret_cast<float4*>(v)[i];
+                adam_elem(P.x, G.x, M.x, V.x, c);
+                adam_elem(P.y, G.y, M.y, V.y, c);
+                adam_elem(P.z, G.z, M.z, V.z, c);
+                adam_elem(P.w, G.w, M.w, V.w, c);
+                reinterpret_cast<float4*>(p)[i] = P;
+                reinterpret_cast<float4*>(m)[i] = M;
+                reinterpret_cast<float4*>(v)[i] = V;
+            }
+            done = nv << 2;
+        }
+        for (int64_t i = done + tid; i < n; i += stride) {
+            T P = p[i], M = m[i], V = v[i];
+            adam_elem(P, g ? g[i] : T(0), M, V, c);
+            p[i] = P;
+            m[i] = M;
+            v[i] = V;
         }
     }
 }
@@ -252,3 +325,63 @@ extern "C" int exafac_gcp_sample_entries(int32_t N, const int64_t* dims, int64_t
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }
+
+template <typename T>
+static void launch_adam(int count, const AdamTensors& ts, int64_t total, double lr, double b1, double b2, double eps,
+                        int64_t step, int project, double lower, bool vec, cudaStream_t st) {
+    AdamCoef<T> c;
+    c.step_size = (T)(lr / (1.0 - std::pow(b1, (double)step)));
+    c.omb1 = (T)(1.0 - b1);
+    c.b2 = (T)b2;
+    c.omb2 = (T)(1.0 - b2);
+    c.bc2_sqrt = (T)std::sqrt(1.0 - std::pow(b2, (double)step));
+    c.eps = (T)eps;
+    c.lower = (T)lower;
+    c.project = project;
+    const int grid = grid_for(vec ? (total + 3) / 4 : total, 256);
+    if constexpr (std::is_same<T, float>::value) {
+        if (vec) {
+            adam_step_kernel<float, true><<<grid, 256, 0, st>>>(count, ts, c);
+            return;
+        }
+    }
+    adam_step_kernel<T, false><<<grid, 256, 0, st>>>(count, ts, c);
+}
+
+extern "C" int exafac_adam_step(int32_t count, void* const* params, const void* const* grads, void* const* exp_avg,
+                                void* const* exp_avg_sq, const int64_t* numel, int32_t dtype, double lr,
+                                double beta1, double beta2, double eps, int64_t step, int32_t project, double lower,
+                                void* stream) {
+    EXAFAC_ARG(count >= 0 && count <= kMaxModes, "count must be in [0, 8]");
+    GCP_DTYPE_ARG(dtype);
+    EXAFAC_ARG(step >= 1, "step must be >= 1 (the step count after this update)");
+    EXAFAC_ARG(beta1 >= 0.0 && beta1 < 1.0 && beta2 >= 0.0 && beta2 < 1.0, "betas must be in [0, 1)");
+    EXAFAC_ARG(eps >= 0.0 && lr >= 0.0, "lr and eps must be >= 0");
+    if (count == 0) return EXAFAC_OK;
+    EXAFAC_ARG(params && exp_avg && exp_avg_sq && numel, "null argument");
+    AdamTensors ts{};
+    int64_t total = 0;
+    bool vec = dtype == EXAFAC_DTYPE_F32;
+    for (int t = 0; t < count; t++) {
+        EXAFAC_ARG(numel[t] >= 0, "element counts must be >= 0");
+        EXAFAC_ARG(numel[t] == 0 || (params[t] && exp_avg[t] && exp_avg_sq[t]), "null parameter or moment");
+        ts.p[t] = params[t];
+        ts.g[t] = grads ? grads[t] : nullptr;
+        ts.m[t] = exp_avg[t];
+        ts.v[t] = exp_avg_sq[t];
+        ts.n[t] = numel[t];
+        total = std::max<int64_t>(total, numel[t]);
+        const uintptr_t a = (uintptr_t)ts.p[t] | (uintptr_t)ts.g[t] | (uintptr_t)ts.m[t] | (uintptr_t)ts.v[t];
+        if (a & 15u) vec = false;
+    }
+    if (total == 0) return EXAFAC_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dtype == EXAFAC_DTYPE_F32)
+        launch_adam<float>(count, ts, total, lr, beta1, beta2, eps, step, project, lower, vec, st);
+    else
+        launch_adam<double>(count, ts, total, lr, beta1, beta2, eps, step, project, lower, false, st);
+    count_launch();
+    EXAFAC_CHECK_LAUNCH();
+    return EXAFAC_OK;
+}
+

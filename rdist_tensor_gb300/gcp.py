@@ -121,9 +121,58 @@ def sample_entries(idx: torch.Tensor, vals: torch.Tensor, dims: Sequence[int], J
     return out_idx, x, w
 
 
+class FusedAdam:
+    """Adam over CUDA tensors in one launch per step of the library's fused
+    kernel (``exafac_adam_step``): torch.optim.Adam's update without weight
+    decay or amsgrad, in the parameters' own precision, followed when
+    ``lower`` is given by the projection onto x >= lower.  It reads each
+    parameter, gradient and moment once and writes the parameter and moments
+    once: 7 words per parameter, where torch's Adam plus a separate
+    projection pass moves 9.  A parameter without a gradient takes a zero
+    gradient (its moments still decay)."""
+
+    def __init__(self, params, lr: float = 1e-3, betas=(0.9, 0.999), eps: float = 1e-8, lower=None):
+        self.params = list(params)
+        if not self.params or len(self.params) > 8:
+            raise ValueError("FusedAdam takes 1 to 8 tensors")
+        dt = self.params[0].dtype
+        if dt not in _DTYPES:
+            raise ValueError("parameters must be float32 or float64")
+        for q in self.params:
+            if not q.is_cuda or q.dtype != dt or not q.is_contiguous():
+                raise ValueError("parameters must be contiguous CUDA tensors of one dtype")
+        self.lr, self.betas, self.eps, self.lower = float(lr), (float(betas[0]), float(betas[1])), float(eps), lower
+        self.dtype = dt
+        self.exp_avg = [torch.zeros_like(q, memory_format=torch.contiguous_format) for q in self.params]
+        self.exp_avg_sq = [torch.zeros_like(q, memory_format=torch.contiguous_format) for q in self.params]
+        self.steps = 0
+        self._numel = (ctypes.c_int64 * len(self.params))(*[q.numel() for q in self.params])
+
+    def zero_grad(self, set_to_none: bool = True):
+        for q in self.params:
+            if set_to_none:
+                q.grad = None
+            elif q.grad is not None:
+                q.grad.zero_()
+
+    @torch.no_grad()
+    def step(self):
+        grads = []
+        for q in self.params:
+            g = q.grad
+            if g is not None and (g.dtype != self.dtype or not g.is_contiguous()):
+                g = g.to(self.dtype).contiguous()
+            grads.append(g)
+        self.steps += 1
+        _lib.call("exafac_adam_step", len(self.params), _ptrs(self.params), _ptrs(grads), _ptrs(self.exp_avg),
+                  _ptrs(self.exp_avg_sq), self._numel, _DTYPES[self.dtype], self.lr, self.betas[0], self.betas[1],
+                  self.eps, self.steps, 0 if self.lower is None else 1,
+                  0.0 if self.lower is None else float(self.lower), _stream())
+
+
 class GCP:
     """Gradient-based GCP of a sparse tensor with stratified entry sampling,
-    Adam steps, and (for the Poisson and Bernoulli losses) nonnegative
+    fused Adam steps, and (for the Poisson and Bernoulli losses) nonnegative
     factors by projection after every step.  Factors start Uniform(0, 0.5)."""
 
     def __init__(self, idx, vals, dims: Sequence[int], rank: int, loss: str = "poisson",
@@ -170,29 +219,28 @@ class GCP:
         self.counter += 1
         return out
 
-    def optimizer(self, lr: float = 1e-2) -> torch.optim.Optimizer:
-        """The model's Adam optimizer (torch's fused CUDA Adam); its moments
+    def optimizer(self, lr: float = 1e-2) -> FusedAdam:
+        """The model's Adam optimizer, fused with the projection onto
+        nonnegative factors for the Poisson and Bernoulli losses; its moments
         persist across steps and fit calls while the rate stays the same."""
         if self._opt is None or self._lr != lr:
-            self._opt = torch.optim.Adam(self.factors, lr=lr, fused=True)
+            lower = 0.0 if self.loss in ("poisson", "bernoulli") else None
+            self._opt = FusedAdam(self.factors, lr=lr, lower=lower)
             self._lr = lr
         return self._opt
 
     def step(self, J_nz: int, J_z: int, lr: float = 1e-2) -> torch.Tensor:
         """One gradient step: a fresh stratified sample, the weighted loss on
-        it, its gradient through the sampled adjoint, an Adam update and (for
-        the Poisson and Bernoulli losses) the projection onto nonnegative
-        factors.  Returns the sampled objective as a device scalar; nothing is
-        read back to the host."""
+        it, its gradient through the sampled adjoint, and the fused Adam
+        update with (for the Poisson and Bernoulli losses) the projection onto
+        nonnegative factors.  Returns the sampled objective as a device
+        scalar; nothing is read back to the host."""
         opt = self.optimizer(lr)
         idx, x, w = self.step_sample(J_nz, J_z)
         opt.zero_grad(set_to_none=True)
         f = self.objective(idx, x, w)
         f.backward()
         opt.step()
-        if self.loss in ("poisson", "bernoulli"):
-            with torch.no_grad():
-                torch._foreach_clamp_min_(self.factors, 0.0)
         return f.detach()
 
     def fit(self, steps: int, J_nz: int, J_z: int, lr: float = 1e-2):

@@ -230,3 +230,46 @@ def test_gcp_reduced_config4_decreases_objective():
     assert bool(torch.isfinite(hist).all())
     assert np.isfinite(f1) and f1 < 0.1 * f0, (f0, f1)
     assert min(float(u.detach().min()) for u in model.factors) >= 0.0
+
+
+@pytest.mark.parametrize("dtype,tol", [("float32", 1e-6), ("float64", 1e-14)])
+def test_fused_adam_matches_torch_adam(dtype, tol):
+    """The fused Adam + projection kernel against torch.optim.Adam followed by
+    clamp_min over six steps: sizes that are and are not multiples of four,
+    one parameter without a gradient, and one with a misaligned (offset)
+    storage that takes the scalar path."""
+    gcp = _cuda()
+    dt = getattr(torch, dtype)
+    g = torch.Generator(device="cuda").manual_seed(4)
+    base = torch.rand(1003 * 7 + 1, generator=g, device="cuda", dtype=dt)
+    shapes = [(1000, 32), (37, 5), (1003, 7)]
+    ours = [torch.rand(s, generator=g, device="cuda", dtype=dt) for s in shapes[:2]]
+    ours.append(base[1:].view(shapes[2]))  # storage offset by one element
+    ref = [p.detach().clone() for p in ours]
+    # the aligned pair takes the float4 body (FP32); the offset tensor, in a
+    # launch of its own, the scalar path
+    opts = [gcp.FusedAdam(ours[:2], lr=3e-2, betas=(0.85, 0.995), eps=1e-7, lower=0.0),
+            gcp.FusedAdam(ours[2:], lr=3e-2, betas=(0.85, 0.995), eps=1e-7, lower=0.0)]
+    moments = [(o, k) for o in opts for k in range(len(o.params))]
+    topt = torch.optim.Adam(ref, lr=3e-2, betas=(0.85, 0.995), eps=1e-7)
+    for step in range(6):
+        grads = [torch.randn(s, generator=g, device="cuda", dtype=dt) for s in shapes]
+        for k, (p, q) in enumerate(zip(ours, ref)):
+            if k == 1 and step % 2 == 1:  # no gradient on odd steps
+                p.grad, q.grad = None, torch.zeros_like(q)
+            else:
+                p.grad, q.grad = grads[k], grads[k].clone()
+        for o in opts:
+            o.step()
+        topt.step()
+        with torch.no_grad():
+            for q in ref:
+                q.clamp_(min=0.0)
+    for k, (p, q) in enumerate(zip(ours, ref)):
+        err = torch.max(torch.abs(p - q)).item()
+        assert err <= tol, (k, err)
+        st = topt.state[q]
+        o, j = moments[k]
+        assert torch.allclose(o.exp_avg[j], st["exp_avg"], rtol=tol * 10, atol=tol)
+        assert torch.allclose(o.exp_avg_sq[j], st["exp_avg_sq"], rtol=tol * 10, atol=tol)
+    assert min(float(p.min()) for p in ours) >= 0.0
