@@ -315,7 +315,7 @@ def gcp_cpu_sample(dims, idx_np, vals_np, R, J_nz, J_z, lr, steps, seed=0):
 
 
 def run_gcp(args, w):
-    """Config-4 line: gradient-based Poisson GCP through the autograd sampled
+    """The GCP line: gradient-based Poisson GCP through the autograd sampled
     adjoint, K Adam steps timed with CUDA events after W warm-up steps, the
     tensor resident on the GPU."""
     import torch
@@ -873,7 +873,7 @@ def main():
     if w.get("kind") == "gcp":
         if args.impl == "reference":
             if int(os.environ.get("RANK", "0")) == 0:
-                print(json.dumps({"impl": "reference", "unavailable": "the reference has no GCP (config 4); its "
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no GCP; its "
                                                                       "CPU restatement is this line's cpu_baseline"}))
             return 0
         return run_gcp(args, w)

@@ -1,5 +1,5 @@
 """Host-side logic of bench.py that needs no GPU: the clock record of the
-timed region, the algorithmic-bytes formula, the config-4 CPU baseline and
+timed region, the algorithmic-bytes formula, the GCP workload's CPU baseline and
 reference line."""
 import datetime
 
@@ -42,7 +42,7 @@ def test_algorithmic_bytes_per_step():
 
 
 def test_gcp_cpu_baseline_runs():
-    """The config-4 CPU baseline (the GCP step restated with torch on the
+    """The GCP workload's CPU baseline (the GCP step restated with torch on the
     host) on a tiny tensor: it steps and reports a rate."""
     import numpy as np
 

@@ -213,8 +213,8 @@ def test_poisson_counts_device():
     assert abs(float(a.mean()) - 0.5) < 0.01 and abs(float(a.var()) - 0.5) < 0.03
 
 
-def test_gcp_reduced_config4_decreases_objective():
-    """Config 4's step (R = 32, J = 2^17 entries, Adam lr = 1e-2) on a
+def test_gcp_reduced_count_tensor_decreases_objective():
+    """The GCP workload's step (R = 32, J = 2^17 entries, Adam lr = 1e-2) on a
     reduced count tensor, 1e5 x 1e5 x 1e3 with 5e6 nonzeros: the exact
     objective over all entries falls (by two orders of magnitude in a torch
     CPU restatement of the same steps), and every sampled objective is
