@@ -92,8 +92,11 @@ int exafac_tree_sample(int64_t n, int32_t F, int32_t R, const double* G_dev, con
  * FP32 vectors (J x R, device) and node indices into G, packed upper
  * triangles (rows in order, node stride R (R + 1) / 2 rounded up to a
  * multiple of 4 floats).  use_tc = 1 (R >= 32): on the tensor cores
- * (tcgen05); 0: FP32 on the CUDA cores.  Slots of equal node next to each
- * other share one staging of the node. */
+ * (tcgen05); 2: the same arithmetic with the node's operand kept resident
+ * across tiles (the kernel of the root and shallow descent levels, for long
+ * runs of equal node; results equal to use_tc = 1 bit for bit); 0: FP32 on
+ * the CUDA cores.  Slots of equal node next to each other share one staging
+ * of the node. */
 int exafac_quad_forms_f32(int32_t R, int64_t J, const float* X_dev, const int64_t* node_dev, const float* G_dev,
                           float* q_dev, int32_t use_tc, void* stream);
 

@@ -363,8 +363,9 @@ __device__ __forceinline__ bool tc_product(TcBlock& b, Load4 load4) {
             }
             umma_commit(b.bar);
         }
-        // the MMAs have read the chunk (and, after the last, written Y)
-        if (!mbar_wait_limited(b.bar, b.phase, b.polls)) *b.abort_flag = 1;
+        // the MMAs have read the chunk (and, after the last, written Y):
+        // thread 0 waits on the barrier, the others at the block barrier
+        if (tid == 0 && !mbar_wait_limited(b.bar, b.phase, b.polls)) *b.abort_flag = 1;
         __syncthreads();
         if (*b.abort_flag) return false;
         b.phase ^= 1u;
@@ -713,12 +714,276 @@ fail:
     }
 }
 
+// ---- the resident-node level kernel: levels whose nodes each fill many tiles
+//
+// At the root and the shallow levels a node's slots fill many consecutive
+// tiles.  This kernel keeps the node's whole B operand (every K block, hi and
+// lo parts: 128 KB at R = 128) in shared memory and expands it again only when
+// the node changes; each block takes a contiguous range of tiles so that its
+// consecutive tiles share the node.  With B resident the slot tile is single
+// buffered: each thread keeps the x values its epilogue needs in registers,
+// so the next tile's slot copies start as soon as the MMAs of this tile are
+// done and land during the epilogue.  The arithmetic (operands, MMA order,
+// epilogue order) is that of bfs_level_tc_kernel: the results are the same
+// bit for bit.
+
+// Shared memory: B (every K block, hi and lo parts), one slot tile, 1 KB
+// alignment slack.
+size_t bfs_level_tcr_smem(int R) {
+    const TcLevelShape L = tc_level_shape(R);
+    return 2 * (size_t)L.nkb * L.b_kb + (size_t)L.nkb * L.a_kb + 1024;
+}
+
+// Average slots per node from which a descent level runs on the
+// resident-node kernel (64 tiles).  Below it the slots of a node are skewed
+// over fewer tiles, node changes become frequent, and the double-buffered
+// slot tiles of bfs_level_tc_kernel win (measured on GB300 at R = 128,
+// J = 2^19: the resident kernel 223 us against 266 us at 8192 slots per
+// node, 285 against 273 at 4096, 381 against 287 at 1024).
+constexpr int64_t kTcrMinSlotsPerNode = 64 * kTcRows;
+
+constexpr int kTcrExpand = (kMaxRank * kMaxRank / 4) / kTcLevelThreads;  // column groups per thread at most
+
+// The whole packed FP32 node P (global memory) as the B operand: hi = the
+// value, lo = the value minus its truncation to TF32, every K block.  All of
+// a thread's loads are issued before its swizzled stores.
+__device__ __forceinline__ void tcr_expand_node(const float* __restrict__ P, const int* rs, int R, unsigned char* Bhi,
+                                                unsigned char* Blo, const TcLevelShape& L) {
+    const int groups = L.Rn * (L.Rk / 4);  // (row, group of 4 columns), row fastest
+    float v[kTcrExpand][4];
+#pragma unroll
+    for (int it = 0; it < kTcrExpand; it++) {
+        const int e = threadIdx.x + it * kTcLevelThreads;
+        const int cg = e / L.Rn, n = e - cg * L.Rn;
+        const bool row_live = e < groups && n < R;
+        const int rn = row_live ? rs[n] : 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = 4 * cg + q;
+            v[it][q] = (row_live && k < R) ? __ldg(P + (k >= n ? rn + (k - n) : rs[k] + (n - k))) : 0.0f;
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < kTcrExpand; it++) {
+        const int e = threadIdx.x + it * kTcLevelThreads;
+        if (e < groups) {
+            const int cg = e / L.Rn, n = e - cg * L.Rn;
+            const uint32_t off = (uint32_t)(cg >> 3) * L.b_kb + (uint32_t)n * 128u +
+                                 ((((uint32_t)cg & 7u) ^ ((uint32_t)n & 7u)) * 16u);
+            *reinterpret_cast<float4*>(Bhi + off) = make_float4(v[it][0], v[it][1], v[it][2], v[it][3]);
+            *reinterpret_cast<float4*>(Blo + off) =
+                make_float4(v[it][0] - tf32_trunc(v[it][0]), v[it][1] - tf32_trunc(v[it][1]),
+                            v[it][2] - tf32_trunc(v[it][2]), v[it][3] - tf32_trunc(v[it][3]));
+        }
+    }
+}
+
+// MODE 0, 1 and 3 as bfs_level_kernel (MODE 2, whose leaves need no MMA,
+// stays on bfs_level_tc_kernel).
+template <int MODE>
+__global__ void __launch_bounds__(kTcLevelThreads, 1)
+    bfs_level_tcr_kernel(int R, const float* __restrict__ G, const float* __restrict__ X, int64_t J,
+                         const int32_t* __restrict__ order, int64_t* __restrict__ node, float2* __restrict__ lh,
+                         float* __restrict__ mroot, const double* __restrict__ dv, uint32_t* __restrict__ flag,
+                         DeviceStatus* status, uint32_t wait_polls) {
+    static_assert(MODE == 0 || MODE == 1 || MODE == 3, "the resident-node kernel takes MODE 0, 1 or 3");
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    __shared__ int32_t cs2[2][kTcRows];  // current node of each slot
+    __shared__ int32_t js2[2][kTcRows];  // sample of each slot
+    __shared__ uint32_t rm2[2][4];       // run starts of each header
+    __shared__ float qpart[4][kTcRows];
+    __shared__ int rs[kMaxRank];  // packed index of (a, a)
+    __shared__ __align__(8) uint64_t mbar;  // the MMAs
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    const TcLevelShape L = tc_level_shape(R);
+    unsigned char* base = tc_raw + ((1024u - (smem_u32(tc_raw) & 1023u)) & 1023u);
+    unsigned char* Bhi = base;
+    unsigned char* Blo = base + L.nkb * L.b_kb;
+    unsigned char* A = base + 2 * L.nkb * L.b_kb;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    if (w == 0) tmem_alloc(&tmem_base, L.ncols);
+    for (int a = tid; a < R; a += kTcLevelThreads) rs[a] = packed_index(R, a, a);
+    if (tid == 0) {
+        mbar_init(&mbar, 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = umma_idesc_tf32(kTcRows, L.Rn);
+    uint32_t mphase = 0;  // thread 0's
+    int64_t resident = -1;  // the node B holds (alike in every thread)
+    auto run_node = [&](int64_t c) -> int64_t { return MODE == 0 ? 0 : (MODE == 3 ? c : 2 * c + 1); };
+    // this block's contiguous range of tiles
+    const int64_t ntiles_all = (J + kTcRows - 1) / kTcRows;
+    const int64_t per = (ntiles_all + gridDim.x - 1) / gridDim.x;
+    const int64_t tfirst = (int64_t)blockIdx.x * per;
+    const int64_t tend = min(ntiles_all, tfirst + per);
+    auto tile_n = [&](int64_t tile) -> int { return (int)min((int64_t)kTcRows, J - tile * kTcRows); };
+    // the epilogue's share: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
+    // rows), column blocks of 16 part, part + 4 (at most two: Rn <= 128)
+    const int qw = w & 3, part = w >> 2, row = qw * 32 + lane;
+    const int ncb = L.Rn / 16;
+    int32_t hj = 0, hc = 0;  // header registers: slot tid of the tile two ahead
+    int it = 0;
+    for (int b = 0; b < 2; b++) {
+        const int64_t tile = tfirst + b;
+        if (tile < tend && tid < tile_n(tile)) {
+            const int32_t j = order ? order[tile * kTcRows + tid] : (int32_t)(tile * kTcRows + tid);
+            js2[b][tid] = j;
+            cs2[b][tid] = MODE == 0 ? 0 : (int32_t)node[j];
+        }
+    }
+    __syncthreads();
+    for (int b = 0; b < 2; b++) {
+        const int64_t tile = tfirst + b;
+        run_mask(cs2[b], tile < tend ? tile_n(tile) : 0, kTcRows, rm2[b]);
+    }
+    __syncthreads();
+    if (tfirst < tend) tc_issue_slots(A, X, js2[0], tile_n(tfirst), R, L);
+    for (int64_t tile = tfirst; tile < tend; tile++, it++) {
+        const int a = it & 1;
+        const int64_t s0 = tile * kTcRows;
+        const int n = tile_n(tile);
+        const int32_t* cs = cs2[a];
+        const int32_t* js = js2[a];
+        const uint32_t* rm = rm2[a];
+        const int64_t t1 = tile + 1, t2 = tile + 2;
+        const bool h_live = t2 < tend && tid < tile_n(t2);
+        if (h_live) hj = order ? order[t2 * kTcRows + tid] : (int32_t)(t2 * kTcRows + tid);
+        float2 pl = make_float2(0.f, 0.f);
+        float pm = 1.0f;
+        double pd = 0.0;
+        if (MODE == 1 && tid < n) {
+            const int32_t j = js[tid];
+            pl = lh[j];
+            pm = mroot[j];
+            pd = dv[j];
+        }
+        cp_async_wait<0>();        // this tile's slot copies
+        fence_proxy_async_smem();  // the slot tile, to the tensor core's proxy
+        __syncthreads();
+        if (h_live) hc = MODE == 0 ? 0 : (int32_t)node[hj];
+        // the epilogue's x values as x_hi + 2 x_lo, x_hi = x truncated to
+        // TF32 (what the MMA reads)
+        float xe[2][16];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int cb = part + 4 * i;
+#pragma unroll
+            for (int q4 = 0; q4 < 4; q4++) {
+                float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (cb < ncb) x = *reinterpret_cast<const float4*>(A + sw128_off(row, cb * 16 + 4 * q4, L.a_kb));
+                const float xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int qq = 0; qq < 4; qq++) {
+                    const float h = tf32_trunc(xs[qq]);
+                    xe[i][4 * q4 + qq] = fmaf(2.0f, xs[qq] - h, h);
+                }
+            }
+        }
+        for (int i0 = 0; i0 < n;) {  // runs of equal node (uniform over the block)
+            const int32_t c = cs[i0];
+            const int i1 = run_end(rm, 4, i0, n);
+            const int64_t g = run_node(c);
+            if (g != resident) {  // the MMAs that read B are done
+                tcr_expand_node(G + g * L.Pf, rs, R, Bhi, Blo, L);
+                fence_proxy_async_smem();
+                __syncthreads();
+                resident = g;
+            }
+            if (tid == 0) {
+                tc_fence_after();
+                for (int kb = 0; kb < L.nkb; kb++) {
+#pragma unroll
+                    for (int sub = 0; sub < 4; sub++) {
+                        const uint64_t ad = umma_desc_sw128(A + kb * L.a_kb + sub * 32);
+                        umma_tf32(tmem, ad, umma_desc_sw128(Bhi + kb * L.b_kb + sub * 32), idesc,
+                                  (kb > 0 || sub > 0) ? 1u : 0u);
+                        umma_tf32(tmem, ad, umma_desc_sw128(Blo + kb * L.b_kb + sub * 32), idesc, 1u);
+                    }
+                }
+                umma_commit(&mbar);
+                if (!mbar_wait_limited(&mbar, mphase, wait_polls)) abort_flag = 1;
+                mphase ^= 1u;
+            }
+            __syncthreads();  // the MMAs are done: Y is in TMEM, A and B are free
+            if (abort_flag) goto fail;
+            tc_fence_after();
+            // after the tile's last run the slot buffer takes the next tile
+            // (x is in registers); its copies land during this epilogue
+            if (i1 >= n && t1 < tend) tc_issue_slots(A, X, js2[a ^ 1], tile_n(t1), R, L);
+            {
+                float acc = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int cb = part + 4 * i;
+                    if (cb < ncb) {
+                        float y[16];
+                        tmem_ld16(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(cb * 16), y);
+#pragma unroll
+                        for (int q = 0; q < 16; q++) acc = fmaf(y[q], xe[i][q], acc);
+                    }
+                }
+                qpart[part][row] = acc;
+            }
+            tc_fence_before();
+            __syncthreads();
+            if (tid >= i0 && tid < i1) {  // slot tid, with its prefetched inputs
+                const float q = (qpart[0][tid] + qpart[1][tid]) + (qpart[2][tid] + qpart[3][tid]);
+                const int32_t j = js[tid];
+                if (MODE == 0 || MODE == 3) {
+                    mroot[j] = q;
+                } else {
+                    const float cutoff = pl.x + q / pm;
+                    const bool left = (float)pd <= cutoff;
+                    node[j] = left ? 2 * (int64_t)c + 1 : 2 * (int64_t)c + 2;
+                    lh[j] = left ? make_float2(pl.x, cutoff) : make_float2(cutoff, pl.y);
+                    flag[s0 + tid] = left ? 1u : 0u;
+                }
+            }
+            i0 = i1;
+        }
+        __syncthreads();  // this tile is done with js2 / cs2 [a] and qpart
+        if (h_live) {
+            js2[a][tid] = hj;
+            cs2[a][tid] = hc;
+        }
+        __syncthreads();
+        run_mask(cs2[a], t2 < tend ? tile_n(t2) : 0, kTcRows, rm2[a]);  // read after the next iteration's barriers
+    }
+    cp_async_wait<0>();
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L.ncols);
+    }
+    return;
+fail:
+    cp_async_wait<0>();
+    if (tid == 0) {
+        report(status, EXAFAC_ERR_TIMEOUT, 21, blockIdx.x, 0);
+        mbar_wait_limited(&mbar, mphase, wait_polls);  // the MMAs in flight may still complete (bounded)
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, L.ncols);
+    }
+}
+
 // Leaf stage on the tensor cores (F > 1, F <= Rn): Y[r] = U_r . x for the
-// leaf's rows, then in each sample's own thread the squared dots' inclusive
-// prefix in row order and the first row r < F - 1 with frac < prefix_r /
-// total, else the last row the leaf holds (as bfs_leaf_kernel).  Warps 0-3
-// hold the lanes; a thread keeps its row's squares in registers, 16 columns
-// per TMEM load.
+// leaf's rows, then for each sample the squared dots' inclusive prefix in row
+// order and the first row r < F - 1 with frac x total < prefix_r, else the
+// last row the leaf holds (the rule of bfs_leaf_kernel).  All sixteen warps
+// share the epilogue: each thread holds one slot's squares for a slice of 32
+// leaf rows (two TMEM loads), the slices' sums meet in shared memory, and the
+// slice that holds the crossing names the row.
 __global__ void __launch_bounds__(kTcThreads, 1)
     bfs_leaf_tc_kernel(int R, TreeShape t, const float* __restrict__ U, const float* __restrict__ X, int64_t J,
                        const int32_t* __restrict__ order, const int64_t* __restrict__ node,
@@ -729,6 +994,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __shared__ int64_t cs[kTcRows];
     __shared__ int32_t js[kTcRows];
     __shared__ uint32_t rmask[kTcRows / 32];
+    __shared__ float psum[4][kTcRows];  // squared dots summed over each slice of 32 leaf rows
+    __shared__ int pick[kTcRows];       // the row each slot takes
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
@@ -747,11 +1014,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         __syncthreads();
         tc_stage_slots(b, R, X, js, n);
-        run_mask(cs, n, kBfsTile, rmask);
+        run_mask(cs, n, kTcRows, rmask);
         __syncthreads();
         for (int i0 = 0; i0 < n;) {
             const int64_t c = cs[i0];
-            const int i1 = run_end(rmask, kBfsTile / 32, i0, n);
+            const int i1 = run_end(rmask, kTcRows / 32, i0, n);
             const int64_t leaf = tree_leaf_idx(t, c);
             const int rows = (int)min((int64_t)F, t.n - leaf * F);
             const float* Ub = U + leaf * F * R;
@@ -775,50 +1042,80 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 tc_end(b, status, 21);
                 return;
             }
-            if (w < 4) {
-                const int row = w * 32 + lane;  // this thread's slot in the tile
-                const bool mine = row >= i0 && row < i1;
-                const uint32_t tl = b.tmem + ((uint32_t)(w * 32) << 16);
+            {
+                // Every warp: lane quarter qw (slots 32 qw .. + 31) and a
+                // slice of 32 leaf rows (columns of Y).  The squared dots'
+                // slice sums go through shared memory; the slot's total and
+                // the sums before each slice follow, and the one slice whose
+                // range [before, before + sum) holds frac x total reports the
+                // first row r < F - 1 of it with frac x total < prefix_r
+                // (the inverse-CDF pick of the row in row order).
+                const int qw = w & 3, part = w >> 2;
+                const int row = qw * 32 + lane;  // this thread's slot in the tile
+                const int c0 = part * 32;
                 const int nb = b.L.Rn / 16;
-                float total = 0.0f;  // the squared dots summed in row order
-                for (int cb = 0; cb < nb; cb++) {
-                    float y[16];
-                    tmem_ld16(tl + (uint32_t)(cb * 16), y);
+                const int fr = min(F, b.L.Rn);   // leaf rows that have a column
+                const uint32_t tl = b.tmem + ((uint32_t)(qw * 32) << 16);
+                float y[2][16];
+                float ps = 0.0f;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int cb = 2 * part + h;
+                    if (cb < nb) {
+                        tmem_ld16(tl + (uint32_t)(cb * 16), y[h]);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 16; q++) y[h][q] = 0.0f;
+                    }
 #pragma unroll
                     for (int q = 0; q < 16; q++)
-                        if (cb * 16 + q < F) total += y[q] * y[q];
+                        if (c0 + 16 * h + q < fr) ps = fmaf(y[h][q], y[h][q], ps);
                 }
+                psum[part][row] = ps;
+                if (part == 0) pick[row] = F - 1;
+                __syncthreads();
+                const bool mine = row >= i0 && row < i1;
                 const int32_t j = mine ? js[row] : 0;
-                const bool is_empty = !(total > 0.0f);
-                float frac = 0.0f;
-                if (mine && !is_empty) {
-                    const float2 bnd = lh[j];
-                    frac = ((float)dv[j] - bnd.x) / (bnd.y - bnd.x);
-                }
-                // the same sum again, stopping at the first r < F - 1 with
-                // frac < prefix_r / total (prefix_{F-1} equals total)
-                int res = F - 1;
-                bool found = !mine || is_empty;
-                float prefix = 0.0f;
-                for (int cb = 0; cb < nb; cb++) {
-                    if (__all_sync(0xffffffffu, found)) break;
-                    float y[16];
-                    tmem_ld16(tl + (uint32_t)(cb * 16), y);
+                float before = 0.0f, total = 0.0f;
 #pragma unroll
-                    for (int q = 0; q < 16; q++) {
-                        const int r = cb * 16 + q;
-                        if (!found && r < F - 1) {
-                            prefix += y[q] * y[q];
-                            if (frac < prefix / total) {
-                                res = r;
-                                found = true;
+                for (int p = 0; p < 4; p++) {
+                    if (p == part) before = total;
+                    total += psum[p][row];
+                }
+                const bool is_empty = !(total > 0.0f);
+                if (mine && !is_empty && c0 < fr) {
+                    const float2 bnd = lh[j];
+                    const float frac = ((float)dv[j] - bnd.x) / (bnd.y - bnd.x);
+                    const float thr = frac * total;
+                    const bool last_slice = c0 + 32 >= fr;
+                    const bool lo_ok = part == 0 || thr >= before;
+                    const bool hi_ok = last_slice || thr < before + psum[part][row];
+                    if (lo_ok && hi_ok) {
+                        int res = min(c0 + 31, fr - 1);  // rounding: the slice's last row
+                        if (last_slice) res = F - 1;
+                        float prefix = before;
+                        bool found = false;
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+#pragma unroll
+                            for (int q = 0; q < 16; q++) {
+                                const int r = c0 + 16 * h + q;
+                                prefix = fmaf(y[h][q], y[h][q], prefix);
+                                if (!found && r < F - 1 && r < fr && thr < prefix) {
+                                    res = r;
+                                    found = true;
+                                }
                             }
                         }
+                        pick[row] = res;
                     }
                 }
-                if (mine) {
+                __syncthreads();
+                if (mine && part == 0) {
+                    const int rows_here = rows;
+                    int res = pick[row];
                     if (is_empty) res = 0;
-                    else if (res >= rows) res = rows - 1;  // frac >= 1 in a partial leaf
+                    else if (res >= rows_here) res = rows_here - 1;  // frac >= 1 in a partial leaf
                     samples[(int64_t)j * N + col] = (uint32_t)(leaf * F + res);
                     if (is_empty) empty[j] = 1;
                 }
@@ -916,11 +1213,11 @@ __global__ void __launch_bounds__(kBfsWarps * 32) bfs_leaf_kernel(int R, TreeSha
             cs[i] = node[j];
         }
         __syncthreads();
-        run_mask(cs, n, kTcRows, rmask);
+        run_mask(cs, n, kBfsTile, rmask);
         __syncthreads();
         for (int i0 = 0; i0 < n;) {
             const int64_t c = cs[i0];
-            const int i1 = run_end(rmask, kTcRows / 32, i0, n);
+            const int i1 = run_end(rmask, kBfsTile / 32, i0, n);
             const int64_t leaf = tree_leaf_idx(t, c);
             const int rows = (int)min((int64_t)F, t.n - leaf * F);
             const float* Ub = U + leaf * F * R;
@@ -1060,18 +1357,28 @@ static void bfs_set_smem_limits() {
     cudaFuncSetAttribute(bfs_level_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     cudaFuncSetAttribute(bfs_level_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
     cudaFuncSetAttribute(bfs_leaf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tlsm);
+    const int rsm = (int)bfs_level_tcr_smem(kMaxRank);
+    cudaFuncSetAttribute(bfs_level_tcr_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm);
+    cudaFuncSetAttribute(bfs_level_tcr_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm);
+    cudaFuncSetAttribute(bfs_level_tcr_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm);
     done = true;
 }
 
 // One level (MODE as bfs_level_kernel) over slots order[0 .. J) of the packed
-// FP32 nodes G: on the tensor cores when use_tc (R >= kTcMinRank), else on
-// the CUDA cores.
+// FP32 nodes G: on the tensor cores when use_tc (R >= kTcMinRank), with the
+// node kept resident when `resident` (long runs: the root and shallow levels;
+// MODE 0, 1 and 3), else on the CUDA cores.
 template <int MODE>
-static void bfs_level_launch(bool use_tc, int R, const float* G, const float* X, int64_t J, const int32_t* order,
-                             int64_t* node, float2* lh, float* m, const double* dv, uint32_t* flag, const TreeShape& t,
-                             DeviceStatus* status, uint32_t polls, cudaStream_t st) {
+static void bfs_level_launch(bool use_tc, bool resident, int R, const float* G, const float* X, int64_t J,
+                             const int32_t* order, int64_t* node, float2* lh, float* m, const double* dv,
+                             uint32_t* flag, const TreeShape& t, DeviceStatus* status, uint32_t polls,
+                             cudaStream_t st) {
     const int Pf = packed_stride_f32(R);
-    if (use_tc) {
+    if (use_tc && resident && MODE != 2) {
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
+        bfs_level_tcr_kernel<MODE == 2 ? 1 : MODE><<<blocks, kTcLevelThreads, bfs_level_tcr_smem(R), st>>>(
+            R, G, X, J, order, node, lh, m, dv, flag, status, polls);
+    } else if (use_tc) {
         const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kTcRows), 152));
         bfs_level_tc_kernel<MODE><<<blocks, kTcLevelThreads, bfs_level_tc_smem(R), st>>>(R, G, X, J, order, node, lh,
                                                                                        m, dv, flag, t, status, polls);
@@ -1097,7 +1404,7 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
     bfs_reset_kernel<<<grid_for_elems(J), 256, 0, st>>>(J, b.node, b.lh, b.order[b.cur], b.off[0], 1);
     count_launch();
     const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(J, kBfsTile), kBfsBlocks));
-    bfs_level_launch<0>(tc, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
+    bfs_level_launch<0>(tc, true, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
     int oi = 0;                  // off[oi]: the current level's slot ranges
     int64_t lb = 0, nl = 1;      // the level's first node and node count
     const int64_t levels = t.lfill_level;
@@ -1108,9 +1415,11 @@ static int bfs_descend(Session& s, const TreeShape& t, const float* G, const flo
         const bool is_tail = lvl == levels;
         if (is_tail && !tail) break;
         if (is_tail)
-            bfs_level_launch<2>(tc, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
+            bfs_level_launch<2>(tc, false, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status,
+                                polls, st);
         else
-            bfs_level_launch<1>(tc, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv, b.flag, t, s.status, polls, st);
+            bfs_level_launch<1>(tc, J >= kTcrMinSlotsPerNode * nl, R, G, X, J, b.order[b.cur], b.node, b.lh, b.m, dv,
+                                b.flag, t, s.status, polls, st);
         EXAFAC_TRY(scan_exclusive_u32_to_i64(b.flag, b.SL, J, b.SL + J, s.scan_sc, st));
         if (!is_tail) {
             bfs_offsets_kernel<<<grid_for_elems(nl), 256, 0, st>>>(nl, J, b.off[oi], b.SL, b.off[oi ^ 1]);
@@ -1166,7 +1475,7 @@ int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t s
         count_launch();
     }
     // h^T Phi h (one node: Phi), then the weights
-    bfs_level_launch<0>(R >= kTcMinRank, R, s.PhiPF, b.h, J, b.order[b.cur], b.node, b.lh, b.m, nullptr, b.flag,
+    bfs_level_launch<0>(R >= kTcMinRank, true, R, s.PhiPF, b.h, J, b.order[b.cur], b.node, b.lh, b.m, nullptr, b.flag,
                         s.etree, s.status, s.wait_polls ? s.wait_polls : kSpinLimit, st);
     bfs_weight_kernel<<<grid_for_elems(J), 256, 0, st>>>(R, J, b.m, b.empty, s.weights);
     count_launch();
@@ -1183,11 +1492,12 @@ extern "C" int exafac_quad_forms_f32(int32_t R, int64_t J, const float* X, const
     EXAFAC_ARG(R >= 1 && R <= kMaxRank, "exafac_quad_forms_f32: R out of range");
     EXAFAC_ARG(J >= 1 && J <= INT32_MAX, "exafac_quad_forms_f32: J out of range");
     EXAFAC_ARG(X && node && G && q, "exafac_quad_forms_f32: null pointer");
+    EXAFAC_ARG(use_tc >= 0 && use_tc <= 2, "exafac_quad_forms_f32: use_tc must be 0, 1 or 2");
     EXAFAC_ARG(!use_tc || R >= kTcMinRank, "exafac_quad_forms_f32: the tensor-core form needs R >= 32");
     bfs_set_smem_limits();
     TreeShape t{};
-    bfs_level_launch<3>(use_tc != 0, R, G, X, J, nullptr, const_cast<int64_t*>(node), nullptr, q, nullptr, nullptr, t,
-                        nullptr, kSpinLimit, (cudaStream_t)stream);
+    bfs_level_launch<3>(use_tc != 0, use_tc == 2, R, G, X, J, nullptr, const_cast<int64_t*>(node), nullptr, q, nullptr,
+                        nullptr, t, nullptr, kSpinLimit, (cudaStream_t)stream);
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
 }

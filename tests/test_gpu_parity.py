@@ -323,6 +323,50 @@ def test_mixed_sts_distribution(lib, oracle_mod, precision, R):
     opt.deinitialize()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "tf32"])
+@pytest.mark.parametrize("R", [16, 40])
+def test_mixed_sts_distribution_many_leaves(lib, oracle_mod, precision, R):
+    """The STS-CP draws through row trees of many leaves: a 40 x 4000 x 9
+    tensor, draws for mode 0, whose mode-1 tree has 4000 / R leaves (250 at
+    R = 16 on the CUDA-core leaf kernel, 100 at R = 40 on the tensor-core
+    one), so that leaf boundaries fall anywhere inside the leaf stage's slot
+    tiles.  J = 2^18 seeded draws; Pearson's chi-square of the mode-1 and
+    mode-2 marginals against the exact leverage distribution, p > 1e-4."""
+    from scipy.stats import chi2
+
+    from rdist_tensor_gb300 import synthetic
+
+    dims = (40, 4000, 9)
+    rng = np.random.default_rng(17)
+    nnz = 20000
+    idx = np.stack([rng.integers(0, d, nnz) for d in dims], axis=1).astype(np.uint32)
+    idx = np.unique(idx, axis=0)
+    vals = rng.standard_normal(idx.shape[0])
+    factors = synthetic.gaussian_factors(dims, R, seed=13)
+    J = 1 << 18
+    opt, lr = make_optimizer_prec(dims, idx, vals, factors, "sts_cp", J, precision)
+    uni = dev(rng.random((3, 2, J)), torch.float64)
+    s, w = opt.draw(0, J, uni)
+    s = s.cpu().numpy().astype(np.int64)
+    cells = np.array([(a, b) for a in range(dims[1]) for b in range(dims[2])])
+    full = np.zeros((cells.shape[0], 3), dtype=np.uint32)
+    full[:, 1], full[:, 2] = cells[:, 0], cells[:, 1]
+    p = sts_quadratic_forms(factors, full, 0)
+    p = (p / p.sum()).reshape(dims[1], dims[2])
+    for k, marg in ((1, p.sum(axis=1)), (2, p.sum(axis=0))):
+        obs = np.bincount(s[:, k], minlength=dims[k])
+        exp = marg * J
+        live = exp > 0
+        assert obs[~live].sum() == 0
+        stat = float(np.sum((obs[live] - exp[live]) ** 2 / exp[live]))
+        pval = float(chi2.sf(stat, live.sum() - 1))
+        print(f"{precision} R={R} mode-{k} marginal: chi2 {stat:.1f} dof {live.sum() - 1} p {pval:.3g}")
+        assert pval > 1e-4
+    qs = sts_quadratic_forms(factors, s.astype(np.uint32), 0)
+    assert rel_err(w.cpu().numpy(), R / (qs * J)) < (1e-12 if precision == "fp64" else 1e-5)
+    opt.deinitialize()
+
+
 @pytest.mark.parametrize("R", [16, 48, 100])
 @pytest.mark.parametrize("precision", ["tf32", "bf16"])
 @pytest.mark.parametrize("sampler", ["cp_arls_lev", "sts_cp"])

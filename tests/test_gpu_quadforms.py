@@ -45,8 +45,10 @@ def make_nodes(R, count, rng):
 def test_quad_forms(lib, R, layout):
     """J = 1000 (not a multiple of the 128-slot tile), 37 nodes; "runs":
     slots sorted by node (the descents' layout), "scattered": every slot
-    its own run.  |q - q_exact| <= 1e-5 x^T |A| x on both paths (FP32 and
-    TF32 hi + lo), and the two paths agree to the same bound."""
+    its own run.  |q - q_exact| <= 1e-5 x^T |A| x on every path (FP32, TF32
+    hi + lo, and TF32 hi + lo with the node resident), the FP32 and TF32
+    paths agree to the same bound, and the two tensor-core kernels agree bit
+    for bit."""
     rng = np.random.default_rng(R)
     J, nodes = 1000, 37
     full, packed = make_nodes(R, nodes, rng)
@@ -59,9 +61,9 @@ def test_quad_forms(lib, R, layout):
     scale = np.einsum("jr,jrs,js->j", np.abs(X64), np.abs(full[node]), np.abs(X64))
     Xd = torch.as_tensor(X).cuda()
     nd = torch.as_tensor(node.astype(np.int64)).cuda()
-    Gd = {0: torch.as_tensor(packed).cuda(), 1: torch.as_tensor(packed).cuda()}
+    Gd = {tc: torch.as_tensor(packed).cuda() for tc in (0, 1, 2)}
     out = {}
-    for tc in (0, 1):
+    for tc in (0, 1, 2):
         q = torch.full((J,), float("nan"), dtype=torch.float32, device="cuda")
         lib.call("exafac_quad_forms_f32", R, J, ctypes.c_void_p(Xd.data_ptr()), ctypes.c_void_p(nd.data_ptr()),
                  ctypes.c_void_p(Gd[tc].data_ptr()), ctypes.c_void_p(q.data_ptr()), tc, None)
@@ -72,6 +74,41 @@ def test_quad_forms(lib, R, layout):
         assert np.all(np.isfinite(out[tc]))
         assert err < 1e-5
     assert np.max(np.abs(out[1] - out[0]) / scale) < 2e-5
+    assert np.array_equal(out[2], out[1])
+
+
+@pytest.mark.parametrize("R", [64, 100, 128])
+@pytest.mark.parametrize("layout", ["runs", "scattered"])
+def test_quad_forms_resident_many_tiles(lib, R, layout):
+    """The resident-node kernel over more tiles than blocks (J = 60,001: 469
+    tiles, four per block, a partial last tile): its contiguous tile ranges,
+    single slot buffer refilled during the epilogue, and node changes within
+    and between tiles; bit for bit equal to bfs_level_tc_kernel and within
+    1e-5 x^T |A| x of FP64."""
+    rng = np.random.default_rng(7 * R)
+    J, nodes = 60_001, 6
+    full, packed = make_nodes(R, nodes, rng)
+    X = rng.standard_normal((J, R)).astype(np.float32)
+    node = rng.integers(0, nodes, J)
+    if layout == "runs":
+        node = np.sort(node)
+    X64 = X.astype(np.float64)
+    exact = np.einsum("jr,jrs,js->j", X64, full[node], X64)
+    scale = np.einsum("jr,jrs,js->j", np.abs(X64), np.abs(full[node]), np.abs(X64))
+    Xd = torch.as_tensor(X).cuda()
+    nd = torch.as_tensor(node.astype(np.int64)).cuda()
+    Gd = torch.as_tensor(packed).cuda()
+    out = {}
+    for tc in (1, 2):
+        q = torch.full((J,), float("nan"), dtype=torch.float32, device="cuda")
+        lib.call("exafac_quad_forms_f32", R, J, ctypes.c_void_p(Xd.data_ptr()), ctypes.c_void_p(nd.data_ptr()),
+                 ctypes.c_void_p(Gd.data_ptr()), ctypes.c_void_p(q.data_ptr()), tc, None)
+        torch.cuda.synchronize()
+        out[tc] = q.cpu().numpy().astype(np.float64)
+    err = np.max(np.abs(out[2] - exact) / scale)
+    print(f"R={R} {layout}: resident-node kernel max error / (x^T |A| x) = {err:.2e}")
+    assert np.all(np.isfinite(out[2])) and err < 1e-5
+    assert np.array_equal(out[2], out[1])
 
 
 def test_quad_forms_repeat(lib):
