@@ -636,10 +636,13 @@ __global__ void spd_pinv_packed_kernel(int R, const double* __restrict__ A, doub
         const double lkk = L[tri(k, k)];
         for (int i = k + 1 + tid; i < R; i += nt) L[tri(i, k)] /= lkk;
         __syncthreads();
-        const int m = R - k - 1;
-        for (int e = tid; e < m * m; e += nt) {
-            const int i = k + 1 + e / m, j = k + 1 + e % m;
-            if (j <= i) L[tri(i, j)] -= L[tri(i, k)] * L[tri(j, k)];
+        {  // the trailing lower triangle: a warp per row, its lanes along the row
+            const int wid = tid >> 5, lane = tid & 31, nw = nt >> 5;
+            for (int i = k + 1 + wid; i < R; i += nw) {
+                const double lik = L[tri(i, k)];
+                double* row = L + tri(i, 0);
+                for (int j = k + 1 + lane; j <= i; j += 32) row[j] -= lik * L[tri(j, k)];
+            }
         }
         __syncthreads();
     }
@@ -652,12 +655,13 @@ __global__ void spd_pinv_packed_kernel(int R, const double* __restrict__ A, doub
         }
         __syncthreads();
         double part = 0.0;
-        for (int e = tid; e < R * R; e += nt) {
+        for (int e = tid; e < R * R; e += nt) {  // (a, b), a <= b, computed once and mirrored
             const int a = e / R, b = e % R;
-            const int k0 = a > b ? a : b;
-            const double acc = gram_dot(Li, a, b, k0, R);
-            out[e] = acc;
-            part += acc * acc;
+            if (a > b) continue;
+            const double acc = gram_dot(Li, a, b, b, R);
+            out[a * R + b] = acc;
+            out[b * R + a] = acc;
+            part += (a == b ? 1.0 : 2.0) * (acc * acc);
         }
         part = warp_sum(part);
         if ((tid & 31) == 0) fro_w[tid >> 5] = part;
@@ -908,13 +912,16 @@ __device__ void chol_packed_block(int R, double* L, int* piv, double stop, doubl
         for (int i = k + 1 + tid; i < R; i += nt) col[i] = L[tri(i, k)] / lkk;
         __syncthreads();
         if (tid == 0) L[tri(k, k)] = lkk;
-        const int m = R - k - 1;
-        for (int e = tid; e < m * m; e += nt) {
-            const int i = k + 1 + e / m, j = k + 1 + e % m;
-            if (j < i) L[tri(i, j)] -= col[i] * col[j];
-            else if (j == i) {
-                L[tri(i, i)] -= col[i] * col[i];
-                L[tri(i, k)] = col[i];
+        {  // the trailing lower triangle: a warp per row, its lanes along the row
+            const int wid = tid >> 5, lane = tid & 31, nw = nt >> 5;
+            for (int i = k + 1 + wid; i < R; i += nw) {
+                const double ci = col[i];
+                double* row = L + tri(i, 0);
+                for (int j = k + 1 + lane; j < i; j += 32) row[j] -= ci * col[j];
+                if (lane == 0) {
+                    row[i] -= ci * ci;
+                    row[k] = ci;
+                }
             }
         }
         __syncthreads();
@@ -935,13 +942,11 @@ __global__ void sts_phi_chol_kernel(int N, int n, int R, int first, double tol, 
     double* Li = smem + P;
     const double* A = chain + (int64_t)first * R2;
     double* EN = E + (int64_t)N * R2;
-    for (int e = tid; e < P; e += nt) {
-        int i = 0;
-        while (tri(i + 1, 0) <= e) i++;
-        const int j = e - tri(i, 0);
-        L[e] = A[j * R + i];  // upper triangle of A
-        Li[e] = 0.0;
-    }
+    for (int i = tid >> 5; i < R; i += nt >> 5)  // a warp per row of the packed lower triangle
+        for (int j = tid & 31; j <= i; j += 32) {
+            L[tri(i, j)] = A[j * R + i];  // upper triangle of A
+            Li[tri(i, j)] = 0.0;
+        }
     __syncthreads();
     int rank;
     chol_packed_block(R, L, nullptr, 0.0, col, &rank);
@@ -955,12 +960,13 @@ __global__ void sts_phi_chol_kernel(int N, int n, int R, int first, double tol, 
         }
         __syncthreads();
         double part = 0.0;
-        for (int e = tid; e < R2; e += nt) {  // Phi = L^{-T} L^{-1}
+        for (int e = tid; e < R2; e += nt) {  // Phi = L^{-T} L^{-1}: (a, b), a <= b, once and mirrored
             const int a = e / R, b = e % R;
-            const int k0 = a > b ? a : b;
-            const double acc = gram_dot(Li, a, b, k0, R);
-            Phi[e] = acc;
-            part += acc * acc;
+            if (a > b) continue;
+            const double acc = gram_dot(Li, a, b, b, R);
+            Phi[a * R + b] = acc;
+            Phi[b * R + a] = acc;
+            part += (a == b ? 1.0 : 2.0) * (acc * acc);
         }
         part = warp_sum(part);
         if ((tid & 31) == 0) fro_w[tid >> 5] = part;
@@ -1008,17 +1014,13 @@ __global__ void sts_chain_chol_kernel(int N, int n, int R, const double* __restr
     __shared__ double dmax_w[32];
     const int k = blockIdx.x;
     if (k == 0 || k == n || k >= N) return;
-    const int P = R * (R + 1) / 2, R2 = R * R;
+    const int R2 = R * R;
     const int tid = threadIdx.x, nt = blockDim.x;
     const double* A = chain + (int64_t)k * R2;
     double* Ek = E + (int64_t)k * R2;
     double* L = smem;
-    for (int e = tid; e < P; e += nt) {
-        int i = 0;
-        while (tri(i + 1, 0) <= e) i++;
-        const int j = e - tri(i, 0);
-        L[e] = A[j * R + i];
-    }
+    for (int i = tid >> 5; i < R; i += nt >> 5)  // a warp per row of the packed lower triangle
+        for (int j = tid & 31; j <= i; j += 32) L[tri(i, j)] = A[j * R + i];
     double dm = 0.0;
     for (int i = tid; i < R; i += nt) dm = fmax(dm, A[i * R + i]);
     for (int o = 16; o > 0; o >>= 1) dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
