@@ -28,10 +28,15 @@ preprocessing (decompose.py:82-96).
   e2e        the same metric through the public API with host buffers: every
              sweep copies its uniform draws from pinned host memory (on a copy
              stream, overlapping the previous sweep) and reads sigma back.
-  roofline   sampled MTTKRP (fibre lookup, hit grouping, weighted reduction
-             fused with the R x R solve) against the measured HBM copy
-             bandwidth; algorithmic bytes per step (see algorithmic_bytes)
-             summed over a sweep, divided by the region's CUDA-event time.
+  roofline   the dominant kernel against the measured HBM copy bandwidth:
+             for the mixed STS-CP forms at R >= 32 the resident-node tcgen05
+             level kernel (level_kernel_roofline; the double-buffered one of
+             the deeper levels in roofline_deep_levels, the sampled MTTKRP
+             region in roofline_sampled_mttkrp); otherwise the sampled
+             MTTKRP (fibre lookup, hit grouping, weighted reduction fused
+             with the R x R solve): algorithmic bytes per step (see
+             algorithmic_bytes) summed over a sweep, divided by the region's
+             CUDA-event time.
   cpu_baseline  the oracle port of the reference on this machine's cores
              (a bounded sample, scaled to the workload: see its "sample").
 
@@ -180,18 +185,20 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def level_kernel_roofline(R, J, nodes=1024, launches=5, seed=0):
-    """Roofline of the mixed forms' dominant kernel, the tcgen05 level kernel
-    of the breadth-first STS-CP descents, timed live: exafac_quad_forms_f32 on
-    the tensor cores (the level kernel's quadratic forms, without the branch
-    epilogue) over J FP32 vectors of rank R, slots sorted by node over
-    `nodes` distinct packed nodes, as at a middle level of a descent.  One
-    launch reads every vector once (J R 4 bytes, gathered rows) and each
-    node's packed Gram once; its tensor-core work is two TF32 MMAs per K step
-    (2 J R^2 multiply-adds) against the 2 J R^2 flops of the forms.  CUDA
-    events on the launching stream, the average of `launches` launches after
-    two warm-up launches; inputs (J R 4 bytes, 268 MB at J = 2^19, R = 128)
-    larger than L2."""
+def level_kernel_roofline(R, J, nodes=64, use_tc=2, launches=5, seed=0):
+    """Roofline of a tcgen05 level kernel of the mixed forms' breadth-first
+    STS-CP descents, timed live: exafac_quad_forms_f32 (the level kernel's
+    quadratic forms, without the branch epilogue) over J FP32 vectors of
+    rank R, slots sorted by node over `nodes` distinct packed nodes.
+    use_tc = 2: the resident-node kernel (bfs_level_tcr_kernel, the root and
+    the shallow levels: 64 nodes of 8192 slots is level 6 at J = 2^19);
+    use_tc = 1: the double-buffered kernel of the deeper levels
+    (bfs_level_tc_kernel; 1024 nodes of 512 slots).  One launch reads every
+    vector once (J R 4 bytes, gathered rows) and each node's packed Gram
+    once; its tensor-core work is two TF32 MMAs per K step (2 J R^2
+    multiply-adds).  CUDA events on the launching stream, the average of
+    `launches` launches after two warm-up launches; inputs (J R 4 bytes,
+    268 MB at J = 2^19, R = 128) larger than L2."""
     import torch
 
     from rdist_tensor_gb300 import _lib
@@ -204,7 +211,7 @@ def level_kernel_roofline(R, J, nodes=1024, launches=5, seed=0):
     q = torch.empty(J, dtype=torch.float32, device="cuda")
     st = torch.cuda.current_stream()
     args = (R, J, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(node.data_ptr()), ctypes.c_void_p(G.data_ptr()),
-            ctypes.c_void_p(q.data_ptr()), 1, ctypes.c_void_p(st.cuda_stream))
+            ctypes.c_void_p(q.data_ptr()), use_tc, ctypes.c_void_p(st.cuda_stream))
     for _ in range(2):
         _lib.call("exafac_quad_forms_f32", *args)
     torch.cuda.synchronize()
@@ -219,10 +226,12 @@ def level_kernel_roofline(R, J, nodes=1024, launches=5, seed=0):
     algo = J * R * 4 + used * Pf * 4
     peak, peak_kind = measured_peaks()
     achieved = algo / dur / 1e9
+    name = ("bfs_level_tcr_kernel (tcgen05 quadratic forms of a descent level, node resident)" if use_tc == 2 else
+            "bfs_level_tc_kernel (tcgen05 quadratic forms of a descent level, double-buffered slots)")
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "bfs_level_tc_kernel (tcgen05 quadratic forms of a descent level)",
-            "algorithmic_bytes": algo, "duration_s": dur, "launches": launches, "peak_source": peak_kind,
-            "tensor_tflops": 2.0 * J * R * R / dur / 1e12, "J": J, "R": R, "nodes": used}
+            "traffic": None, "kernel": name, "algorithmic_bytes": algo, "duration_s": dur, "launches": launches,
+            "peak_source": peak_kind, "tensor_tflops": 2.0 * J * R * R / dur / 1e12, "J": J, "R": R,
+            "nodes": used}
 
 
 def gcp_adjoint_roofline(model, J_nz, J_z, launches=20):
@@ -626,8 +635,10 @@ def run_gpu(args, w):
     ws, rank, local = dist_init()
     torch.cuda.set_device(local)
     lib = _lib.load()
-    if args.kernel_only:  # the dominant kernel alone (for a kernel profile)
-        print(json.dumps({"roofline": level_kernel_roofline(w["R"], w["J"])}), flush=True)
+    if args.kernel_only:  # the level kernels alone (for a kernel profile): resident-node, then double-buffered
+        print(json.dumps({"roofline": level_kernel_roofline(w["R"], w["J"]),
+                          "roofline_deep_levels": level_kernel_roofline(w["R"], w["J"], nodes=1024, use_tc=1)}),
+              flush=True)
         return 0
     dims, idx, vals = make_workload(w, seed=args.seed + rank)
     N, R, J = len(dims), w["R"], w["J"]
@@ -791,10 +802,11 @@ def run_gpu(args, w):
                 "units_per_step": [{"unique_samples": a, "hits": b, "touched_rows": c} for a, b, c in units]}
 
     # ---- roofline of the dominant kernel (the mixed STS-CP descents') -----
-    mttkrp = None
+    mttkrp = deep = None
     if w["sampler"] == "sts_cp" and precision != "fp64" and R >= 32:
         mttkrp = roofline
         roofline = level_kernel_roofline(R, J)
+        deep = level_kernel_roofline(R, J, nodes=1024, use_tc=1)
 
     # ---- the drop-in round loop (execute_ALS_rounds, region timers on) ----
     rounds = 2
@@ -842,6 +854,7 @@ def run_gpu(args, w):
             "config": cfg, "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
     if mttkrp is not None:
         line["roofline_sampled_mttkrp"] = mttkrp
+        line["roofline_deep_levels"] = deep
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
