@@ -1298,22 +1298,34 @@ __global__ void bfs_leaf1_kernel(TreeShape t, int64_t J, const int64_t* __restri
 }
 
 // sh = h * E_next[v] and h = h * U_k[row] (row-wise products), h = 1.
+// sh[j] = h[j] * E[v[j]] and h[j] *= U[row of j], elementwise over R: a warp
+// per sample row, 16-byte accesses along the row when the rows are 16-byte
+// aligned (one multiply per element either way, as before).
+__device__ __forceinline__ void row_product(int R, const float* a, const float* __restrict__ b, float* out) {
+    const int lane = threadIdx.x & 31;
+    if ((R & 3) == 0 && (((uintptr_t)a | (uintptr_t)b | (uintptr_t)out) & 15u) == 0) {
+        for (int c = 4 * lane; c < R; c += 128) {
+            const float4 x = *reinterpret_cast<const float4*>(a + c);
+            const float4 y = __ldg(reinterpret_cast<const float4*>(b + c));
+            *reinterpret_cast<float4*>(out + c) = make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w);
+        }
+    } else {
+        for (int c = lane; c < R; c += 32) out[c] = a[c] * __ldg(b + c);
+    }
+}
+
 __global__ void bfs_scale_kernel(int R, int64_t J, const float* __restrict__ h, const float* __restrict__ Ek,
                                  const int32_t* __restrict__ v, float* __restrict__ sh) {
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < J * R; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = e / R;
-        const int r = (int)(e - j * R);
-        sh[e] = h[e] * Ek[(int64_t)v[j] * R + r];
-    }
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < J; j += nw)
+        row_product(R, h + j * R, Ek + (int64_t)v[j] * R, sh + j * R);
 }
 
 __global__ void bfs_row_update_kernel(int R, int64_t J, const float* __restrict__ Uk, const uint32_t* __restrict__ samples,
                                       int N, int col, float* __restrict__ h) {
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < J * R; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = e / R;
-        const int r = (int)(e - j * R);
-        h[e] *= Uk[(int64_t)samples[j * N + col] * R + r];
-    }
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < J; j += nw)
+        row_product(R, h + j * R, Uk + (int64_t)samples[j * N + col] * R, h + j * R);
 }
 
 __global__ void bfs_init_kernel(int R, int64_t J, float* __restrict__ h, int32_t* __restrict__ empty) {
@@ -1466,12 +1478,12 @@ int sts_draw_bfs(Session& s, int n, int64_t J, const double* uni, cudaStream_t s
         // eigen tree of mode k, driven by h: v, then sh = h * E_next[v]
         EXAFAC_TRY(bfs_descend(s, s.etree, s.eigF + (int64_t)k * s.etree.node_count * Pf, nullptr, b.h,
                                uni + ((int64_t)k * 2 + 0) * J, J, n, b.v, st));
-        bfs_scale_kernel<<<grid_for_elems(J * R), 256, 0, st>>>(R, J, b.h, Ek, b.v, b.sh);
+        bfs_scale_kernel<<<grid_for_elems(J * 32), 256, 0, st>>>(R, J, b.h, Ek, b.v, b.sh);
         count_launch();
         // row tree of mode k, driven by sh: the row, then h *= U_k[row]
         EXAFAC_TRY(bfs_descend(s, s.rtree[k], s.treeF[k], s.Uf[k], b.sh, uni + ((int64_t)k * 2 + 1) * J, J, k,
                                nullptr, st));
-        bfs_row_update_kernel<<<grid_for_elems(J * R), 256, 0, st>>>(R, J, s.Uf[k], s.samples, N, k, b.h);
+        bfs_row_update_kernel<<<grid_for_elems(J * 32), 256, 0, st>>>(R, J, s.Uf[k], s.samples, N, k, b.h);
         count_launch();
     }
     // h^T Phi h (one node: Phi), then the weights
