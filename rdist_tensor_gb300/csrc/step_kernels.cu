@@ -493,26 +493,39 @@ __global__ void __launch_bounds__(kDesignWarps * 32) design_mma_wide_kernel(int 
     const int64_t ju = *ju_dev;
     for (int64_t base = (int64_t)blockIdx.x * 32; base < ju; base += (int64_t)gridDim.x * 32) {
         const int nrow = (int)min((int64_t)32, ju - base);
+        // the sample indices of the warp's four rows for every mode (lane
+        // l < 4 N: row l / N, mode l % N) and their weights, in one round of
+        // loads before the first gather
+        int64_t myi = 0;
+        double myw = 0.0;
+        if (lane < 4 * N) {
+            const int rr = lane / N, k = lane - rr * N;
+            if (4 * w + rr < nrow) myi = sd[(base + 4 * w + rr) * N + k];
+        }
+        if (lane < 4 && 4 * w + lane < nrow) myw = wd[base + 4 * w + lane];
         for (int rr = 0; rr < 4; rr++) {
             const int r = 4 * w + rr;
             const int64_t j = base + r;
             double d[kCB];
 #pragma unroll
             for (int cb = 0; cb < kCB; cb++) d[cb] = 1.0;
-            double wj = 0.0;
-            if (r < nrow) {
-                wj = wd[j];
-                for (int k = 0; k < N; k++) {
-                    if (k == n) continue;
-                    const int64_t i = sd[j * N + k];
+            const double wj = __shfl_sync(0xffffffffu, myw, rr);
+            if (r < nrow) {  // uniform over the warp
+                // modes unrolled: the factor pointers stay in the parameter
+                // bank and a row's gathers of every mode are independent
+#pragma unroll
+                for (int k = 0; k < kMaxModes; k++) {
+                    if (k >= N || k == n) continue;
+                    const int64_t i = __shfl_sync(0xffffffffu, myi, rr * N + k);
+                    const double* ur = f.U[k] + i * R;
 #pragma unroll
                     for (int cb = 0; cb < kCB; cb++) {
                         const int c = lane + 32 * cb;
-                        if (c < R) d[cb] *= f.U[k][i * R + c];
+                        if (c < R) d[cb] *= ur[c];
                     }
                 }
             }
-            const double sw = sqrt(wj);
+            const double sw = sqrt(r < nrow ? wj : 0.0);
 #pragma unroll
             for (int cb = 0; cb < kCB; cb++) {
                 const int c = lane + 32 * cb;
