@@ -226,7 +226,8 @@ int normalize_balanced(Session& s, int n, bool arls, cudaStream_t st);
 int mttkrp_scatter_out(Session& s, double* out, cudaStream_t st);
 // 32 < R <= 128 (wide_kernels.cu): MTTKRP + solve + Gram, and renormalisation,
 // in FP64 (FP64 form) or FP32 (mixed forms).
-int mttkrp_solve_wide(Session& s, int n, cudaStream_t st);
+// before_solve (may be null): an event the solve waits for (the pseudo-inverse).
+int mttkrp_solve_wide(Session& s, int n, cudaStream_t st, cudaEvent_t before_solve = nullptr);
 int normalize_wide(Session& s, int n, bool arls, cudaStream_t st);
 int spmm_solve(Session& s, int n, cudaStream_t st);
 int spmm_solve_into(Session& s, int n, const double* Phi, double* out, cudaStream_t st);

@@ -270,6 +270,10 @@ struct exafac_als_s {
     // on the caller's stream).
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // recorded on the side stream once the design rows are written (before
+    // their Gram's pseudo-inverse): the wide MTTKRP needs the rows only, the
+    // solve after it the pseudo-inverse (join)
+    cudaEvent_t rows_ready = nullptr;
     // and, queued after it, the clearing of the factor rows the previous
     // update of the mode wrote and this one does not (disjoint from the rows
     // the update writes), beside the MTTKRP and solve; joined before the
@@ -293,6 +297,7 @@ struct exafac_als_s {
                 if (e) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
+        if (rows_ready) cudaEventDestroy(rows_ready);
         if (fork2) cudaEventDestroy(fork2);
         if (join2) cudaEventDestroy(join2);
         if (side) cudaStreamDestroy(side);
@@ -305,19 +310,21 @@ struct exafac_als_s {
 // Launches the design rows, their Gram and its pseudo-inverse on the side
 // stream after the work already queued on st (the deduplicated samples):
 // they need nothing of the fibre lookup and hit grouping that st runs next,
-// and those write nothing they read.  st must wait on h->join before reading
-// the design rows or Phi.
+// and those write nothing they read.  st must wait on h->rows_ready before
+// reading the design rows and on h->join before reading the pseudo-inverse.
 static int fork_design(exafac_als_s* h, int n, int64_t J, cudaStream_t st) {
     if (!h->side) {
         EXAFAC_CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
+        EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->rows_ready, cudaEventDisableTiming));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->fork2, cudaEventDisableTiming));
         EXAFAC_CUDA_TRY(cudaEventCreateWithFlags(&h->join2, cudaEventDisableTiming));
     }
     EXAFAC_CUDA_TRY(cudaEventRecord(h->fork, st));
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork, 0));
     EXAFAC_TRY(design_gram(h->s, n, J, h->side));
+    EXAFAC_CUDA_TRY(cudaEventRecord(h->rows_ready, h->side));
     EXAFAC_TRY(design_pinv(h->s, h->side));
     EXAFAC_CUDA_TRY(cudaEventRecord(h->join, h->side));
     return EXAFAC_OK;
@@ -523,9 +530,14 @@ extern "C" int exafac_als_step(exafac_als_t h, int32_t n, int64_t J, const doubl
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(h->side, h->fork2, 0));
     EXAFAC_TRY(zero_old_rows(s, n, h->side));
     EXAFAC_CUDA_TRY(cudaEventRecord(h->join2, h->side));
-    EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join, 0));
-    if (tiled) EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
-    else EXAFAC_TRY(mttkrp_solve_wide(s, n, st));
+    if (tiled) {
+        EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join, 0));
+        EXAFAC_TRY(mttkrp_solve_balanced(s, n, st));
+    } else {
+        // the MTTKRP rows beside the pseudo-inverse, which only the solve reads
+        EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->rows_ready, 0));
+        EXAFAC_TRY(mttkrp_solve_wide(s, n, st, h->join));
+    }
     // the old rows are cleared (the renormalisation may rescale every row)
     EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, h->join2, 0));
     EXAFAC_TRY(mark(h, 3, st));

@@ -464,7 +464,7 @@ static int wide_normalize(Session& s, int n, bool arls, cudaStream_t st) {
 }
 
 template <typename T>
-static int wide_step(Session& s, int n, cudaStream_t st) {
+static int wide_step(Session& s, int n, cudaStream_t st, cudaEvent_t before_solve) {
     const int CB = (s.R + 31) / 32;
     switch (CB) {
         case 2: EXAFAC_TRY((wide_mttkrp<T, 2>(s, st))); break;
@@ -472,6 +472,7 @@ static int wide_step(Session& s, int n, cudaStream_t st) {
         default: EXAFAC_TRY((wide_mttkrp<T, 4>(s, st))); break;
     }
     EXAFAC_TRY(clear_dense_factor(s, n, st));  // a never-updated factor is cleared before the writes
+    if (before_solve) EXAFAC_CUDA_TRY(cudaStreamWaitEvent(st, before_solve, 0));
     switch (CB) {
         case 2: return wide_solve<T, 2>(s, n, st);
         case 3: return wide_solve<T, 3>(s, n, st);
@@ -489,9 +490,9 @@ static int wide_norm(Session& s, int n, bool arls, cudaStream_t st) {
     }
 }
 
-int mttkrp_solve_wide(Session& s, int n, cudaStream_t st) {
-    if (s.cfg.precision == EXAFAC_PREC_FP64) return wide_step<double>(s, n, st);
-    return wide_step<float>(s, n, st);
+int mttkrp_solve_wide(Session& s, int n, cudaStream_t st, cudaEvent_t before_solve) {
+    if (s.cfg.precision == EXAFAC_PREC_FP64) return wide_step<double>(s, n, st, before_solve);
+    return wide_step<float>(s, n, st, before_solve);
 }
 
 int normalize_wide(Session& s, int n, bool arls, cudaStream_t st) {
