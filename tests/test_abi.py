@@ -84,3 +84,39 @@ def test_grid_shim_rejects_multi_rank():
     assert g.get_dimension() == 3
     with pytest.raises(RuntimeError, match="number of MPI ranks"):
         Grid(np.array([2, 1, 1], dtype=np.int32))
+
+
+def test_adam_and_quad_forms_argument_errors(lib):
+    """Host-side checks of the fused Adam step and the quadratic-forms entry
+    (they return before any device work)."""
+    P = ctypes.c_void_p
+    one = (ctypes.c_int64 * 1)(4)
+    ptrs = (ctypes.c_void_p * 1)(None)
+    adam = lib.exafac_adam_step
+    assert adam(9, ptrs, None, ptrs, ptrs, one, 0, 1e-2, 0.9, 0.999, 1e-8, 1, 1, 0.0, None) == 1
+    assert b"count" in lib.exafac_last_error()
+    assert adam(1, ptrs, None, ptrs, ptrs, one, 0, 1e-2, 0.9, 0.999, 1e-8, 0, 1, 0.0, None) == 1
+    assert b"step" in lib.exafac_last_error()
+    assert adam(1, ptrs, None, ptrs, ptrs, one, 0, 1e-2, 1.0, 0.999, 1e-8, 1, 1, 0.0, None) == 1
+    assert b"betas" in lib.exafac_last_error()
+    assert adam(1, ptrs, None, ptrs, ptrs, one, 2, 1e-2, 0.9, 0.999, 1e-8, 1, 1, 0.0, None) == 1
+    assert adam(1, ptrs, None, ptrs, ptrs, one, 0, 1e-2, 0.9, 0.999, 1e-8, 1, 1, 0.0, None) == 1  # null tensors
+    assert adam(0, None, None, None, None, None, 0, 1e-2, 0.9, 0.999, 1e-8, 1, 1, 0.0, None) == 0  # nothing to do
+    quad = lib.exafac_quad_forms_f32
+    buf = (ctypes.c_float * 4)()
+    p = ctypes.cast(buf, P)
+    assert quad(64, 128, None, None, None, None, 1, None) == 1
+    assert quad(64, 128, p, p, p, p, 3, None) == 1
+    assert b"use_tc" in lib.exafac_last_error()
+    assert quad(16, 128, p, p, p, p, 2, None) == 1
+    assert b"R >= 32" in lib.exafac_last_error()
+
+
+def test_fused_adam_refuses_host_tensors():
+    torch = pytest.importorskip("torch")
+    from rdist_tensor_gb300 import gcp
+
+    with pytest.raises(ValueError, match="CUDA"):
+        gcp.FusedAdam([torch.zeros(4)])
+    with pytest.raises(ValueError, match="1 to 8"):
+        gcp.FusedAdam([])
