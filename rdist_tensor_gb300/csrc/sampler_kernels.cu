@@ -302,19 +302,14 @@ static int narrow_copy(const double* in, float* out, int64_t n, cudaStream_t st)
 // Pf, the padding zeroed.
 __global__ void narrow_nodes_kernel(const double* __restrict__ in, int P, float* __restrict__ out, int Pf,
                                     int64_t nodes) {
-    const int64_t total = nodes * Pf;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = i / Pf;
-        const int e = (int)(i - c * Pf);
-        out[i] = e < P ? narrow_f64(in[c * P + e]) : 0.0f;
-    }
+    for (int64_t c = blockIdx.x; c < nodes; c += gridDim.x)  // a block per node, threads along it
+        for (int e = threadIdx.x; e < Pf; e += blockDim.x) out[c * Pf + e] = e < P ? narrow_f64(in[c * P + e]) : 0.0f;
 }
 
 static int narrow_nodes(const double* in, float* out, int R, int64_t nodes, cudaStream_t st) {
     const int P = packed_size(R), Pf = packed_stride_f32(R);
     if (nodes <= 0) return EXAFAC_OK;
-    narrow_nodes_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nodes * Pf, 256), 152 * 16), 256, 0, st>>>(in, P, out,
-                                                                                                         Pf, nodes);
+    narrow_nodes_kernel<<<(unsigned)std::min<int64_t>(nodes, 152 * 16), 256, 0, st>>>(in, P, out, Pf, nodes);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
@@ -389,38 +384,32 @@ __global__ void sts_emat_kernel(int N, int n, int R, const double* __restrict__ 
 // over the GPU: one launch for the leaves of every sampled mode, one per
 // level for the sums, one for the products.
 
-// Row a of packed index e (R x R upper triangle, rows in order).
-__device__ __forceinline__ int packed_row(int R, int e) {
-    const double b = 2.0 * R + 1.0;
-    int a = (int)((b - sqrt(b * b - 8.0 * e)) * 0.5);
-    if (a < 0) a = 0;
-    if (a > R - 1) a = R - 1;
-    while (a > 0 && packed_index(R, a, a) > e) a--;
-    while (a + 1 < R && packed_index(R, a + 1, a + 1) <= e) a++;
-    return a;
-}
-
 __device__ __forceinline__ int eigen_next(int N, int n, int k) {
     int nxt = k + 1;
     if (nxt == n) nxt++;
     return nxt > N ? N : nxt;
 }
 
+// The leaves' packed outer products: a warp per packed row a of one leaf of
+// one sampled mode, its lanes along the row (b = a .. R - 1).
 __global__ void eigen_leaves_kernel(int N, int n, int R, TreeShape t, const double* __restrict__ E,
                                     double* __restrict__ eigG) {
     const int P = packed_size(R);
     const int64_t first_leaf = t.node_count - t.leaf_count;
-    const int64_t per_mode = t.leaf_count * P;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)N * per_mode;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(i / per_mode);
+    const int64_t rows = (int64_t)N * t.leaf_count * R;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < rows; q += nw) {
+        const int k = (int)(q / (t.leaf_count * R));
         if (k == n) continue;
-        const int64_t li = (i % per_mode) / P;
-        const int e = (int)(i % P);
-        const int a = packed_row(R, e), b = a + (e - packed_index(R, a, a));
+        const int64_t rem = q - (int64_t)k * t.leaf_count * R;
+        const int64_t li = rem / R;
+        const int a = (int)(rem - li * R);
         const double* Ek = E + (int64_t)eigen_next(N, n, k) * R * R;
         const int64_t v = tree_leaf_idx(t, first_leaf + li);
-        eigG[((int64_t)k * t.node_count + first_leaf + li) * P + e] = Ek[v * R + a] * Ek[v * R + b];
+        const double xa = Ek[v * R + a];
+        double* out = eigG + ((int64_t)k * t.node_count + first_leaf + li) * P + packed_index(R, a, a);
+        for (int b = a + lane; b < R; b += 32) out[b - a] = xa * Ek[v * R + b];
     }
 }
 
@@ -439,17 +428,23 @@ __global__ void eigen_level_kernel(int N, int n, int P, TreeShape t, int64_t sta
     }
 }
 
+// Every node times its mode's Gram, elementwise: a warp per packed row a of
+// one node of one sampled mode, its lanes along the row.
 __global__ void eigen_hadamard_kernel(int N, int n, int R, TreeShape t, const double* __restrict__ gram,
                                       double* __restrict__ eigG) {
     const int P = packed_size(R);
-    const int64_t per_mode = t.node_count * P;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)N * per_mode;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(i / per_mode);
+    const int64_t rows = (int64_t)N * t.node_count * R;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < rows; q += nw) {
+        const int k = (int)(q / (t.node_count * R));
         if (k == n) continue;
-        const int e = (int)(i % P);
-        const int a = packed_row(R, e), b = a + (e - packed_index(R, a, a));
-        eigG[i] *= gram[(int64_t)k * R * R + a * R + b];
+        const int64_t rem = q - (int64_t)k * t.node_count * R;
+        const int64_t c = rem / R;
+        const int a = (int)(rem - c * R);
+        double* G = eigG + ((int64_t)k * t.node_count + c) * P + packed_index(R, a, a);
+        const double* g = gram + (int64_t)k * R * R + (int64_t)a * R;
+        for (int b = a + lane; b < R; b += 32) G[b - a] *= g[b];
     }
 }
 
@@ -457,7 +452,7 @@ static int build_eigen_trees(Session& s, int n, cudaStream_t st) {
     const int N = s.N, R = s.R, P = s.P;
     const TreeShape& t = s.etree;
     auto grid = [](int64_t work) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(work, 256), 152 * 16)); };
-    eigen_leaves_kernel<<<grid((int64_t)N * t.leaf_count * P), 256, 0, st>>>(N, n, R, t, s.Emat, s.eigG);
+    eigen_leaves_kernel<<<grid((int64_t)N * t.leaf_count * R * 32), 256, 0, st>>>(N, n, R, t, s.Emat, s.eigG);
     count_launch();
     int64_t start = t.nodes_before_lfill, end = t.node_count - t.leaf_count;
     for (int64_t lvl = t.lfill_level; lvl >= 0; lvl--) {
@@ -468,7 +463,7 @@ static int build_eigen_trees(Session& s, int n, cudaStream_t st) {
         end = start;
         start = ((start + 1) / 2) - 1;
     }
-    eigen_hadamard_kernel<<<grid((int64_t)N * t.node_count * P), 256, 0, st>>>(N, n, R, t, s.gram, s.eigG);
+    eigen_hadamard_kernel<<<grid((int64_t)N * t.node_count * R * 32), 256, 0, st>>>(N, n, R, t, s.gram, s.eigG);
     count_launch();
     EXAFAC_CHECK_LAUNCH();
     return EXAFAC_OK;
